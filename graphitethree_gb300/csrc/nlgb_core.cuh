@@ -1,0 +1,514 @@
+// nlgb_core.cuh -- device-side building blocks of the Jacobi-PCG solvers.
+//
+// The reference's hot loop is OpenNL's nlSolveSystemIterative(NL_CG) with a
+// Jacobi preconditioner (called from src/lib/OGF/scene_graph/NL/matrix.cpp:
+// 364,390-393 and, through nlSolve, from plugins/OGF/WarpDrive/commands/
+// voxel_grob_transport_commands.cpp:281).  Per iteration it does one CRS SpMV
+// (nlMultMatrixVector), two dot products and three axpy-like vector updates.
+//
+// Here every system is cut into fixed "tiles" of `tile_rows` consecutive rows.
+// A tile is always processed by one 256-thread CTA with one fixed thread
+// mapping, and every scalar (p.q, r.z, r.r) is the canonical reduction of the
+// per-tile partials.  Because the summation order depends only on the system
+// (its n, tile_rows and threads-per-row), the plain one-kernel-per-phase
+// solver, the batched persistent kernel and the server all produce
+// bit-identical iterates for the same system, whatever else is in the batch.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace nlgb {
+
+constexpr int kCTA = 256;            // threads per CTA for every solver kernel
+constexpr int kWarps = kCTA / 32;
+constexpr int kParts = 4;            // partial-sum slots per tile
+
+enum : int {
+  ST_RUNNING = 0,
+  ST_CONVERGED = 1,
+  ST_MAX_ITER = 2,
+  ST_BREAKDOWN = 3,
+  ST_STAGNATION = 4,
+  ST_DEVICE_ERR = 5,
+  ST_BAD_INPUT = 6,
+  ST_ABORTED = 7,
+};
+
+// Device-resident scalar state of one system (one per system, in HBM).
+struct __align__(16) SysState {
+  double rho, alpha, beta;     // CG scalars (FP64 in both precisions)
+  double bnorm2;               // ||b||^2
+  double thresh2;              // eps^2 (outer / plain)
+  double rr;                   // last ||r||^2 (recursive residual)
+  double rr_true;              // ||b - A x||^2 recomputed in FP64 at the end
+  double rr64_prev;            // mixed: previous outer true residual^2
+  double in_rr0;               // mixed: ||r||^2 at the start of the inner solve
+  double in_thresh2;           // mixed: inner eps^2
+  long long iter;              // CG iterations performed (inner ones, mixed)
+  long long max_iter;
+  long long guard;             // body passes executed (termination guard)
+  long long guard_cap;
+  int status;                  // ST_*
+  int mode;                    // mixed: 0 = an outer step is due, 1 = inner PCG
+  int outer, max_outer;        // mixed refinement steps
+  int in_iter, in_max;         // mixed inner iterations in this outer step
+  int zero_rhs;                // b == 0: the solution is x = 0
+  int stall;                   // mixed: outer steps in a row without progress
+  unsigned int cnt[4];         // last-CTA counters of the phase kernels
+};
+
+// Everything a tile procedure needs about one system.
+struct SysView {
+  int n;                 // rows (== columns)
+  int tile_rows;         // rows per tile (multiple of 512)
+  int n_tiles;
+  int tpr;               // threads per row used by the SpMV (1..32)
+  const int* rp;         // CRS row pointers (n+1)
+  const int* ci;         // CRS column indices
+  const double* va;      // FP64 values
+  const float* va32;     // FP32 values (mixed), may be null
+  const double* dinv;    // Jacobi: 1/diag (1 where diag == 0)
+  const float* dinv32;
+  const double* b;
+  double* x;
+  double* r;
+  double* p;
+  double* q;
+  float* r32;
+  float* p32;
+  float* q32;
+  float* c32;            // mixed: correction accumulated by the inner PCG
+  double* part;          // n_tiles * kParts tile partials
+  SysState* st;
+  const volatile int* abort_flag;   // host-mapped; nonzero -> stop
+};
+
+// ---------------------------------------------------------------------------
+// Reductions with a fixed order.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block sum of up to 4 values at once; result broadcast to all threads.
+template <int K>
+__device__ __forceinline__ void block_sum(double (&v)[K]) {
+  __shared__ double red[K][kWarps];
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
+  __syncthreads();   // protect red[] from a previous use
+  if (l == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) red[k][w] = v[k];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < kWarps; ++i) s += red[k][i];
+    v[k] = s;
+  }
+}
+
+// Canonical reduction of component `comp` of the tile partials (strided by
+// kParts): thread t sums tiles t, t+256, ... in order, then block_sum.
+template <int K>
+__device__ __forceinline__ void canon_reduce(const double* part, int n_tiles,
+                                             const int (&comp)[K], double (&out)[K]) {
+#pragma unroll
+  for (int k = 0; k < K; ++k) out[k] = 0.0;
+  for (int t = threadIdx.x; t < n_tiles; t += kCTA) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) out[k] += __ldcg(part + (size_t)t * kParts + comp[k]);
+  }
+  block_sum<K>(out);
+}
+
+// Sub-warp sum over T lanes (butterfly: every lane ends with the same value).
+template <int T, typename A>
+__device__ __forceinline__ A subwarp_sum(A v) {
+#pragma unroll
+  for (int o = T / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// Row dot product a_row . x with T threads per row.  All 32 lanes of the warp
+// must call it (the shuffles use the full mask); `valid` masks the loads.
+// kCoh: gather x through L2 only (needed when x was written earlier in the
+// same kernel by another CTA, i.e. in the persistent batched kernel).
+// ---------------------------------------------------------------------------
+template <int T, typename VT, typename XT, typename A, bool kCoh = false>
+__device__ __forceinline__ A row_dot(const int* __restrict__ rp, const int* __restrict__ ci,
+                                     const VT* __restrict__ va, const XT* __restrict__ x,
+                                     int row, bool valid, int lane) {
+  A sum = A(0);
+  if (valid) {
+    const int k0 = __ldg(rp + row), k1 = __ldg(rp + row + 1);
+#pragma unroll 2
+    for (int k = k0 + lane; k < k1; k += T) {
+      const int c = __ldg(ci + k);
+      const XT xc = kCoh ? __ldcg(x + c) : __ldg(x + c);
+      sum = fma(A(__ldg(va + k)), A(xc), sum);
+    }
+  }
+  return subwarp_sum<T, A>(sum);
+}
+
+__device__ __forceinline__ int tile_lo(const SysView& s, int tile) { return tile * s.tile_rows; }
+__device__ __forceinline__ int tile_hi(const SysView& s, int tile) {
+  const int h = (tile + 1) * s.tile_rows;
+  return h < s.n ? h : s.n;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 tile procedures (plain form).
+// ---------------------------------------------------------------------------
+
+// q = A p on the tile; returns (block-wide) sum_i p_i q_i.
+template <int T, bool kCoh = false>
+__device__ double tile_spmv_pq(const SysView& s, int tile) {
+  const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
+  const int sub = threadIdx.x / T, lane = threadIdx.x % T;
+  constexpr int RPP = kCTA / T;  // rows per pass
+  double acc[1] = {0.0};
+  for (int base = lo; base < hi; base += RPP) {
+    const int row = base + sub;
+    const bool valid = row < hi;
+    const double qv = row_dot<T, double, double, double, kCoh>(s.rp, s.ci, s.va, s.p, row, valid, lane);
+    if (valid && lane == 0) {
+      s.q[row] = qv;
+      acc[0] = fma(__ldcg(s.p + row), qv, acc[0]);
+    }
+  }
+  block_sum<1>(acc);
+  return acc[0];
+}
+
+// r = b - A x, p = D^-1 r on the tile; returns (b.b, r.D^-1 r, r.r).
+template <int T, bool kCoh = false>
+__device__ void tile_residual(const SysView& s, int tile, double (&out)[3]) {
+  const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
+  const int sub = threadIdx.x / T, lane = threadIdx.x % T;
+  constexpr int RPP = kCTA / T;
+  out[0] = out[1] = out[2] = 0.0;
+  for (int base = lo; base < hi; base += RPP) {
+    const int row = base + sub;
+    const bool valid = row < hi;
+    const double ax = row_dot<T, double, double, double, kCoh>(s.rp, s.ci, s.va, s.x, row, valid, lane);
+    if (valid && lane == 0) {
+      const double bi = s.b[row];
+      const double ri = bi - ax;
+      const double zi = s.dinv[row] * ri;
+      s.r[row] = ri;
+      s.p[row] = zi;
+      out[0] = fma(bi, bi, out[0]);
+      out[1] = fma(zi, ri, out[1]);
+      out[2] = fma(ri, ri, out[2]);
+    }
+  }
+  block_sum<3>(out);
+}
+
+// Vector-phase loop helper: pairs of rows with 16-byte loads.  Row pairs
+// [lo, hi) with lo even; an odd tail row is handled by thread 0 last.
+template <typename F2, typename F1>
+__device__ __forceinline__ void pair_loop(int lo, int hi, F2&& body2, F1&& body1) {
+  const int p0 = lo >> 1, p1 = hi >> 1;
+  for (int i2 = p0 + threadIdx.x; i2 < p1; i2 += kCTA) body2(i2);
+  if ((hi & 1) && threadIdx.x == 0) body1(hi - 1);
+}
+
+// x += a p, r -= a q; returns (r.D^-1 r, r.r).
+__device__ __forceinline__ void tile_update_xr(const SysView& s, int tile, double alpha,
+                                               double (&out)[2]) {
+  const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
+  double rz = 0.0, rr = 0.0;
+  double2* x2 = reinterpret_cast<double2*>(s.x);
+  double2* r2 = reinterpret_cast<double2*>(s.r);
+  const double2* p2 = reinterpret_cast<const double2*>(s.p);
+  const double2* q2 = reinterpret_cast<const double2*>(s.q);
+  const double2* d2 = reinterpret_cast<const double2*>(s.dinv);
+  pair_loop(lo, hi,
+    [&](int i2) {
+      double2 xv = __ldcg(x2 + i2), rv = __ldcg(r2 + i2);
+      const double2 pv = __ldcg(p2 + i2), qv = __ldcg(q2 + i2), dv = __ldg(d2 + i2);
+      xv.x = fma(alpha, pv.x, xv.x); xv.y = fma(alpha, pv.y, xv.y);
+      rv.x = fma(-alpha, qv.x, rv.x); rv.y = fma(-alpha, qv.y, rv.y);
+      x2[i2] = xv; r2[i2] = rv;
+      const double zx = dv.x * rv.x, zy = dv.y * rv.y;
+      rz = fma(zx, rv.x, rz); rz = fma(zy, rv.y, rz);
+      rr = fma(rv.x, rv.x, rr); rr = fma(rv.y, rv.y, rr);
+    },
+    [&](int i) {
+      s.x[i] = fma(alpha, __ldcg(s.p + i), __ldcg(s.x + i));
+      const double ri = fma(-alpha, __ldcg(s.q + i), __ldcg(s.r + i));
+      s.r[i] = ri;
+      rz = fma(s.dinv[i] * ri, ri, rz);
+      rr = fma(ri, ri, rr);
+    });
+  out[0] = rz; out[1] = rr;
+  block_sum<2>(out);
+}
+
+// p = D^-1 r + beta p.
+__device__ __forceinline__ void tile_update_p(const SysView& s, int tile, double beta) {
+  const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
+  double2* p2 = reinterpret_cast<double2*>(s.p);
+  const double2* r2 = reinterpret_cast<const double2*>(s.r);
+  const double2* d2 = reinterpret_cast<const double2*>(s.dinv);
+  pair_loop(lo, hi,
+    [&](int i2) {
+      const double2 rv = __ldcg(r2 + i2), dv = __ldg(d2 + i2);
+      double2 pv = __ldcg(p2 + i2);
+      pv.x = fma(beta, pv.x, dv.x * rv.x);
+      pv.y = fma(beta, pv.y, dv.y * rv.y);
+      p2[i2] = pv;
+    },
+    [&](int i) {
+      s.p[i] = fma(beta, __ldcg(s.p + i), s.dinv[i] * __ldcg(s.r + i));
+    });
+}
+
+// Zero x on the tile (used when b == 0).
+__device__ __forceinline__ void tile_zero_x(const SysView& s, int tile) {
+  const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
+  for (int i = lo + threadIdx.x; i < hi; i += kCTA) s.x[i] = 0.0;
+}
+
+// ||b - A x||^2 on the tile, without writing anything.
+template <int T, bool kCoh = false>
+__device__ double tile_true_rr(const SysView& s, int tile) {
+  const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
+  const int sub = threadIdx.x / T, lane = threadIdx.x % T;
+  constexpr int RPP = kCTA / T;
+  double acc[1] = {0.0};
+  for (int base = lo; base < hi; base += RPP) {
+    const int row = base + sub;
+    const bool valid = row < hi;
+    const double ax = row_dot<T, double, double, double, kCoh>(s.rp, s.ci, s.va, s.x, row, valid, lane);
+    if (valid && lane == 0) {
+      const double ri = s.b[row] - ax;
+      acc[0] = fma(ri, ri, acc[0]);
+    }
+  }
+  block_sum<1>(acc);
+  return acc[0];
+}
+
+// ---------------------------------------------------------------------------
+// Mixed-precision tile procedures: FP32 matrix values and Krylov vectors,
+// FP64 for the outer residual, the solution update and the accumulation of
+// every dot product that feeds alpha / beta.
+// ---------------------------------------------------------------------------
+
+// x += c (FP64 update from the FP32 correction), c = 0.
+__device__ __forceinline__ void tile_mx_apply(const SysView& s, int tile) {
+  const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
+  double2* x2 = reinterpret_cast<double2*>(s.x);
+  float2* c2 = reinterpret_cast<float2*>(s.c32);
+  pair_loop(lo, hi,
+    [&](int i2) {
+      double2 xv = __ldcg(x2 + i2);
+      const float2 cv = __ldcg(c2 + i2);
+      xv.x += double(cv.x); xv.y += double(cv.y);
+      x2[i2] = xv;
+      c2[i2] = make_float2(0.f, 0.f);
+    },
+    [&](int i) {
+      s.x[i] = __ldcg(s.x + i) + double(__ldcg(s.c32 + i));
+      s.c32[i] = 0.f;
+    });
+}
+
+// Outer step: r64 = b - A64 x (FP64), r32 = float(r64), p32 = D^-1 r32.
+// Returns (b.b, ||r64||^2, r32.z32, ||r32||^2) -- all accumulated in FP64.
+template <int T, bool kCoh = false>
+__device__ void tile_mx_outer(const SysView& s, int tile, double (&out)[4]) {
+  const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
+  const int sub = threadIdx.x / T, lane = threadIdx.x % T;
+  constexpr int RPP = kCTA / T;
+  out[0] = out[1] = out[2] = out[3] = 0.0;
+  for (int base = lo; base < hi; base += RPP) {
+    const int row = base + sub;
+    const bool valid = row < hi;
+    const double ax = row_dot<T, double, double, double, kCoh>(s.rp, s.ci, s.va, s.x, row, valid, lane);
+    if (valid && lane == 0) {
+      const double bi = s.b[row];
+      const double ri = bi - ax;
+      const float r32 = float(ri);
+      const float z32 = s.dinv32[row] * r32;
+      s.r32[row] = r32;
+      s.p32[row] = z32;
+      out[0] = fma(bi, bi, out[0]);
+      out[1] = fma(ri, ri, out[1]);
+      out[2] = fma(double(z32), double(r32), out[2]);
+      out[3] = fma(double(r32), double(r32), out[3]);
+    }
+  }
+  block_sum<4>(out);
+}
+
+// q32 = A32 p32 (FP32 row sums); returns sum p.q accumulated in FP64.
+template <int T, bool kCoh = false>
+__device__ double tile_mx_spmv_pq(const SysView& s, int tile) {
+  const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
+  const int sub = threadIdx.x / T, lane = threadIdx.x % T;
+  constexpr int RPP = kCTA / T;
+  double acc[1] = {0.0};
+  for (int base = lo; base < hi; base += RPP) {
+    const int row = base + sub;
+    const bool valid = row < hi;
+    const float qv = row_dot<T, float, float, float, kCoh>(s.rp, s.ci, s.va32, s.p32, row, valid, lane);
+    if (valid && lane == 0) {
+      s.q32[row] = qv;
+      acc[0] = fma(double(__ldcg(s.p32 + row)), double(qv), acc[0]);
+    }
+  }
+  block_sum<1>(acc);
+  return acc[0];
+}
+
+// c32 += a p32, r32 -= a q32 (FP32 arithmetic, alpha from FP64);
+// returns (r.D^-1 r, r.r) accumulated in FP64.
+__device__ __forceinline__ void tile_mx_update_cr(const SysView& s, int tile, double alpha,
+                                                  double (&out)[2]) {
+  const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
+  const float a = float(alpha);
+  double rz = 0.0, rr = 0.0;
+  float2* c2 = reinterpret_cast<float2*>(s.c32);
+  float2* r2 = reinterpret_cast<float2*>(s.r32);
+  const float2* p2 = reinterpret_cast<const float2*>(s.p32);
+  const float2* q2 = reinterpret_cast<const float2*>(s.q32);
+  const float2* d2 = reinterpret_cast<const float2*>(s.dinv32);
+  pair_loop(lo, hi,
+    [&](int i2) {
+      float2 cv = __ldcg(c2 + i2), rv = __ldcg(r2 + i2);
+      const float2 pv = __ldcg(p2 + i2), qv = __ldcg(q2 + i2), dv = __ldg(d2 + i2);
+      cv.x = fmaf(a, pv.x, cv.x); cv.y = fmaf(a, pv.y, cv.y);
+      rv.x = fmaf(-a, qv.x, rv.x); rv.y = fmaf(-a, qv.y, rv.y);
+      c2[i2] = cv; r2[i2] = rv;
+      const float zx = dv.x * rv.x, zy = dv.y * rv.y;
+      rz = fma(double(zx), double(rv.x), rz); rz = fma(double(zy), double(rv.y), rz);
+      rr = fma(double(rv.x), double(rv.x), rr); rr = fma(double(rv.y), double(rv.y), rr);
+    },
+    [&](int i) {
+      s.c32[i] = fmaf(a, __ldcg(s.p32 + i), __ldcg(s.c32 + i));
+      const float ri = fmaf(-a, __ldcg(s.q32 + i), __ldcg(s.r32 + i));
+      s.r32[i] = ri;
+      const float zi = s.dinv32[i] * ri;
+      rz = fma(double(zi), double(ri), rz);
+      rr = fma(double(ri), double(ri), rr);
+    });
+  out[0] = rz; out[1] = rr;
+  block_sum<2>(out);
+}
+
+// p32 = D^-1 r32 + beta p32.
+__device__ __forceinline__ void tile_mx_update_p(const SysView& s, int tile, double beta) {
+  const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
+  const float bt = float(beta);
+  float2* p2 = reinterpret_cast<float2*>(s.p32);
+  const float2* r2 = reinterpret_cast<const float2*>(s.r32);
+  const float2* d2 = reinterpret_cast<const float2*>(s.dinv32);
+  pair_loop(lo, hi,
+    [&](int i2) {
+      const float2 rv = __ldcg(r2 + i2), dv = __ldg(d2 + i2);
+      float2 pv = __ldcg(p2 + i2);
+      pv.x = fmaf(bt, pv.x, dv.x * rv.x);
+      pv.y = fmaf(bt, pv.y, dv.y * rv.y);
+      p2[i2] = pv;
+    },
+    [&](int i) {
+      s.p32[i] = fmaf(bt, __ldcg(s.p32 + i), s.dinv32[i] * __ldcg(s.r32 + i));
+    });
+}
+
+// ---------------------------------------------------------------------------
+// Scalar steps (run by one thread once all tile partials of a phase are in).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool finite_pos(double v) { return v > 0.0 && v < 1.0e300; }
+
+// After the initial residual: decide whether any iteration is needed.
+__device__ __forceinline__ void scalar_after_init(SysState* st, double bb, double rz, double rr) {
+  st->bnorm2 = bb;
+  st->rho = rz;
+  st->rr = rr;
+  st->iter = 0;
+  if (!(bb > 0.0)) {             // b == 0 (or NaN): x = 0 is the solution
+    st->zero_rhs = (bb == 0.0);
+    st->status = (bb == 0.0) ? ST_CONVERGED : ST_BREAKDOWN;
+    return;
+  }
+  if (!(rr <= 1.0e300)) { st->status = ST_BREAKDOWN; return; }
+  if (rr <= st->thresh2 * bb) { st->status = ST_CONVERGED; return; }
+  if (st->max_iter <= 0) { st->status = ST_MAX_ITER; return; }
+  if (!finite_pos(rz)) { st->status = ST_BREAKDOWN; return; }
+}
+
+__device__ __forceinline__ void scalar_after_pq(SysState* st, double pq) {
+  if (!finite_pos(pq)) { st->status = ST_BREAKDOWN; return; }
+  st->alpha = st->rho / pq;
+}
+
+__device__ __forceinline__ void scalar_after_xr(SysState* st, double rz, double rr) {
+  st->iter += 1;
+  st->rr = rr;
+  if (!(rr <= 1.0e300)) { st->status = ST_BREAKDOWN; return; }
+  if (rr <= st->thresh2 * st->bnorm2) { st->status = ST_CONVERGED; return; }
+  if (st->iter >= st->max_iter) { st->status = ST_MAX_ITER; return; }
+  if (!finite_pos(rz)) { st->status = ST_BREAKDOWN; return; }
+  st->beta = rz / st->rho;
+  st->rho = rz;
+}
+
+// Mixed: after the FP64 outer residual.  Returns through st->mode / status.
+__device__ __forceinline__ void scalar_after_outer(SysState* st, double bb, double rr64,
+                                                   double rz32, double rr32) {
+  if (st->outer == 0) st->bnorm2 = bb;
+  const double bb0 = st->bnorm2;
+  st->rr = rr64;
+  if (!(bb0 > 0.0)) {
+    st->zero_rhs = (bb0 == 0.0);
+    st->status = (bb0 == 0.0) ? ST_CONVERGED : ST_BREAKDOWN;
+    return;
+  }
+  if (!(rr64 <= 1.0e300)) { st->status = ST_BREAKDOWN; return; }
+  if (rr64 <= st->thresh2 * bb0) { st->status = ST_CONVERGED; return; }
+  if (st->iter >= st->max_iter) { st->status = ST_MAX_ITER; return; }
+  if (st->outer >= st->max_outer) { st->status = ST_STAGNATION; return; }
+  // Stagnation: three outer steps in a row without halving the residual.
+  if (st->outer > 0 && rr64 > 0.25 * st->rr64_prev) {
+    st->stall += 1;
+    if (st->stall >= 3) { st->status = ST_STAGNATION; return; }
+  } else {
+    st->stall = 0;
+  }
+  st->rr64_prev = rr64;
+  st->outer += 1;
+  if (!finite_pos(rz32) || !finite_pos(rr32)) { st->status = ST_BREAKDOWN; return; }
+  st->rho = rz32;
+  st->in_rr0 = rr32;
+  st->in_iter = 0;
+  st->mode = 1;
+}
+
+// Mixed inner: after the FP32 vector update.  mode -> 0 ends the inner solve.
+__device__ __forceinline__ void scalar_after_mx_cr(SysState* st, double rz, double rr) {
+  st->iter += 1;
+  st->in_iter += 1;
+  if (!(rr <= 1.0e300)) { st->status = ST_BREAKDOWN; return; }
+  if (rr <= st->in_thresh2 * st->in_rr0 || st->in_iter >= st->in_max ||
+      st->iter >= st->max_iter || !finite_pos(rz)) {
+    st->mode = 0;
+    return;
+  }
+  st->beta = rz / st->rho;
+  st->rho = rz;
+}
+
+}  // namespace nlgb

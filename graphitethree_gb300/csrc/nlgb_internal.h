@@ -1,0 +1,149 @@
+// nlgb_internal.h -- host-side internals shared by the translation units of
+// libnl_gb300 (not installed, not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+namespace nlgb {
+
+// Thread-local error text reported by nlGetErrorString()/nlgb_last_error().
+void set_error(const std::string& msg);
+const char* last_error();
+
+#define NLGB_CUDA_TRY(expr)                                                     \
+  do {                                                                          \
+    cudaError_t e_ = (expr);                                                    \
+    if (e_ != cudaSuccess) {                                                    \
+      ::nlgb::set_error(std::string(#expr) + ": " + cudaGetErrorString(e_));    \
+      return e_;                                                                \
+    }                                                                           \
+  } while (0)
+
+// A CRS matrix resident in GPU memory (int32 indices, FP64 values).
+struct DeviceCRS {
+  int n = 0;               // rows
+  int m = 0;               // columns
+  long long nnz = 0;
+  int* rp = nullptr;
+  int* ci = nullptr;
+  double* va = nullptr;
+  float* va32 = nullptr;   // lazily built for the mixed-precision solver
+  double* dinv = nullptr;  // Jacobi inverse diagonal (lazily built)
+  float* dinv32 = nullptr;
+  int tpr = 0;             // threads per row chosen by the autotuner
+  int tile_rows = 0;
+  int max_row = 0;         // longest row (nnz)
+  bool owns = true;        // false: a view sharing another matrix's arrays
+};
+
+cudaError_t crs_upload(DeviceCRS& A, int n, int m, const int* rp, const int* ci,
+                       const double* va, cudaStream_t s);
+cudaError_t crs_adopt_device(DeviceCRS& A, int n, int m, long long nnz, int* rp, int* ci,
+                             double* va, cudaStream_t s);
+void crs_free(DeviceCRS& A);
+cudaError_t crs_prepare(DeviceCRS& A, bool need_fp32, cudaStream_t s);  // jacobi, fp32, tuning
+long long device_bytes(const DeviceCRS& A);
+
+// Autotuner: threads per row and tile rows from the nnz-per-row histogram.
+struct TuneChoice { int tpr; int tile_rows; };
+TuneChoice autotune(int n, long long nnz, int max_row, const int* hist33);
+cudaError_t row_histogram(const DeviceCRS& A, int* hist33_host, int* max_row, cudaStream_t s);
+
+// SpMV y = A x with the autotuned layout (device pointers).
+cudaError_t spmv64(const DeviceCRS& A, const double* x, double* y, cudaStream_t s);
+cudaError_t spmv32(const DeviceCRS& A, const float* x, float* y, cudaStream_t s);
+
+struct SolveParams {
+  double eps = 1e-10;
+  long long max_iter = -1;     // -1: 5 n
+  int precision = 0;           // 0 FP64, 1 mixed
+  double inner_eps = 1e-5;
+  int max_outer = 40;
+  int tpr = 0;                 // 0: autotuned
+};
+
+struct SolveResult {
+  int status = 0;
+  long long iterations = 0;
+  int outer_steps = 0;
+  double rel_residual = 0;       // recursive (plain) / true FP64 (mixed) at stop
+  double true_rel_residual = 0;  // ||b - A x|| / ||b|| recomputed in FP64
+  double seconds = 0;
+};
+
+// Plain FP64 or mixed FP32/FP64-refined Jacobi-PCG on one resident matrix.
+// The whole iteration loop is a single CUDA-graph launch (while-conditional
+// node); the host waits once per solve.
+class PcgSolver {
+ public:
+  PcgSolver() = default;
+  ~PcgSolver();
+  PcgSolver(const PcgSolver&) = delete;
+  PcgSolver& operator=(const PcgSolver&) = delete;
+
+  cudaError_t bind(DeviceCRS* A, cudaStream_t stream);
+  // b, x: device pointers of length n (x holds the initial guess on entry).
+  cudaError_t solve(const double* b, double* x, const SolveParams& prm, SolveResult* res);
+  void set_abort_flag(const volatile int* f) { abort_flag_ = f; }
+  cudaStream_t stream() const { return stream_; }
+
+ private:
+  cudaError_t alloc(bool mixed);
+  cudaError_t build_plain_graph();
+  cudaError_t build_mixed_graph();
+  void release();
+
+  DeviceCRS* A_ = nullptr;
+  cudaStream_t stream_ = nullptr;
+  int tpr_ = 0;
+  int n_ = 0, tile_rows_ = 0, n_tiles_ = 0;
+  double *b_ = nullptr, *x_ = nullptr, *r_ = nullptr, *p_ = nullptr, *q_ = nullptr, *part_ = nullptr;
+  float *r32_ = nullptr, *p32_ = nullptr, *q32_ = nullptr, *c32_ = nullptr;
+  void* st_ = nullptr;          // SysState (device)
+  void* st_host_ = nullptr;     // pinned staging
+  const volatile int* abort_flag_ = nullptr;
+  cudaGraphExec_t plain_exec_ = nullptr, mixed_exec_ = nullptr;
+  cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+  bool mixed_alloc_ = false;
+};
+
+// Least-squares normal equations assembled on the GPU (row-merge into CRS).
+// Rows: coefficient ranges [row_ptr[r], row_ptr[r+1]) of (col, val) where
+// col >= 0 is a free-variable index and col < 0 encodes locked variable
+// (-col - 1); rhs[k * n_rows + r]; weight[r] (may be null: all 1).
+// Locked values: xl[k * n_vars + var].  Output: CRS of A^T W A over the free
+// variables and Aᵀ W (b - A_l x_l) for each of the k systems (device).
+struct LSRowsDevice {
+  long long n_rows = 0;
+  long long n_coefs = 0;
+  int n_free = 0;
+  int n_vars = 0;
+  int n_systems = 1;
+  const long long* row_ptr = nullptr;
+  const int* col = nullptr;
+  const double* val = nullptr;
+  const double* rhs = nullptr;
+  const double* weight = nullptr;
+  const double* xl = nullptr;
+};
+cudaError_t assemble_normal_equations(const LSRowsDevice& rows, DeviceCRS& out,
+                                      double* rhs_out /* k * n_free, device */,
+                                      cudaStream_t s);
+// Square (non least-squares) system: rows are the equations of the free
+// variables; locked columns move to the right-hand side.
+cudaError_t assemble_square(const LSRowsDevice& rows, DeviceCRS& out, double* rhs_out,
+                            cudaStream_t s);
+
+// Device BLAS-1 (FP64).
+cudaError_t dev_dot(const double* x, const double* y, long long n, double* out_host, cudaStream_t s);
+cudaError_t dev_axpy(long long n, double a, const double* x, double* y, cudaStream_t s);
+cudaError_t dev_scal(long long n, double a, double* x, cudaStream_t s);
+cudaError_t dev_mul(long long n, const double* x, double* y, cudaStream_t s);
+
+// Process-wide default stream of the OpenNL API (created on first use).
+cudaStream_t api_stream();
+bool is_device_pointer(const void* p);
+
+}  // namespace nlgb

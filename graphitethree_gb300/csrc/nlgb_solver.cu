@@ -1,0 +1,614 @@
+// nlgb_solver.cu -- plain FP64 and mixed FP32/FP64 Jacobi-PCG on one GPU.
+//
+// Replaces the iteration of OpenNL's nlSolveSystemIterative(NL_CG, Jacobi)
+// (call sites: src/lib/OGF/scene_graph/NL/matrix.cpp:364,390-393; nlSolve at
+// plugins/OGF/WarpDrive/commands/voxel_grob_transport_commands.cpp:281).
+//
+// One PCG iteration = three kernels (SpMV + p.q; x/r update + r.z, r.r;
+// p update).  Each kernel's last CTA reduces the tile partials in a fixed
+// order and advances the scalar state in HBM, so the host never reads a
+// scalar during the solve: the loop is a CUDA-graph while-node whose
+// condition is cleared from the device.  A guard kernel counts body passes
+// and clears the condition after a hard cap, so the loop always ends.
+#include "nlgb_core.cuh"
+#include "nlgb_internal.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+namespace nlgb {
+
+// ---------------------------------------------------------------------------
+// Last-CTA election: thread 0 publishes this tile's partials; returns true in
+// every thread of the CTA that arrived last.
+// ---------------------------------------------------------------------------
+template <int K>
+__device__ __forceinline__ bool publish_elect(const SysView& s, int tile, const double (&v)[K],
+                                              unsigned int* counter) {
+  __shared__ int am_last;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) __stcg(s.part + (size_t)tile * kParts + k, v[k]);
+    __threadfence();
+    const unsigned int prev = atomicAdd(counter, 1u);
+    am_last = (prev == (unsigned int)s.n_tiles - 1u);
+    if (am_last) *counter = 0u;   // next use is in a later kernel
+  }
+  __syncthreads();
+  if (am_last) __threadfence();
+  return am_last != 0;
+}
+
+__device__ __forceinline__ int ld_status(const SysState* st) { return __ldcg(&st->status); }
+__device__ __forceinline__ int ld_mode(const SysState* st) { return __ldcg(&st->mode); }
+
+// ---------------------------------------------------------------------------
+// Plain FP64 kernels.
+// ---------------------------------------------------------------------------
+template <int T>
+__global__ void __launch_bounds__(kCTA) k_init(SysView s) {
+  double v[3];
+  tile_residual<T>(s, blockIdx.x, v);
+  if (publish_elect<3>(s, blockIdx.x, v, &s.st->cnt[0])) {
+    const int comp[3] = {0, 1, 2};
+    double o[3];
+    canon_reduce<3>(s.part, s.n_tiles, comp, o);
+    if (threadIdx.x == 0) scalar_after_init(s.st, o[0], o[1], o[2]);
+  }
+}
+
+template <int T>
+__global__ void __launch_bounds__(kCTA) k_spmv_pq(SysView s) {
+  if (ld_status(s.st) != ST_RUNNING) return;
+  double v[1] = {tile_spmv_pq<T>(s, blockIdx.x)};
+  if (publish_elect<1>(s, blockIdx.x, v, &s.st->cnt[1])) {
+    const int comp[1] = {0};
+    double o[1];
+    canon_reduce<1>(s.part, s.n_tiles, comp, o);
+    if (threadIdx.x == 0) scalar_after_pq(s.st, o[0]);
+  }
+}
+
+__global__ void __launch_bounds__(kCTA) k_update_xr(SysView s) {
+  if (ld_status(s.st) != ST_RUNNING) return;
+  const double alpha = __ldcg(&s.st->alpha);
+  double v[2];
+  tile_update_xr(s, blockIdx.x, alpha, v);
+  if (publish_elect<2>(s, blockIdx.x, v, &s.st->cnt[2])) {
+    const int comp[2] = {0, 1};
+    double o[2];
+    canon_reduce<2>(s.part, s.n_tiles, comp, o);
+    if (threadIdx.x == 0) scalar_after_xr(s.st, o[0], o[1]);
+  }
+}
+
+__global__ void __launch_bounds__(kCTA) k_update_p(SysView s) {
+  if (ld_status(s.st) != ST_RUNNING) return;
+  tile_update_p(s, blockIdx.x, __ldcg(&s.st->beta));
+}
+
+// Termination guard of a while-node body (single thread).
+__global__ void k_guard(SysView s, cudaGraphConditionalHandle h, int need_mode) {
+  SysState* st = s.st;
+  st->guard += 1;
+  bool stop = st->status != ST_RUNNING;
+  if (!stop && s.abort_flag != nullptr && *s.abort_flag != 0) {
+    st->status = ST_ABORTED;
+    stop = true;
+  }
+  if (!stop && st->guard >= st->guard_cap) {
+    st->status = ST_MAX_ITER;
+    stop = true;
+  }
+  if (!stop && need_mode >= 0 && st->mode != need_mode) stop = true;
+  if (stop) cudaGraphSetConditional(h, 0u);
+}
+
+// ||b - A x||^2 of the final iterate; zeroes x when b == 0.
+template <int T>
+__global__ void __launch_bounds__(kCTA) k_final(SysView s) {
+  double v[1] = {0.0};
+  if (__ldcg(&s.st->zero_rhs)) {
+    tile_zero_x(s, blockIdx.x);
+  } else {
+    v[0] = tile_true_rr<T>(s, blockIdx.x);
+  }
+  if (publish_elect<1>(s, blockIdx.x, v, &s.st->cnt[3])) {
+    const int comp[1] = {0};
+    double o[1];
+    canon_reduce<1>(s.part, s.n_tiles, comp, o);
+    if (threadIdx.x == 0) s.st->rr_true = o[0];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Mixed-precision kernels.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kCTA) k_mx_apply(SysView s) {
+  if (ld_status(s.st) != ST_RUNNING) return;
+  tile_mx_apply(s, blockIdx.x);
+}
+
+template <int T>
+__global__ void __launch_bounds__(kCTA) k_mx_outer(SysView s, cudaGraphConditionalHandle h_in) {
+  if (ld_status(s.st) != ST_RUNNING) return;
+  double v[4];
+  tile_mx_outer<T>(s, blockIdx.x, v);
+  if (publish_elect<4>(s, blockIdx.x, v, &s.st->cnt[0])) {
+    const int comp[4] = {0, 1, 2, 3};
+    double o[4];
+    canon_reduce<4>(s.part, s.n_tiles, comp, o);
+    if (threadIdx.x == 0) {
+      scalar_after_outer(s.st, o[0], o[1], o[2], o[3]);
+      const bool inner = s.st->status == ST_RUNNING && s.st->mode == 1;
+      cudaGraphSetConditional(h_in, inner ? 1u : 0u);
+    }
+  }
+}
+
+template <int T>
+__global__ void __launch_bounds__(kCTA) k_mx_spmv_pq(SysView s) {
+  if (ld_status(s.st) != ST_RUNNING || ld_mode(s.st) != 1) return;
+  double v[1] = {tile_mx_spmv_pq<T>(s, blockIdx.x)};
+  if (publish_elect<1>(s, blockIdx.x, v, &s.st->cnt[1])) {
+    const int comp[1] = {0};
+    double o[1];
+    canon_reduce<1>(s.part, s.n_tiles, comp, o);
+    if (threadIdx.x == 0) scalar_after_pq(s.st, o[0]);
+  }
+}
+
+__global__ void __launch_bounds__(kCTA) k_mx_update_cr(SysView s) {
+  if (ld_status(s.st) != ST_RUNNING || ld_mode(s.st) != 1) return;
+  const double alpha = __ldcg(&s.st->alpha);
+  double v[2];
+  tile_mx_update_cr(s, blockIdx.x, alpha, v);
+  if (publish_elect<2>(s, blockIdx.x, v, &s.st->cnt[2])) {
+    const int comp[2] = {0, 1};
+    double o[2];
+    canon_reduce<2>(s.part, s.n_tiles, comp, o);
+    if (threadIdx.x == 0) scalar_after_mx_cr(s.st, o[0], o[1]);
+  }
+}
+
+__global__ void __launch_bounds__(kCTA) k_mx_update_p(SysView s) {
+  if (ld_status(s.st) != ST_RUNNING || ld_mode(s.st) != 1) return;
+  tile_mx_update_p(s, blockIdx.x, __ldcg(&s.st->beta));
+}
+
+// ---------------------------------------------------------------------------
+// Standalone SpMV (nlMultMatrixVector) and helpers.
+// ---------------------------------------------------------------------------
+template <int T, typename V, typename X>
+__global__ void __launch_bounds__(kCTA) k_spmv(int n, int tile_rows, const int* __restrict__ rp,
+                                               const int* __restrict__ ci, const V* __restrict__ va,
+                                               const X* __restrict__ x, X* __restrict__ y) {
+  const int lo = blockIdx.x * tile_rows;
+  const int hi = min(lo + tile_rows, n);
+  const int sub = threadIdx.x / T, lane = threadIdx.x % T;
+  constexpr int RPP = kCTA / T;
+  for (int base = lo; base < hi; base += RPP) {
+    const int row = base + sub;
+    const bool valid = row < hi;
+    const X v = row_dot<T, V, X, X>(rp, ci, va, x, row, valid, lane);
+    if (valid && lane == 0) y[row] = v;
+  }
+}
+
+// dinv[i] = 1 / a_ii (1 when the diagonal is missing or zero); fp32 copies.
+__global__ void k_jacobi(int n, const int* __restrict__ rp, const int* __restrict__ ci,
+                         const double* __restrict__ va, double* dinv, float* dinv32) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double d = 0.0;
+  for (int k = rp[i]; k < rp[i + 1]; ++k)
+    if (ci[k] == i) d += va[k];
+  const double inv = (d != 0.0) ? 1.0 / d : 1.0;
+  dinv[i] = inv;
+  if (dinv32) dinv32[i] = float(inv);
+}
+
+__global__ void k_to_f32(long long n, const double* __restrict__ a, float* __restrict__ b) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    b[i] = float(a[i]);
+}
+
+// Histogram of row lengths: bins 0..31 exact, bin 32 = longer; max length.
+__global__ void k_row_hist(int n, const int* __restrict__ rp, int* hist33, int* maxlen) {
+  __shared__ int h[33];
+  __shared__ int mx;
+  if (threadIdx.x < 33) h[threadIdx.x] = 0;
+  if (threadIdx.x == 0) mx = 0;
+  __syncthreads();
+  int local_max = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int len = rp[i + 1] - rp[i];
+    atomicAdd(&h[len < 32 ? len : 32], 1);
+    local_max = max(local_max, len);
+  }
+  atomicMax(&mx, local_max);
+  __syncthreads();
+  if (threadIdx.x < 33 && h[threadIdx.x]) atomicAdd(&hist33[threadIdx.x], h[threadIdx.x]);
+  if (threadIdx.x == 0) atomicMax(maxlen, mx);
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+// ---------------------------------------------------------------------------
+static int grid_for(long long n, int threads) {
+  long long g = (n + threads - 1) / threads;
+  return (int)std::max(1LL, std::min(g, 152LL * 32));
+}
+
+TuneChoice autotune(int n, long long nnz, int max_row, const int* hist33) {
+  // Threads per row: the smallest power of two covering ~half of the typical
+  // row (each lane then does about two fused multiply-adds, which keeps two
+  // independent loads in flight per lane), raised when long rows dominate.
+  long long cnt = 0, acc = 0;
+  for (int b = 0; b < 33; ++b) { cnt += hist33 ? hist33[b] : 0; acc += hist33 ? (long long)hist33[b] * b : 0; }
+  const double mean = n > 0 ? double(nnz) / double(n) : 0.0;
+  // 90th percentile of the clipped histogram.
+  int p90 = 0;
+  if (hist33 && cnt > 0) {
+    long long c = 0;
+    for (int b = 0; b < 33; ++b) { c += hist33[b]; if (c * 10 >= cnt * 9) { p90 = b; break; } }
+  } else {
+    p90 = (int)std::ceil(mean);
+  }
+  const double typical = std::max(mean, 0.75 * double(p90 == 32 ? std::max(32, max_row) : p90));
+  int tpr = 1;
+  while (tpr < 32 && tpr * 2 < typical) tpr *= 2;
+  // Tile rows: about one resident wave of CTAs on 152 SMs, 512..4096 rows.
+  long long want = (long long)n / (152LL * 6);
+  int tile = 512;
+  while (tile < 4096 && tile < want) tile *= 2;
+  (void)acc;
+  return TuneChoice{tpr, tile};
+}
+
+cudaError_t row_histogram(const DeviceCRS& A, int* hist33_host, int* max_row, cudaStream_t s) {
+  int* d = nullptr;
+  NLGB_CUDA_TRY(cudaMallocAsync(&d, 34 * sizeof(int), s));
+  NLGB_CUDA_TRY(cudaMemsetAsync(d, 0, 34 * sizeof(int), s));
+  if (A.n > 0) k_row_hist<<<grid_for(A.n, 256), 256, 0, s>>>(A.n, A.rp, d, d + 33);
+  NLGB_CUDA_TRY(cudaGetLastError());
+  int h[34];
+  NLGB_CUDA_TRY(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s));
+  NLGB_CUDA_TRY(cudaStreamSynchronize(s));
+  NLGB_CUDA_TRY(cudaFreeAsync(d, s));
+  std::memcpy(hist33_host, h, 33 * sizeof(int));
+  *max_row = h[33];
+  return cudaSuccess;
+}
+
+cudaError_t crs_upload(DeviceCRS& A, int n, int m, const int* rp, const int* ci,
+                       const double* va, cudaStream_t s) {
+  crs_free(A);
+  const long long nnz = rp[n];
+  A.n = n; A.m = m; A.nnz = nnz;
+  NLGB_CUDA_TRY(cudaMalloc(&A.rp, (size_t)(n + 1) * sizeof(int)));
+  NLGB_CUDA_TRY(cudaMalloc(&A.ci, (size_t)std::max(1LL, nnz) * sizeof(int)));
+  NLGB_CUDA_TRY(cudaMalloc(&A.va, (size_t)std::max(1LL, nnz) * sizeof(double)));
+  NLGB_CUDA_TRY(cudaMemcpyAsync(A.rp, rp, (size_t)(n + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
+  if (nnz > 0) {
+    NLGB_CUDA_TRY(cudaMemcpyAsync(A.ci, ci, (size_t)nnz * sizeof(int), cudaMemcpyHostToDevice, s));
+    NLGB_CUDA_TRY(cudaMemcpyAsync(A.va, va, (size_t)nnz * sizeof(double), cudaMemcpyHostToDevice, s));
+  }
+  return cudaSuccess;
+}
+
+cudaError_t crs_adopt_device(DeviceCRS& A, int n, int m, long long nnz, int* rp, int* ci,
+                             double* va, cudaStream_t) {
+  crs_free(A);
+  A.n = n; A.m = m; A.nnz = nnz; A.rp = rp; A.ci = ci; A.va = va;
+  return cudaSuccess;
+}
+
+void crs_free(DeviceCRS& A) {
+  if (!A.owns) { A = DeviceCRS(); return; }
+  cudaFree(A.rp); cudaFree(A.ci); cudaFree(A.va); cudaFree(A.va32);
+  cudaFree(A.dinv); cudaFree(A.dinv32);
+  A = DeviceCRS();
+}
+
+long long device_bytes(const DeviceCRS& A) {
+  long long b = (long long)(A.n + 1) * 4 + A.nnz * 12;
+  if (A.va32) b += A.nnz * 4;
+  if (A.dinv) b += (long long)A.n * 8;
+  if (A.dinv32) b += (long long)A.n * 4;
+  return b;
+}
+
+cudaError_t crs_prepare(DeviceCRS& A, bool need_fp32, cudaStream_t s) {
+  if (A.tpr == 0) {
+    int hist[33];
+    int mx = 0;
+    NLGB_CUDA_TRY(row_histogram(A, hist, &mx, s));
+    A.max_row = mx;
+    const TuneChoice c = autotune(A.n, A.nnz, mx, hist);
+    A.tpr = c.tpr;
+    A.tile_rows = c.tile_rows;
+  }
+  if (!A.dinv) {
+    NLGB_CUDA_TRY(cudaMalloc(&A.dinv, (size_t)std::max(1, A.n) * sizeof(double)));
+    NLGB_CUDA_TRY(cudaMalloc(&A.dinv32, (size_t)std::max(1, A.n) * sizeof(float)));
+    if (A.n > 0) k_jacobi<<<(A.n + 255) / 256, 256, 0, s>>>(A.n, A.rp, A.ci, A.va, A.dinv, A.dinv32);
+    NLGB_CUDA_TRY(cudaGetLastError());
+  }
+  if (need_fp32 && !A.va32) {
+    NLGB_CUDA_TRY(cudaMalloc(&A.va32, (size_t)std::max(1LL, A.nnz) * sizeof(float)));
+    if (A.nnz > 0) k_to_f32<<<grid_for(A.nnz, 256), 256, 0, s>>>(A.nnz, A.va, A.va32);
+    NLGB_CUDA_TRY(cudaGetLastError());
+  }
+  return cudaSuccess;
+}
+
+template <typename V, typename X>
+static cudaError_t spmv_dispatch(const DeviceCRS& A, const V* va, const X* x, X* y, cudaStream_t s) {
+  if (A.n == 0) return cudaSuccess;
+  const int tile = A.tile_rows > 0 ? A.tile_rows : 512;
+  const int grid = (A.n + tile - 1) / tile;
+  switch (A.tpr > 0 ? A.tpr : 4) {
+    case 1: k_spmv<1, V, X><<<grid, kCTA, 0, s>>>(A.n, tile, A.rp, A.ci, va, x, y); break;
+    case 2: k_spmv<2, V, X><<<grid, kCTA, 0, s>>>(A.n, tile, A.rp, A.ci, va, x, y); break;
+    case 4: k_spmv<4, V, X><<<grid, kCTA, 0, s>>>(A.n, tile, A.rp, A.ci, va, x, y); break;
+    case 8: k_spmv<8, V, X><<<grid, kCTA, 0, s>>>(A.n, tile, A.rp, A.ci, va, x, y); break;
+    case 16: k_spmv<16, V, X><<<grid, kCTA, 0, s>>>(A.n, tile, A.rp, A.ci, va, x, y); break;
+    default: k_spmv<32, V, X><<<grid, kCTA, 0, s>>>(A.n, tile, A.rp, A.ci, va, x, y); break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t spmv64(const DeviceCRS& A, const double* x, double* y, cudaStream_t s) {
+  NLGB_CUDA_TRY((spmv_dispatch<double, double>(A, A.va, x, y, s)));
+  return cudaSuccess;
+}
+cudaError_t spmv32(const DeviceCRS& A, const float* x, float* y, cudaStream_t s) {
+  NLGB_CUDA_TRY((spmv_dispatch<float, float>(A, A.va32, x, y, s)));
+  return cudaSuccess;
+}
+
+// --- graph construction helpers ---
+// `dep` may be null (no dependency) or a node the new one runs after.
+static cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, cudaGraphNode_t dep,
+                              const void* fn, int grid, int block, void** args) {
+  cudaKernelNodeParams kp;
+  std::memset(&kp, 0, sizeof(kp));
+  kp.func = const_cast<void*>(fn);
+  kp.gridDim = dim3((unsigned)std::max(1, grid));
+  kp.blockDim = dim3((unsigned)block);
+  kp.sharedMemBytes = 0;
+  kp.kernelParams = args;
+  return cudaGraphAddKernelNode(node, g, dep ? &dep : nullptr, dep ? 1 : 0, &kp);
+}
+
+static cudaError_t add_while(cudaGraph_t g, cudaGraphNode_t* node, cudaGraphNode_t dep,
+                             cudaGraphConditionalHandle h, cudaGraph_t* body) {
+  alignas(cudaGraphNodeParams) unsigned char raw[sizeof(cudaGraphNodeParams)];
+  std::memset(raw, 0, sizeof(raw));
+  cudaGraphNodeParams* cp = reinterpret_cast<cudaGraphNodeParams*>(raw);
+  cp->type = cudaGraphNodeTypeConditional;
+  cp->conditional.handle = h;
+  cp->conditional.type = cudaGraphCondTypeWhile;
+  cp->conditional.size = 1;
+  cudaError_t e = cudaGraphAddNode(node, g, dep ? &dep : nullptr, nullptr, dep ? 1 : 0, cp);
+  if (e != cudaSuccess) return e;
+  *body = cp->conditional.phGraph_out[0];
+  return cudaSuccess;
+}
+
+template <int T> struct PlainKernels {
+  static const void* init() { return (const void*)k_init<T>; }
+  static const void* spmv() { return (const void*)k_spmv_pq<T>; }
+  static const void* fin() { return (const void*)k_final<T>; }
+  static const void* mx_outer() { return (const void*)k_mx_outer<T>; }
+  static const void* mx_spmv() { return (const void*)k_mx_spmv_pq<T>; }
+};
+
+struct KernelSet { const void *init, *spmv, *fin, *mx_outer, *mx_spmv; };
+static KernelSet kernels_for(int tpr) {
+  switch (tpr) {
+#define NLGB_KS(T) case T: return {PlainKernels<T>::init(), PlainKernels<T>::spmv(), PlainKernels<T>::fin(), PlainKernels<T>::mx_outer(), PlainKernels<T>::mx_spmv()};
+    NLGB_KS(1) NLGB_KS(2) NLGB_KS(4) NLGB_KS(8) NLGB_KS(16)
+    default: return {PlainKernels<32>::init(), PlainKernels<32>::spmv(), PlainKernels<32>::fin(), PlainKernels<32>::mx_outer(), PlainKernels<32>::mx_spmv()};
+#undef NLGB_KS
+  }
+}
+
+constexpr int kUnrollPlain = 4;   // CG iterations per while-body pass
+constexpr int kUnrollInner = 4;
+
+PcgSolver::~PcgSolver() { release(); }
+
+void PcgSolver::release() {
+  if (plain_exec_) cudaGraphExecDestroy(plain_exec_);
+  if (mixed_exec_) cudaGraphExecDestroy(mixed_exec_);
+  plain_exec_ = mixed_exec_ = nullptr;
+  cudaFree(b_); cudaFree(x_); cudaFree(r_); cudaFree(p_); cudaFree(q_); cudaFree(part_);
+  cudaFree(r32_); cudaFree(p32_); cudaFree(q32_); cudaFree(c32_); cudaFree(st_);
+  if (st_host_) cudaFreeHost(st_host_);
+  if (ev0_) cudaEventDestroy(ev0_);
+  if (ev1_) cudaEventDestroy(ev1_);
+  b_ = x_ = r_ = p_ = q_ = part_ = nullptr;
+  r32_ = p32_ = q32_ = c32_ = nullptr;
+  st_ = st_host_ = nullptr;
+  ev0_ = ev1_ = nullptr;
+  mixed_alloc_ = false;
+}
+
+cudaError_t PcgSolver::bind(DeviceCRS* A, cudaStream_t stream) {
+  release();
+  A_ = A;
+  stream_ = stream;
+  n_ = A->n;
+  tpr_ = A->tpr;
+  tile_rows_ = A->tile_rows;
+  n_tiles_ = std::max(1, (n_ + tile_rows_ - 1) / tile_rows_);
+  return alloc(false);
+}
+
+cudaError_t PcgSolver::alloc(bool mixed) {
+  const size_t n8 = (size_t)std::max(2, n_ + 2) * sizeof(double);
+  if (!x_) {
+    NLGB_CUDA_TRY(cudaMalloc(&b_, n8));
+    NLGB_CUDA_TRY(cudaMalloc(&x_, n8));
+    NLGB_CUDA_TRY(cudaMalloc(&r_, n8));
+    NLGB_CUDA_TRY(cudaMalloc(&p_, n8));
+    NLGB_CUDA_TRY(cudaMalloc(&q_, n8));
+    NLGB_CUDA_TRY(cudaMalloc(&part_, (size_t)n_tiles_ * kParts * sizeof(double)));
+    NLGB_CUDA_TRY(cudaMalloc(&st_, sizeof(SysState)));
+    NLGB_CUDA_TRY(cudaMallocHost(&st_host_, sizeof(SysState)));
+    NLGB_CUDA_TRY(cudaEventCreate(&ev0_));
+    NLGB_CUDA_TRY(cudaEventCreate(&ev1_));
+  }
+  if (mixed && !mixed_alloc_) {
+    const size_t n4 = (size_t)std::max(4, n_ + 4) * sizeof(float);
+    NLGB_CUDA_TRY(cudaMalloc(&r32_, n4));
+    NLGB_CUDA_TRY(cudaMalloc(&p32_, n4));
+    NLGB_CUDA_TRY(cudaMalloc(&q32_, n4));
+    NLGB_CUDA_TRY(cudaMalloc(&c32_, n4));
+    mixed_alloc_ = true;
+  }
+  return cudaSuccess;
+}
+
+static SysView make_view(DeviceCRS* A, int tile_rows, int n_tiles, double* b, double* x, double* r,
+                         double* p, double* q, float* r32, float* p32, float* q32, float* c32,
+                         double* part, void* st, const volatile int* abort_flag) {
+  SysView v;
+  std::memset(&v, 0, sizeof(v));
+  v.n = A->n; v.tile_rows = tile_rows; v.n_tiles = n_tiles; v.tpr = A->tpr;
+  v.rp = A->rp; v.ci = A->ci; v.va = A->va; v.va32 = A->va32;
+  v.dinv = A->dinv; v.dinv32 = A->dinv32;
+  v.b = b; v.x = x; v.r = r; v.p = p; v.q = q;
+  v.r32 = r32; v.p32 = p32; v.q32 = q32; v.c32 = c32;
+  v.part = part; v.st = (SysState*)st; v.abort_flag = abort_flag;
+  return v;
+}
+
+cudaError_t PcgSolver::build_plain_graph() {
+  SysView v = make_view(A_, tile_rows_, n_tiles_, b_, x_, r_, p_, q_, nullptr, nullptr, nullptr,
+                        nullptr, part_, st_, abort_flag_);
+  const KernelSet ks = kernels_for(tpr_);
+  cudaGraph_t g;
+  NLGB_CUDA_TRY(cudaGraphCreate(&g, 0));
+  cudaGraphConditionalHandle h;
+  NLGB_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault));
+  void* a1[] = {&v};
+  cudaGraphNode_t n_init, n_loop, n_fin, prev;
+  NLGB_CUDA_TRY(add_kernel(g, &n_init, nullptr, ks.init, n_tiles_, kCTA, a1));
+  cudaGraph_t body;
+  NLGB_CUDA_TRY(add_while(g, &n_loop, n_init, h, &body));
+  prev = nullptr;
+  for (int u = 0; u < kUnrollPlain; ++u) {
+    cudaGraphNode_t n1, n2, n3;
+    NLGB_CUDA_TRY(add_kernel(body, &n1, prev, ks.spmv, n_tiles_, kCTA, a1));
+    NLGB_CUDA_TRY(add_kernel(body, &n2, n1, (const void*)k_update_xr, n_tiles_, kCTA, a1));
+    NLGB_CUDA_TRY(add_kernel(body, &n3, n2, (const void*)k_update_p, n_tiles_, kCTA, a1));
+    prev = n3;
+  }
+  int need_mode = -1;
+  void* ag[] = {&v, &h, &need_mode};
+  cudaGraphNode_t n_g;
+  NLGB_CUDA_TRY(add_kernel(body, &n_g, prev, (const void*)k_guard, 1, 1, ag));
+  NLGB_CUDA_TRY(add_kernel(g, &n_fin, n_loop, ks.fin, n_tiles_, kCTA, a1));
+  cudaError_t e = cudaGraphInstantiate(&plain_exec_, g, 0);
+  cudaGraphDestroy(g);
+  NLGB_CUDA_TRY(e);
+  return cudaSuccess;
+}
+
+cudaError_t PcgSolver::build_mixed_graph() {
+  SysView v = make_view(A_, tile_rows_, n_tiles_, b_, x_, r_, p_, q_, r32_, p32_, q32_, c32_,
+                        part_, st_, abort_flag_);
+  const KernelSet ks = kernels_for(tpr_);
+  cudaGraph_t g;
+  NLGB_CUDA_TRY(cudaGraphCreate(&g, 0));
+  cudaGraphConditionalHandle h_out;
+  NLGB_CUDA_TRY(cudaGraphConditionalHandleCreate(&h_out, g, 1u, cudaGraphCondAssignDefault));
+  void* a1[] = {&v};
+  cudaGraphNode_t n_outer_loop, n_fin;
+  cudaGraph_t obody;
+  NLGB_CUDA_TRY(add_while(g, &n_outer_loop, nullptr, h_out, &obody));
+  cudaGraphConditionalHandle h_in;
+  NLGB_CUDA_TRY(cudaGraphConditionalHandleCreate(&h_in, obody, 0u, cudaGraphCondAssignDefault));
+  cudaGraphNode_t n_apply, n_outer, n_inner_loop, n_og;
+  NLGB_CUDA_TRY(add_kernel(obody, &n_apply, nullptr, (const void*)k_mx_apply, n_tiles_, kCTA, a1));
+  void* ao[] = {&v, &h_in};
+  NLGB_CUDA_TRY(add_kernel(obody, &n_outer, n_apply, ks.mx_outer, n_tiles_, kCTA, ao));
+  cudaGraph_t ibody;
+  NLGB_CUDA_TRY(add_while(obody, &n_inner_loop, n_outer, h_in, &ibody));
+  cudaGraphNode_t prev = nullptr;
+  for (int u = 0; u < kUnrollInner; ++u) {
+    cudaGraphNode_t n1, n2, n3;
+    NLGB_CUDA_TRY(add_kernel(ibody, &n1, prev, ks.mx_spmv, n_tiles_, kCTA, a1));
+    NLGB_CUDA_TRY(add_kernel(ibody, &n2, n1, (const void*)k_mx_update_cr, n_tiles_, kCTA, a1));
+    NLGB_CUDA_TRY(add_kernel(ibody, &n3, n2, (const void*)k_mx_update_p, n_tiles_, kCTA, a1));
+    prev = n3;
+  }
+  int need_inner = 1, need_any = -1;
+  void* agi[] = {&v, &h_in, &need_inner};
+  cudaGraphNode_t n_ig;
+  NLGB_CUDA_TRY(add_kernel(ibody, &n_ig, prev, (const void*)k_guard, 1, 1, agi));
+  void* ago[] = {&v, &h_out, &need_any};
+  NLGB_CUDA_TRY(add_kernel(obody, &n_og, n_inner_loop, (const void*)k_guard, 1, 1, ago));
+  NLGB_CUDA_TRY(add_kernel(g, &n_fin, n_outer_loop, ks.fin, n_tiles_, kCTA, a1));
+  cudaError_t e = cudaGraphInstantiate(&mixed_exec_, g, 0);
+  cudaGraphDestroy(g);
+  NLGB_CUDA_TRY(e);
+  return cudaSuccess;
+}
+
+cudaError_t PcgSolver::solve(const double* b, double* x, const SolveParams& prm, SolveResult* res) {
+  const bool mixed = prm.precision == 1;
+  if (mixed) {
+    NLGB_CUDA_TRY(crs_prepare(*A_, true, stream_));
+    NLGB_CUDA_TRY(alloc(true));
+  }
+  if (mixed && !mixed_exec_) NLGB_CUDA_TRY(build_mixed_graph());
+  if (!mixed && !plain_exec_) NLGB_CUDA_TRY(build_plain_graph());
+
+  SysState* h = (SysState*)st_host_;
+  std::memset(h, 0, sizeof(SysState));
+  const long long max_iter = prm.max_iter >= 0 ? prm.max_iter : 5LL * n_;
+  h->thresh2 = prm.eps * prm.eps;
+  h->max_iter = max_iter;
+  h->status = ST_RUNNING;
+  h->mode = 0;
+  h->max_outer = std::max(1, prm.max_outer);
+  h->in_thresh2 = prm.inner_eps * prm.inner_eps;
+  h->in_max = (int)std::min<long long>(max_iter, 1LL << 30);
+  h->in_max = std::max(1, h->in_max);
+  // Hard cap on while-body passes: enough for max_iter iterations plus the
+  // outer steps; reached only if the scalar logic failed to stop the loop.
+  const int unroll = mixed ? kUnrollInner : kUnrollPlain;
+  h->guard_cap = max_iter / unroll + 2LL * (h->max_outer + 2) + 4;
+  NLGB_CUDA_TRY(cudaMemcpyAsync(st_, h, sizeof(SysState), cudaMemcpyHostToDevice, stream_));
+  NLGB_CUDA_TRY(cudaMemcpyAsync(b_, b, (size_t)n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
+  NLGB_CUDA_TRY(cudaMemcpyAsync(x_, x, (size_t)n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
+  if (mixed) NLGB_CUDA_TRY(cudaMemsetAsync(c32_, 0, (size_t)n_ * sizeof(float), stream_));
+  NLGB_CUDA_TRY(cudaEventRecord(ev0_, stream_));
+  NLGB_CUDA_TRY(cudaGraphLaunch(mixed ? mixed_exec_ : plain_exec_, stream_));
+  NLGB_CUDA_TRY(cudaEventRecord(ev1_, stream_));
+  NLGB_CUDA_TRY(cudaMemcpyAsync(x, x_, (size_t)n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
+  NLGB_CUDA_TRY(cudaMemcpyAsync(h, st_, sizeof(SysState), cudaMemcpyDeviceToHost, stream_));
+  NLGB_CUDA_TRY(cudaStreamSynchronize(stream_));
+  float ms = 0.f;
+  NLGB_CUDA_TRY(cudaEventElapsedTime(&ms, ev0_, ev1_));
+  if (res) {
+    res->status = h->status;
+    res->iterations = h->iter;
+    res->outer_steps = h->outer;
+    const double bb = h->bnorm2;
+    res->rel_residual = bb > 0 ? std::sqrt(h->rr / bb) : 0.0;
+    res->true_rel_residual = bb > 0 ? std::sqrt(h->rr_true / bb) : 0.0;
+    res->seconds = ms * 1e-3;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace nlgb

@@ -1,0 +1,227 @@
+"""High-level Python API over libnl_gb300: resident matrices, solves and the
+full OpenNL context path for a row stream.
+
+* ``Matrix``: a CRS matrix resident in GPU memory (nl_gb300.h
+  ``nlgb_matrix``), with ``spmv`` and ``solve`` (plain FP64 or mixed
+  FP32-inner / FP64-refined Jacobi-PCG).
+* ``assemble``: GPU least-squares / square assembly of a ``RowStream``.
+* ``solve_opennl``: the reference's own call sequence (nlNewContext,
+  nlSolverParameteri, nlBegin/nlEnd, rows, nlSolve, nlGetVariable) through
+  the C ABI -- what geogram's builders do behind Graphite's commands.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .systems import RowStream
+
+K = _lib.header_constants()
+PRECISION = {"double": K["NL_GB300_PRECISION_DOUBLE"], "fp64": K["NL_GB300_PRECISION_DOUBLE"],
+             "mixed": K["NL_GB300_PRECISION_MIXED"]}
+STATUS = {K[n]: n.replace("NL_GB300_STATUS_", "").lower() for n in K if n.startswith("NL_GB300_STATUS_")}
+
+
+class SolverError(RuntimeError):
+    pass
+
+
+@dataclass
+class SolveInfo:
+    status: str
+    iterations: int
+    refinement_steps: int
+    rel_residual: float
+    true_rel_residual: float
+    seconds: float
+
+
+def _ptr(a, t):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def _check(rc: int, what: str):
+    if rc != 0:
+        raise SolverError(f"{what} failed ({rc}): {_lib.last_error()}")
+
+
+def device_available() -> bool:
+    return bool(_lib.load().nlgb_device_available())
+
+
+class Matrix:
+    """CRS matrix resident in HBM (int32 indices, FP64 values)."""
+
+    def __init__(self, rp, ci, va, n_cols: int | None = None, _handle=None):
+        L = _lib.load()
+        if _handle is not None:
+            self._h = _handle
+        else:
+            rp = np.ascontiguousarray(rp, np.int32)
+            ci = np.ascontiguousarray(ci, np.int32)
+            va = np.ascontiguousarray(va, np.float64)
+            n = rp.shape[0] - 1
+            h = L.nlgb_matrix_create(n, n if n_cols is None else n_cols, _ptr(rp, None),
+                                     _ptr(ci, None), _ptr(va, None))
+            if not h:
+                raise SolverError(f"nlgb_matrix_create failed: {_lib.last_error()}")
+            self._h = h
+        n = ctypes.c_int(); nnz = ctypes.c_longlong(); tpr = ctypes.c_int(); tile = ctypes.c_int()
+        _check(L.nlgb_matrix_info(self._h, ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(tpr),
+                                  ctypes.byref(tile)), "nlgb_matrix_info")
+        self.n, self.nnz, self.threads_per_row, self.tile_rows = n.value, nnz.value, tpr.value, tile.value
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().nlgb_matrix_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_layout(self, threads_per_row: int = 0, tile_rows: int = 0):
+        _check(_lib.load().nlgb_matrix_set_layout(self._h, threads_per_row, tile_rows), "set_layout")
+        self.__init__(None, None, None, _handle=self._h)
+
+    def download(self):
+        rp = np.empty(self.n + 1, np.int32)
+        ci = np.empty(max(1, self.nnz), np.int32)
+        va = np.empty(max(1, self.nnz), np.float64)
+        _check(_lib.load().nlgb_matrix_download(self._h, rp.ctypes.data_as(_lib.i32p),
+                                                ci.ctypes.data_as(_lib.i32p),
+                                                va.ctypes.data_as(_lib.f64p)), "download")
+        return rp, ci[: self.nnz], va[: self.nnz]
+
+    def jacobi(self) -> np.ndarray:
+        d = np.empty(self.n, np.float64)
+        _check(_lib.load().nlgb_matrix_jacobi(self._h, d.ctypes.data_as(_lib.f64p)), "jacobi")
+        return d
+
+    def spmv(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.empty(self.n, np.float64)
+        _check(_lib.load().nlgb_spmv(self._h, _ptr(x, None), _ptr(y, None)), "nlgb_spmv")
+        return y
+
+    def solve(self, b, x0=None, eps: float = 1e-10, max_iter: int = -1, precision: str = "double",
+              inner_eps: float = 1e-5, max_outer: int = 40):
+        """Solve A x = b.  Host numpy arrays in and out.  Returns (x, SolveInfo)."""
+        L = _lib.load()
+        b = np.ascontiguousarray(b, np.float64)
+        x = np.zeros(self.n) if x0 is None else np.array(x0, np.float64, copy=True)
+        p = _lib.NlgbParams(eps, max_iter, PRECISION[precision], inner_eps, max_outer)
+        r = _lib.NlgbResult()
+        _check(L.nlgb_solve(self._h, _ptr(b, None), _ptr(x, None), ctypes.byref(p), ctypes.byref(r)),
+               "nlgb_solve")
+        return x, SolveInfo(STATUS.get(r.status, str(r.status)), r.iterations, r.refinement_steps,
+                            r.rel_residual, r.true_rel_residual, r.seconds)
+
+    def solve_device(self, b_ptr: int, x_ptr: int, eps: float = 1e-10, max_iter: int = -1,
+                     precision: str = "double", inner_eps: float = 1e-5, max_outer: int = 40):
+        """Solve with device pointers (e.g. torch tensors' data_ptr())."""
+        L = _lib.load()
+        p = _lib.NlgbParams(eps, max_iter, PRECISION[precision], inner_eps, max_outer)
+        r = _lib.NlgbResult()
+        _check(L.nlgb_solve(self._h, ctypes.c_void_p(b_ptr), ctypes.c_void_p(x_ptr), ctypes.byref(p),
+                            ctypes.byref(r)), "nlgb_solve")
+        return SolveInfo(STATUS.get(r.status, str(r.status)), r.iterations, r.refinement_steps,
+                         r.rel_residual, r.true_rel_residual, r.seconds)
+
+
+def assemble(rs: RowStream):
+    """GPU assembly of a row stream.  Returns (Matrix, rhs (n_systems, n_free), seconds)."""
+    L = _lib.load()
+    col = rs.encoded_cols()
+    n_free = int((rs.locked == 0).sum())
+    rhs = np.ascontiguousarray(rs.rhs.T, np.float64)
+    row_ptr = np.ascontiguousarray(rs.row_ptr, np.int64)
+    val = np.ascontiguousarray(rs.val, np.float64)
+    weight = None if rs.weight is None else np.ascontiguousarray(rs.weight, np.float64)
+    xl = np.ascontiguousarray(rs.values, np.float64)
+    out = np.empty((rs.n_systems, max(1, n_free)), np.float64)
+    h = ctypes.c_void_p()
+    secs = ctypes.c_double()
+    _check(L.nlgb_assemble(int(rs.least_squares), rs.n_rows, row_ptr.ctypes.data_as(_lib.i64p),
+                           col.ctypes.data_as(_lib.i32p), val.ctypes.data_as(_lib.f64p),
+                           rhs.ctypes.data_as(_lib.f64p),
+                           None if weight is None else weight.ctypes.data_as(_lib.f64p), n_free,
+                           rs.n_vars, xl.ctypes.data_as(_lib.f64p), rs.n_systems, ctypes.byref(h),
+                           out.ctypes.data_as(_lib.f64p), ctypes.byref(secs)), "nlgb_assemble")
+    return Matrix(None, None, None, _handle=h.value), out[:, :n_free], secs.value
+
+
+def solve_opennl(rs: RowStream, precision: str = "double", eps: float = 1e-10,
+                 max_iter: int | None = None, per_call: bool = False):
+    """Run the OpenNL context sequence on a row stream; returns (values
+    (n_systems, n_vars), info dict).  per_call=True feeds rows through
+    nlBegin(NL_ROW)/nlCoefficient/nlEnd(NL_ROW) one call at a time (slow in
+    Python; for small conformance cases), else through nlgb_add_rows."""
+    from . import opennl as nl
+    ctx = nl.nlNewContext()
+    try:
+        nl.nlSolverParameteri(nl.NL_NB_VARIABLES, rs.n_vars)
+        nl.nlSolverParameteri(nl.NL_NB_SYSTEMS, rs.n_systems)
+        nl.nlSolverParameteri(nl.NL_LEAST_SQUARES, nl.NL_TRUE if rs.least_squares else nl.NL_FALSE)
+        nl.nlSolverParameteri(nl.NL_SOLVER, nl.NL_CG)
+        nl.nlSolverParameteri(nl.NL_PRECONDITIONER, nl.NL_PRECOND_JACOBI)
+        nl.nlSolverParameterd(nl.NL_THRESHOLD, eps)
+        if max_iter is not None:
+            nl.nlSolverParameteri(nl.NL_MAX_ITERATIONS, int(max_iter))
+        nl.nlSolverParameteri(nl.NL_GB300_PRECISION, PRECISION[precision])
+        nl.nlBegin(nl.NL_SYSTEM)
+        if per_call:
+            for s in range(rs.n_systems):
+                for i in range(rs.n_vars):
+                    nl.nlMultiSetVariable(i, s, float(rs.values[s, i]))
+            for i in np.flatnonzero(rs.locked):
+                nl.nlLockVariable(int(i))
+        else:
+            nl.nlgbSetVariables(rs.values, rs.locked)
+        nl.nlBegin(nl.NL_MATRIX)
+        if per_call:
+            for r in range(rs.n_rows):
+                nl.nlBegin(nl.NL_ROW)
+                for k in range(rs.row_ptr[r], rs.row_ptr[r + 1]):
+                    nl.nlCoefficient(int(rs.var[k]), float(rs.val[k]))
+                for s in range(rs.n_systems):
+                    nl.nlMultiRightHandSide(s, float(rs.rhs[r, s]))
+                if rs.weight is not None:
+                    nl.nlRowScaling(float(rs.weight[r]))
+                nl.nlEnd(nl.NL_ROW)
+        else:
+            rc = nl.nlgbAddRows(rs.row_ptr, rs.var, rs.val, rs.rhs, rs.weight)
+            if rc != 0:
+                raise SolverError(f"nlgb_add_rows failed: {nl.nlGetErrorString()}")
+        nl.nlEnd(nl.NL_MATRIX)
+        nl.nlEnd(nl.NL_SYSTEM)
+        ok = nl.nlSolve()
+        info = {
+            "ok": bool(ok),
+            "status": STATUS.get(nl.nlGetIntegerv(nl.NL_GB300_STATUS), "?"),
+            "iterations": nl.nlGetIntegerv(nl.NL_USED_ITERATIONS),
+            "refinement_steps": nl.nlGetIntegerv(nl.NL_GB300_REFINEMENT_STEPS),
+            "error": nl.nlGetDoublev(nl.NL_ERROR),
+            "true_error": nl.nlGetDoublev(nl.NL_GB300_TRUE_RESIDUAL),
+            "elapsed": nl.nlGetDoublev(nl.NL_ELAPSED_TIME),
+            "assembly_time": nl.nlGetDoublev(nl.NL_GB300_ASSEMBLY_TIME),
+            "nnz": nl.nlGetIntegerv(nl.NL_NNZ),
+            "error_string": nl.nlGetErrorString() if not ok else "",
+        }
+        if per_call:
+            vals = np.array([[nl.nlMultiGetVariable(i, s) for i in range(rs.n_vars)]
+                             for s in range(rs.n_systems)])
+        else:
+            vals = nl.nlgbGetVariables(rs.n_systems, rs.n_vars)
+        return vals, info
+    finally:
+        nl.nlDeleteContext(ctx)

@@ -1,0 +1,185 @@
+"""CPU oracle for the OpenNL sparse-solver hot path -- TEST INFRASTRUCTURE.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference
+arm may import this module; the library never does.
+
+* ``assemble``: least-squares normal equations / square systems from a row
+  stream (C, nl_oracle.c), bit-exact reference for the GPU row-merge.
+* ``pcg``: FP64 Jacobi-PCG with OpenMP threads (C), the timed CPU baseline
+  and the iterative oracle.
+* ``direct_solve``: scipy SuperLU, the FP64 direct oracle.
+* ``dense_normal_equations``: an independent numpy restatement used to pin
+  ``assemble`` (no shared code with the C path).
+
+OpenNL's own source is absent from the reference checkout (geogram submodule
+not checked out), so parity against OpenNL itself is unpinned; the oracle is
+pinned against analytic known-answer tests, numpy dense algebra and scipy's
+SuperLU (tests/test_oracle.py, tests/golden/).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "libnl_oracle.so"
+
+_c_int_p = ctypes.POINTER(ctypes.c_int)
+_c_ll_p = ctypes.POINTER(ctypes.c_longlong)
+_c_dbl_p = ctypes.POINTER(ctypes.c_double)
+
+_lib = None
+
+
+def build() -> Path:
+    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            build()
+        L = ctypes.CDLL(str(LIB))
+        L.nlo_assemble.restype = ctypes.c_void_p
+        L.nlo_assemble.argtypes = [ctypes.c_int, ctypes.c_longlong, _c_ll_p, _c_int_p, _c_dbl_p,
+                                   _c_dbl_p, _c_dbl_p, ctypes.c_int, ctypes.c_int, _c_dbl_p,
+                                   ctypes.c_int]
+        L.nlo_system_info.argtypes = [ctypes.c_void_p, _c_int_p, _c_ll_p]
+        L.nlo_system_copy.argtypes = [ctypes.c_void_p, _c_int_p, _c_int_p, _c_dbl_p, _c_dbl_p]
+        L.nlo_system_free.argtypes = [ctypes.c_void_p]
+        L.nlo_spmv.argtypes = [ctypes.c_int, _c_int_p, _c_int_p, _c_dbl_p, _c_dbl_p, _c_dbl_p, ctypes.c_int]
+        L.nlo_pcg.restype = ctypes.c_int
+        L.nlo_pcg.argtypes = [ctypes.c_int, _c_int_p, _c_int_p, _c_dbl_p, _c_dbl_p, _c_dbl_p,
+                              ctypes.c_double, ctypes.c_longlong, ctypes.c_int, ctypes.c_int,
+                              _c_ll_p, _c_dbl_p]
+        L.nlo_max_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(ct) if a is not None else None
+
+
+def max_threads() -> int:
+    return int(lib().nlo_max_threads())
+
+
+def dedupe_rows(row_ptr, var, val):
+    """Merge repeated variables of a row into their first occurrence (the
+    nlCoefficient semantics of include/nl.h)."""
+    row_ptr = np.asarray(row_ptr, np.int64)
+    out_rp = [0]
+    out_var, out_val = [], []
+    for r in range(row_ptr.shape[0] - 1):
+        seen = {}
+        for k in range(row_ptr[r], row_ptr[r + 1]):
+            v = int(var[k])
+            if v in seen:
+                out_val[seen[v]] += float(val[k])
+            else:
+                seen[v] = len(out_var)
+                out_var.append(v)
+                out_val.append(float(val[k]))
+        out_rp.append(len(out_var))
+    return (np.asarray(out_rp, np.int64), np.asarray(out_var, np.int32),
+            np.asarray(out_val, np.float64))
+
+
+def assemble(least_squares: bool, row_ptr, col, val, rhs, weight, n_free: int, n_vars: int,
+             xl, n_systems: int = 1):
+    """Row stream (encoded columns: free index or -(var+1)) -> (rp, ci, va, rhs[k, n])."""
+    row_ptr = np.ascontiguousarray(row_ptr, np.int64)
+    col = np.ascontiguousarray(col, np.int32)
+    val = np.ascontiguousarray(val, np.float64)
+    n_rows = row_ptr.shape[0] - 1
+    rhs = None if rhs is None else np.ascontiguousarray(rhs, np.float64).reshape(n_systems, n_rows)
+    weight = None if weight is None else np.ascontiguousarray(weight, np.float64)
+    xl = np.ascontiguousarray(xl if xl is not None else np.zeros((n_systems, max(1, n_vars))), np.float64)
+    L = lib()
+    h = L.nlo_assemble(int(least_squares), n_rows, _p(row_ptr, _c_ll_p), _p(col, _c_int_p),
+                       _p(val, _c_dbl_p), _p(rhs, _c_dbl_p), _p(weight, _c_dbl_p), n_free, n_vars,
+                       _p(xl, _c_dbl_p), n_systems)
+    n = ctypes.c_int()
+    nnz = ctypes.c_longlong()
+    L.nlo_system_info(h, ctypes.byref(n), ctypes.byref(nnz))
+    rp = np.empty(n.value + 1, np.int32)
+    ci = np.empty(max(1, nnz.value), np.int32)
+    va = np.empty(max(1, nnz.value), np.float64)
+    rh = np.empty((n_systems, max(1, n.value)), np.float64)
+    L.nlo_system_copy(h, _p(rp, _c_int_p), _p(ci, _c_int_p), _p(va, _c_dbl_p), _p(rh, _c_dbl_p))
+    L.nlo_system_free(h)
+    return rp, ci[: nnz.value], va[: nnz.value], rh[:, : n.value]
+
+
+def assemble_rowstream(rs):
+    """Assemble a graphitethree_gb300.systems.RowStream (after deduping rows)."""
+    rp, var, val = dedupe_rows(rs.row_ptr, rs.var, rs.val)
+    fidx = np.full(rs.n_vars, -1, np.int64)
+    fv = np.flatnonzero(rs.locked == 0)
+    fidx[fv] = np.arange(fv.shape[0])
+    f = fidx[var]
+    col = np.where(f >= 0, f, -(var.astype(np.int64) + 1)).astype(np.int32)
+    rhs = np.ascontiguousarray(rs.rhs.T)
+    return assemble(rs.least_squares, rp, col, val, rhs, rs.weight, int(fv.shape[0]), rs.n_vars,
+                    rs.values, rs.n_systems)
+
+
+def spmv(rp, ci, va, x, nthreads: int = 0):
+    rp = np.ascontiguousarray(rp, np.int32); ci = np.ascontiguousarray(ci, np.int32)
+    va = np.ascontiguousarray(va, np.float64); x = np.ascontiguousarray(x, np.float64)
+    n = rp.shape[0] - 1
+    y = np.empty(n, np.float64)
+    lib().nlo_spmv(n, _p(rp, _c_int_p), _p(ci, _c_int_p), _p(va, _c_dbl_p), _p(x, _c_dbl_p),
+                   _p(y, _c_dbl_p), nthreads or max_threads())
+    return y
+
+
+def pcg(rp, ci, va, b, x0=None, eps: float = 1e-10, max_iter: int | None = None,
+        jacobi: bool = True, nthreads: int = 0):
+    """FP64 (Jacobi-)PCG.  Returns (x, status, iterations, rel_residual)."""
+    rp = np.ascontiguousarray(rp, np.int32); ci = np.ascontiguousarray(ci, np.int32)
+    va = np.ascontiguousarray(va, np.float64); b = np.ascontiguousarray(b, np.float64)
+    n = rp.shape[0] - 1
+    x = np.zeros(n) if x0 is None else np.array(x0, np.float64, copy=True)
+    it = ctypes.c_longlong()
+    rr = ctypes.c_double()
+    st = lib().nlo_pcg(n, _p(rp, _c_int_p), _p(ci, _c_int_p), _p(va, _c_dbl_p), _p(b, _c_dbl_p),
+                       _p(x, _c_dbl_p), eps, 5 * n if max_iter is None else max_iter, int(jacobi),
+                       nthreads or max_threads(), ctypes.byref(it), ctypes.byref(rr))
+    return x, int(st), int(it.value), float(rr.value)
+
+
+def direct_solve(rp, ci, va, b):
+    """FP64 direct oracle: scipy SuperLU."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    n = len(rp) - 1
+    A = sp.csr_matrix((va, ci, rp), shape=(n, n)).tocsc()
+    return spla.spsolve(A, np.asarray(b, np.float64))
+
+
+def dense_normal_equations(rs):
+    """Independent numpy restatement of the least-squares normal equations
+    (dense; small systems only)."""
+    rp, var, val = dedupe_rows(rs.row_ptr, rs.var, rs.val)
+    n_rows = rp.shape[0] - 1
+    A = np.zeros((n_rows, rs.n_vars))
+    for r in range(n_rows):
+        for k in range(rp[r], rp[r + 1]):
+            A[r, var[k]] += val[k]
+    w = np.ones(n_rows) if rs.weight is None else np.asarray(rs.weight)
+    free = rs.locked == 0
+    Af, Al = A[:, free], A[:, ~free]
+    out_M = (Af * w[:, None]).T @ Af
+    rhs = []
+    for s in range(rs.n_systems):
+        srow = rs.rhs[:, s] - Al @ rs.values[s][~free]
+        rhs.append((Af * w[:, None]).T @ srow)
+    return out_M, np.array(rhs)

@@ -1,0 +1,287 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+Bars (written in each test):
+  * assembly of the normal equations: bit-exact (same sum order, no FMA);
+  * SpMV: |y - y_oracle| <= 1e-14 * (|A| |x|) per row (sum order differs);
+  * plain FP64 PCG at relative residual 1e-10: relative solution difference
+    <= 1e-8 against the oracle's FP64 PCG and against scipy's direct solve
+    (tighter threshold on the ill-conditioned LSCM normal equations, where
+    two CG implementations stopping at 1e-10 may differ by more: H1);
+  * mixed FP32-inner / FP64-refined: true FP64 residual <= 1e-10 and the
+    same 1e-8 solution bar against the FP64 direct oracle.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+from graphitethree_gb300 import opennl as nl
+from graphitethree_gb300 import solver, systems
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+# ---------------------------------------------------------------------------
+# assembly
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("name", golden_names())
+def test_assembly_bit_exact_golden(gpu_ok, oracle_mod, name):
+    rs, exp = load_golden(name)
+    rp, ci, va, rhs = oracle_mod.assemble_rowstream(rs)
+    rp_d, var_d, val_d = oracle_mod.dedupe_rows(rs.row_ptr, rs.var, rs.val)
+    rs2 = systems.RowStream(rs.n_vars, rp_d, var_d, val_d, rs.rhs, rs.locked, rs.values,
+                            rs.least_squares, rs.weight)
+    M, grhs, _ = solver.assemble(rs2)
+    g_rp, g_ci, g_va = M.download()
+    assert np.array_equal(g_rp, rp)
+    if rs.least_squares:
+        assert np.array_equal(g_ci, ci)
+        assert np.array_equal(g_va, va)          # bit-exact
+    else:
+        assert np.array_equal(g_ci, ci) and np.array_equal(g_va, va)
+    assert np.array_equal(grhs, rhs)             # bit-exact
+
+
+@pytest.mark.parametrize("case", ["lscm_64x48", "voxel_w", "lscm_multi"])
+def test_assembly_bit_exact_generated(gpu_ok, oracle_mod, case):
+    if case == "lscm_64x48":
+        rs = systems.lscm_system(64, 48, seed=21)
+    elif case == "voxel_w":
+        rs = systems.voxel_rows(12, 10, 9, seed=3, locked_fraction=0.2)
+        rs.weight = np.random.default_rng(0).uniform(0.5, 2.0, rs.n_rows)
+        rs.rhs = np.random.default_rng(1).normal(size=(rs.n_rows, 1))
+    else:
+        rs = systems.lscm_system(20, 17, seed=8)
+        rs.rhs = np.random.default_rng(2).normal(size=(rs.n_rows, 3))
+        rs.values = np.random.default_rng(3).normal(size=(3, rs.n_vars))
+    rp, ci, va, rhs = oracle_mod.assemble_rowstream(rs)
+    M, grhs, _ = solver.assemble(rs)
+    g_rp, g_ci, g_va = M.download()
+    assert np.array_equal(g_rp, rp) and np.array_equal(g_ci, ci)
+    assert np.array_equal(g_va, va) and np.array_equal(grhs, rhs)
+
+
+def test_assembly_rejects_bad_indices(gpu_ok):
+    rs = systems.lscm_system(6, 6, seed=1)
+    rs.var = rs.var.copy()
+    rs.var[3] = rs.n_vars + 5
+    with pytest.raises(Exception):
+        solver.assemble(rs)
+
+
+# ---------------------------------------------------------------------------
+# SpMV
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("tpr", [1, 2, 4, 8, 16, 32])
+def test_spmv_matches_oracle_every_layout(gpu_ok, oracle_mod, tpr):
+    fs = systems.fairing_system(70, 53, seed=4)
+    A = solver.Matrix(fs.rp, fs.ci, fs.va)
+    A.set_layout(tpr, 512)
+    x = np.random.default_rng(tpr).normal(size=fs.n)
+    y = A.spmv(x)
+    yo = oracle_mod.spmv(fs.rp, fs.ci, fs.va, x)
+    absrow = oracle_mod.spmv(fs.rp, fs.ci, np.abs(fs.va), np.abs(x))
+    assert np.all(np.abs(y - yo) <= 1e-14 * absrow + 1e-300)
+
+
+def test_spmv_ragged_rows_and_empty_rows(gpu_ok, oracle_mod):
+    rng = np.random.default_rng(5)
+    n = 3000
+    lens = rng.integers(0, 70, n)
+    lens[::97] = 0                                   # empty rows
+    rp = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    ci = rng.integers(0, n, rp[-1]).astype(np.int32)
+    va = rng.normal(size=rp[-1])
+    A = solver.Matrix(rp, ci, va)
+    x = rng.normal(size=n)
+    y = A.spmv(x)
+    yo = oracle_mod.spmv(rp, ci, va, x)
+    absrow = oracle_mod.spmv(rp, ci, np.abs(va), np.abs(x))
+    assert np.all(np.abs(y - yo) <= 1e-14 * absrow + 1e-300)
+    assert np.all(y[lens == 0] == 0.0)
+
+
+# ---------------------------------------------------------------------------
+# PCG solves
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("name", golden_names())
+def test_plain_pcg_golden(gpu_ok, oracle_mod, name):
+    rs, exp = load_golden(name)
+    vals, info = solver.solve_opennl(rs, precision="double", eps=1e-12)
+    assert info["ok"], info
+    for s in range(rs.n_systems):
+        ref = exp["solution"][s]
+        got = vals[s][rs.locked == 0]
+        assert rel(got, ref) <= 1e-8, (name, s, rel(got, ref))
+    if "exact" in exp:
+        ex = exp["exact"] if exp["exact"].shape[0] == rs.n_vars else None
+        if ex is not None:
+            assert np.abs(vals[0] - ex).max() < 1e-9
+
+
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+@pytest.mark.parametrize("case", ["lscm_48x40", "fairing_96x80", "voxel"])
+def test_pcg_matches_oracle_and_direct(gpu_ok, oracle_mod, precision, case):
+    if case == "lscm_48x40":
+        rs = systems.lscm_system(48, 40, seed=12)
+    elif case == "fairing_96x80":
+        rs = systems.fairing_system(96, 80, seed=13).to_rows()
+    else:
+        rs = systems.voxel_rows(10, 9, 8, seed=6, locked_fraction=0.3)
+    rp, ci, va, rhs = oracle_mod.assemble_rowstream(rs)
+    vals, info = solver.solve_opennl(rs, precision=precision, eps=1e-10)
+    assert info["ok"], info
+    assert info["true_error"] <= 1e-10 * (1.0 + 1e-6) or precision == "double"
+    for s in range(rs.n_systems):
+        x_gpu = vals[s][rs.locked == 0]
+        x_dir = oracle_mod.direct_solve(rp, ci, va, rhs[s])
+        x_cpu, st, it, rr = oracle_mod.pcg(rp, ci, va, rhs[s], eps=1e-10)
+        assert st == 1
+        assert rel(x_gpu, x_dir) <= 1e-8, (case, precision, rel(x_gpu, x_dir))
+        assert rel(x_gpu, x_cpu) <= 1e-8, (case, precision, rel(x_gpu, x_cpu))
+        if precision == "double":
+            # same algorithm, same stopping rule: iteration counts agree closely
+            assert abs(info["iterations"] / rs.n_systems - it) <= max(3, 0.02 * it)
+
+
+def test_plain_pcg_is_deterministic(gpu_ok):
+    fs = systems.fairing_system(120, 100, seed=2)
+    A = solver.Matrix(fs.rp, fs.ci, fs.va)
+    x1, i1 = A.solve(fs.rhs[0])
+    x2, i2 = A.solve(fs.rhs[0])
+    assert np.array_equal(x1, x2) and i1.iterations == i2.iterations
+
+
+def test_mixed_reports_refinement(gpu_ok, oracle_mod):
+    fs = systems.fairing_system(128, 128, seed=3)
+    A = solver.Matrix(fs.rp, fs.ci, fs.va)
+    x, info = A.solve(fs.rhs[1], precision="mixed", eps=1e-10)
+    assert info.status == "converged" and info.refinement_steps >= 2
+    assert info.true_rel_residual <= 1e-10
+    x_dir = oracle_mod.direct_solve(fs.rp, fs.ci, fs.va, fs.rhs[1])
+    assert rel(x, x_dir) <= 1e-8
+
+
+# ---------------------------------------------------------------------------
+# edge cases
+# ---------------------------------------------------------------------------
+def test_zero_rhs_gives_zero(gpu_ok):
+    fs = systems.fairing_system(30, 30, seed=1)
+    A = solver.Matrix(fs.rp, fs.ci, fs.va)
+    for prec in ("double", "mixed"):
+        x, info = A.solve(np.zeros(fs.n), x0=np.ones(fs.n), precision=prec)
+        assert info.status == "converged" and info.iterations == 0 and not x.any()
+
+
+def test_start_at_solution_and_max_iter_zero(gpu_ok, oracle_mod):
+    fs = systems.fairing_system(30, 30, seed=1)
+    A = solver.Matrix(fs.rp, fs.ci, fs.va)
+    xs = oracle_mod.direct_solve(fs.rp, fs.ci, fs.va, fs.rhs[0])
+    x, info = A.solve(fs.rhs[0], x0=xs, eps=1e-8)
+    assert info.status == "converged" and info.iterations == 0
+    x, info = A.solve(fs.rhs[0], max_iter=0)
+    assert info.status == "max_iter" and info.iterations == 0
+    x, info = A.solve(fs.rhs[0], max_iter=7)
+    assert info.status == "max_iter" and info.iterations == 7
+
+
+def test_breakdown_on_nan_and_indefinite(gpu_ok):
+    fs = systems.fairing_system(20, 20, seed=1)
+    A = solver.Matrix(fs.rp, fs.ci, fs.va)
+    b = fs.rhs[0].copy()
+    b[5] = np.nan
+    x, info = A.solve(b)
+    assert info.status == "breakdown"
+    rp = np.array([0, 1, 2], np.int32); ci = np.array([0, 1], np.int32)
+    B = solver.Matrix(rp, ci, np.array([1.0, -1.0]))
+    x, info = B.solve(np.array([1.0, 1.0]))
+    assert info.status == "breakdown"
+
+
+def test_all_variables_locked(gpu_ok):
+    nl.nlNewContext()
+    nl.nlSolverParameteri(nl.NL_NB_VARIABLES, 2)
+    nl.nlSolverParameteri(nl.NL_LEAST_SQUARES, nl.NL_TRUE)
+    nl.nlBegin(nl.NL_SYSTEM)
+    nl.nlSetVariable(0, 1.0); nl.nlSetVariable(1, 2.0)
+    nl.nlLockVariable(0); nl.nlLockVariable(1)
+    nl.nlBegin(nl.NL_MATRIX)
+    nl.nlBegin(nl.NL_ROW); nl.nlCoefficient(0, 1.0); nl.nlCoefficient(1, 1.0); nl.nlEnd(nl.NL_ROW)
+    nl.nlEnd(nl.NL_MATRIX); nl.nlEnd(nl.NL_SYSTEM)
+    assert nl.nlSolve() == 1
+    assert nl.nlGetVariable(0) == 1.0 and nl.nlGetVariable(1) == 2.0
+    nl.nlDeleteContext(nl.nlGetCurrent())
+
+
+# ---------------------------------------------------------------------------
+# the reference's call sequences
+# ---------------------------------------------------------------------------
+def test_warpdrive_call_sequence_per_call(gpu_ok, oracle_mod):
+    """voxel_grob_transport_commands.cpp:231-287, one C call per coefficient."""
+    rs, exp = load_golden("voxel_6x5x4")
+    vals, info = solver.solve_opennl(rs, eps=1e-12, per_call=True)
+    assert info["ok"]
+    got = vals[0][rs.locked == 0]
+    assert rel(got, exp["solution"][0]) <= 1e-9
+    # locked voxels keep their values
+    assert np.array_equal(vals[0][rs.locked == 1], rs.values[0][rs.locked == 1])
+
+
+def test_bulk_rows_equal_per_call(gpu_ok):
+    rs = systems.lscm_system(10, 9, seed=4)
+    a, ia = solver.solve_opennl(rs, per_call=False)
+    b, ib = solver.solve_opennl(rs, per_call=True)
+    assert np.array_equal(a, b) and ia["iterations"] == ib["iterations"]
+
+
+def test_scripting_matrix_api(gpu_ok, oracle_mod):
+    """OGF::NL::Matrix path: nlSparseMatrixNew/Add, compress, mult,
+    solve_iterative(CG, Jacobi) = nlSolveSystemIterative(nlHostBlas(), ...)."""
+    fs = systems.fairing_system(25, 22, seed=9)
+    M = nl.nlSparseMatrixNew(fs.n, fs.n, nl.NL_MATRIX_STORE_ROWS)
+    for i in range(fs.n):
+        for k in range(fs.rp[i], fs.rp[i + 1]):
+            nl.nlSparseMatrixAdd(M, i, int(fs.ci[k]), float(fs.va[k]))
+    x = np.random.default_rng(0).normal(size=fs.n)
+    y = np.zeros(fs.n)
+    nl.nlMultMatrixVector(M, x, y)                 # dynamic matrix
+    assert rel(y, oracle_mod.spmv(fs.rp, fs.ci, fs.va, x)) < 1e-14
+    M = nl.nlMatrixCompress(M)
+    y2 = np.zeros(fs.n)
+    nl.nlMultMatrixVector(M, x, y2)
+    assert rel(y2, y) < 1e-14
+    P = nl.nlNewJacobiPreconditioner(M)
+    sol = np.zeros(fs.n)
+    its = nl.nlSolveSystemIterative(nl.nlHostBlas(), M, P, fs.rhs[0], sol, nl.NL_CG, 1e-10,
+                                    5 * fs.n, 5)
+    assert its > 0
+    xd = oracle_mod.direct_solve(fs.rp, fs.ci, fs.va, fs.rhs[0])
+    assert rel(sol, xd) <= 1e-8
+    sol2 = np.zeros(fs.n)                          # unpreconditioned CG (P = NULL)
+    nl.nlSolveSystemIterative(nl.nlHostBlas(), M, None, fs.rhs[0], sol2, nl.NL_CG, 1e-10, 5 * fs.n, 5)
+    assert rel(sol2, xd) <= 1e-8
+    nl.nlDeleteMatrix(P)
+    nl.nlDeleteMatrix(M)
+
+
+def test_blas_table(gpu_ok):
+    import ctypes
+    from graphitethree_gb300 import _lib
+    L = _lib.load()
+    tbl = L.nlHostBlas()
+    blas = ctypes.cast(tbl, ctypes.POINTER(ctypes.c_void_p))
+    # function pointers in the NLBlas table order: copy, scal, dot, nrm2, axpy, mul
+    F = ctypes.CFUNCTYPE
+    dot = F(ctypes.c_double, ctypes.c_void_p, ctypes.c_int, _lib.f64p, ctypes.c_int, _lib.f64p,
+            ctypes.c_int)(blas[2])
+    axpy = F(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_double, _lib.f64p, ctypes.c_int,
+             _lib.f64p, ctypes.c_int)(blas[4])
+    x = np.arange(1000, dtype=np.float64)
+    y = np.ones(1000)
+    assert abs(dot(tbl, 1000, x.ctypes.data_as(_lib.f64p), 1, y.ctypes.data_as(_lib.f64p), 1)
+               - x.sum()) < 1e-9
+    axpy(tbl, 1000, 2.0, x.ctypes.data_as(_lib.f64p), 1, y.ctypes.data_as(_lib.f64p), 1)
+    assert np.array_equal(y, 1.0 + 2.0 * x)
