@@ -125,6 +125,9 @@ _SIGS = {
     "nlgb_spmv32_timed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, f64p]),
     "nlgb_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(NlgbParams),
                              C.POINTER(NlgbResult)]),
+    "nlgb_batch_solve": (C.c_int, [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                   C.POINTER(C.c_void_p), C.POINTER(NlgbParams),
+                                   C.POINTER(NlgbResult), f64p]),
     "nlgb_assemble": (C.c_int, [C.c_int, C.c_longlong, i64p, i32p, f64p, f64p, f64p, C.c_int,
                                 C.c_int, f64p, C.c_int, C.POINTER(C.c_void_p), f64p, f64p]),
     "nlgb_add_rows": (C.c_int, [C.c_longlong, i64p, i32p, f64p, f64p, f64p]),

@@ -64,7 +64,9 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         if name.endswith(".cu"):
             cmd = [nvcc, *ARCH, "-lineinfo", *common, "-c", str(src), "-o", str(obj)]
         else:
-            cmd = [nvcc, *common, "-Xcompiler", "-Wall", "-x", "c++", "-c", str(src), "-o", str(obj)]
+            # host code that includes the device-side structs: compiled as CUDA
+            cmd = [nvcc, *ARCH, *common, "-Xcompiler", "-Wall", "-x", "cu", "-c", str(src),
+                   "-o", str(obj)]
         jobs.append((obj, src, cmd))
 
     def run(job):

@@ -104,8 +104,8 @@ struct Context {
   int nb_systems = 1;
   bool symmetric = false;
   int precision = NL_GB300_PRECISION_DOUBLE;
-  double inner_threshold = 1e-5;
-  int max_refinement = 40;
+  double inner_threshold = 0.1;
+  int max_refinement = 100000;
   int tpr_override = 0;
   bool verbose = false;
   bool normalize_rows = false;

@@ -1,6 +1,7 @@
 // nlgb_api.cpp -- explicit-handle C API (include/nl_gb300.h).
 #include "../../include/nl.h"
 #include "../../include/nl_gb300.h"
+#include "nlgb_batch.h"
 #include "nlgb_internal.h"
 
 #include <algorithm>
@@ -87,8 +88,8 @@ void nlgb_default_params(nlgb_params* p) {
   p->eps = 1e-10;
   p->max_iter = -1;
   p->precision = NL_GB300_PRECISION_DOUBLE;
-  p->inner_eps = 1e-5;
-  p->max_outer = 40;
+  p->inner_eps = 0.1;
+  p->max_outer = 100000;
 }
 
 nlgb_matrix nlgb_matrix_create(int n_rows, int n_cols, const int* rp, const int* ci,
@@ -155,8 +156,8 @@ int nlgb_matrix_set_layout(nlgb_matrix A, int tpr, int tile_rows) {
   if (!A) return fail(NLGB_E_INVALID, "nlgb_matrix_set_layout: null matrix");
   if (tpr != 0 && tpr != 1 && tpr != 2 && tpr != 4 && tpr != 8 && tpr != 16 && tpr != 32)
     return fail(NLGB_E_INVALID, "threads_per_row must be 0 or a power of two <= 32");
-  if (tile_rows != 0 && (tile_rows < 512 || tile_rows % 512 != 0 || tile_rows > (1 << 20)))
-    return fail(NLGB_E_INVALID, "tile_rows must be a positive multiple of 512");
+  if (tile_rows != 0 && (tile_rows < 64 || (tile_rows & (tile_rows - 1)) != 0 || tile_rows > (1 << 20)))
+    return fail(NLGB_E_INVALID, "tile_rows must be a power of two in [64, 2^20]");
   if (tpr) A->A.tpr = tpr;
   if (tile_rows) A->A.tile_rows = tile_rows;
   A->bound = false;   // the solver's graphs embed the layout
@@ -267,6 +268,72 @@ int nlgb_solve(nlgb_matrix A, const double* b, double* x, const nlgb_params* prm
     res->seconds = r.seconds;
   }
   return NLGB_OK;
+}
+
+int nlgb_batch_solve(int n_sys, const nlgb_matrix* A, const double* const* b, double* const* x,
+                     const nlgb_params* prm, nlgb_result* res, double* kernel_seconds) {
+  if (n_sys < 0 || (n_sys > 0 && (!A || !b || !x))) return fail(NLGB_E_INVALID, "nlgb_batch_solve: bad arguments");
+  for (int i = 0; i < n_sys; ++i) {
+    if (!A[i] || !b[i] || !x[i]) return fail(NLGB_E_INVALID, "nlgb_batch_solve: null matrix or vector");
+    if (A[i]->A.n != A[i]->A.m) return fail(NLGB_E_INVALID, "nlgb_batch_solve: matrix is not square");
+  }
+  nlgb_params p;
+  nlgb_default_params(&p);
+  if (prm) p = *prm;
+  if (p.precision != NL_GB300_PRECISION_DOUBLE && p.precision != NL_GB300_PRECISION_MIXED)
+    return fail(NLGB_E_INVALID, "nlgb_batch_solve: unknown precision");
+  if (n_sys == 0) return NLGB_OK;
+  if (!ensure_ready()) return NLGB_E_DEVICE;
+  const bool mixed = p.precision == NL_GB300_PRECISION_MIXED;
+  SolveParams sp;
+  sp.eps = p.eps; sp.max_iter = p.max_iter; sp.precision = p.precision;
+  sp.inner_eps = p.inner_eps; sp.max_outer = p.max_outer;
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return NLGB_E_DEVICE;
+  std::vector<SystemSlot> slots((size_t)n_sys);
+  std::vector<SysView> views((size_t)n_sys);
+  std::vector<long long> work((size_t)n_sys);
+  int rc = NLGB_OK;
+  {
+    BatchRunner runner;
+    if (runner.init(s) != cudaSuccess) rc = NLGB_E_DEVICE;
+    for (int i = 0; i < n_sys && rc == NLGB_OK; ++i) {
+      DeviceCRS& M = A[i]->A;
+      if (crs_prepare(M, mixed, s) != cudaSuccess || slots[i].alloc(&M, mixed, s) != cudaSuccess ||
+          slots[i].start(b[i], x[i], sp, s) != cudaSuccess) {
+        rc = NLGB_E_DEVICE;
+        break;
+      }
+      views[i] = slots[i].view;
+      work[i] = M.nnz + 8LL * M.n;
+    }
+    BatchLaunchStats st;
+    if (rc == NLGB_OK && runner.run(views, work, 0, &st) != cudaSuccess) rc = NLGB_E_DEVICE;
+    if (rc == NLGB_OK && kernel_seconds) *kernel_seconds = st.ms * 1e-3;
+    std::vector<SysState> hs((size_t)n_sys);
+    for (int i = 0; i < n_sys && rc == NLGB_OK; ++i) {
+      if (cudaMemcpyAsync(x[i], slots[i].view.x, sizeof(double) * A[i]->A.n, cudaMemcpyDefault, s) != cudaSuccess ||
+          cudaMemcpyAsync(&hs[i], slots[i].view.st, sizeof(SysState), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        rc = NLGB_E_DEVICE;
+    }
+    if (rc == NLGB_OK && cudaStreamSynchronize(s) != cudaSuccess) rc = NLGB_E_DEVICE;
+    if (rc == NLGB_OK && res) {
+      for (int i = 0; i < n_sys; ++i) {
+        const SysState& h = hs[i];
+        res[i].status = h.status;
+        res[i].iterations = h.iter;
+        res[i].refinement_steps = h.outer;
+        res[i].rel_residual = h.bnorm2 > 0 ? std::sqrt(h.rr / h.bnorm2) : 0.0;
+        res[i].true_rel_residual = h.bnorm2 > 0 ? std::sqrt(h.rr_true / h.bnorm2) : 0.0;
+        res[i].seconds = st.ms * 1e-3;
+      }
+    }
+    for (auto& sl : slots) sl.release(s);
+    cudaStreamSynchronize(s);
+  }
+  cudaStreamDestroy(s);
+  if (rc != NLGB_OK && std::string(last_error()).empty()) set_error(cudaGetErrorString(cudaGetLastError()));
+  return rc;
 }
 
 int nlgb_assemble(int least_squares, long long n_rows, const long long* row_ptr, const int* col,

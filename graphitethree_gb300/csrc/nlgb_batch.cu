@@ -1,0 +1,539 @@
+// nlgb_batch.cu -- many independent Jacobi-PCG systems in one persistent
+// kernel launch (plain FP64 or mixed FP32/FP64 per system).
+//
+// Reference context: geogram's mesh_make_atlas solves one LSCM system per
+// chart, one after another, each through nlSolve (called from
+// src/lib/OGF/mesh/commands/mesh_grob_surface_commands.cpp:724); a GPU that
+// runs them one at a time is launch- and latency-bound on the small charts.
+//
+// Layout of one launch (grid = every co-resident CTA, cooperative launch):
+//   * large systems get a static "team" of k CTAs; the team synchronises its
+//     phases with a global-memory barrier (bounded spin, then an error flag);
+//   * every other CTA is a queue worker: it pops the next small system from
+//     an atomic queue and runs it alone (phases separated by __syncthreads).
+// Each system's iteration is the same sequence of tile procedures and scalar
+// steps as the single-system solver (nlgb_solver.cu), with the same tiles
+// and the same canonical reductions, so a system's iterates do not depend on
+// the team size, on the other systems in the launch or on where an epoch
+// boundary falls: a result is bit-identical alone and in any mix.
+// Every CTA of a team computes the scalars redundantly from the tile
+// partials; rank 0 stores the system state back to HBM.
+#include "nlgb_batch.h"
+#include "nlgb_core.cuh"
+#include "nlgb_internal.h"
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+
+namespace nlgb {
+
+namespace {
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+constexpr unsigned long long kBarrierTimeoutNs = 4000000000ULL;   // 4 s
+
+// Team barrier.  k == 1: a CTA barrier.  Returns false (in every thread) if
+// the wait timed out or another CTA already flagged an error.
+__device__ bool team_sync(TeamBar* bar, int k, int* err) {
+  if (k == 1) {
+    __syncthreads();
+    return true;
+  }
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    const unsigned int gen = *((volatile unsigned int*)&bar->gen);
+    __threadfence();
+    const unsigned int arrived = atomicAdd(&bar->count, 1u);
+    if (arrived == (unsigned int)k - 1u) {
+      bar->count = 0u;
+      __threadfence();
+      atomicAdd(&bar->gen, 1u);
+    } else {
+      const unsigned long long t0 = globaltimer_ns();
+      while (*((volatile unsigned int*)&bar->gen) == gen) {
+        if (*((volatile int*)err) != 0) { ok = 0; break; }
+        if (globaltimer_ns() - t0 > kBarrierTimeoutNs) {
+          atomicExch(err, 1);
+          ok = 0;
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// Runtime dispatch of the SpMV tile procedures on the system's threads-per-row
+// (coherent gathers: x and p were written earlier in this kernel).
+#define NLGB_TPR_SWITCH(...)                                            \
+  switch (s.tpr) {                                                      \
+    case 1: { constexpr int T = 1; __VA_ARGS__; } break;                \
+    case 2: { constexpr int T = 2; __VA_ARGS__; } break;                \
+    case 4: { constexpr int T = 4; __VA_ARGS__; } break;                \
+    case 8: { constexpr int T = 8; __VA_ARGS__; } break;                \
+    case 16: { constexpr int T = 16; __VA_ARGS__; } break;              \
+    default: { constexpr int T = 32; __VA_ARGS__; } break;              \
+  }
+
+__device__ void put_parts(const SysView& s, int tile, int slot, const double* v, int K) {
+  if (threadIdx.x == 0)
+    for (int k = 0; k < K; ++k) __stcg(s.part + (size_t)tile * kParts + slot + k, v[k]);
+}
+
+template <int K>
+__device__ void get_sums(const SysView& s, int slot, double (&o)[K]) {
+  int comp[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) comp[k] = slot + k;
+  canon_reduce<K>(s.part, s.n_tiles, comp, o);
+}
+
+// Thread 0 applies a scalar step to the CTA's shared copy of the state; the
+// barrier after it publishes the result to the other threads.
+#define NLGB_SCALAR(stmt)        \
+  if (threadIdx.x == 0) { stmt; } \
+  __syncthreads();
+
+// One system, run by a team (rank r of k CTAs) for at most `budget`
+// iterations.  st: the CTA's shared-memory copy of the system state.
+__device__ void run_system(const SysView& s, SysState* st, int r, int k, TeamBar* bar, int* err,
+                           long long budget) {
+  const bool mixed = st->precision == 1;
+  long long done_iters = 0;
+  if (st->stage == 0) {
+    if (!mixed) {
+      for (int t = r; t < s.n_tiles; t += k) {
+        double v[3];
+        NLGB_TPR_SWITCH(tile_residual<T, true>(s, t, v));
+        put_parts(s, t, kSlotInit, v, 3);
+      }
+      if (!team_sync(bar, k, err)) { NLGB_SCALAR(st->status = ST_DEVICE_ERR; st->stage = 3); return; }
+      double o[3];
+      get_sums<3>(s, kSlotInit, o);
+      NLGB_SCALAR(scalar_after_init(st, o[0], o[1], o[2]); st->stage = st->status == ST_RUNNING ? 1 : 2);
+    } else {
+      // initial FP64 residual (first "reliable update"; c = 0, p = 0)
+      for (int t = r; t < s.n_tiles; t += k) {
+        double v[4];
+        NLGB_TPR_SWITCH(tile_mx_outer<T, true>(s, t, v));
+        put_parts(s, t, kSlotInit, v, 4);
+      }
+      if (!team_sync(bar, k, err)) { NLGB_SCALAR(st->status = ST_DEVICE_ERR; st->stage = 3); return; }
+      double o[4];
+      get_sums<4>(s, kSlotInit, o);
+      NLGB_SCALAR(st->mode = 0; scalar_after_outer(st, o[0], o[1], o[2], o[3]);
+                  st->stage = st->status == ST_RUNNING ? 1 : 2);
+    }
+  }
+  while (st->stage == 1 && (budget <= 0 || done_iters < budget)) {
+    if (!mixed) {
+      // q = A p, p.q
+      for (int t = r; t < s.n_tiles; t += k) {
+        double v[1];
+        NLGB_TPR_SWITCH(v[0] = tile_spmv_pq<T, true>(s, t));
+        put_parts(s, t, kSlotPQ, v, 1);
+      }
+      if (!team_sync(bar, k, err)) break;
+      {
+        double o[1];
+        get_sums<1>(s, kSlotPQ, o);
+        NLGB_SCALAR(scalar_after_pq(st, o[0]));
+      }
+      if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
+      const double alpha = st->alpha;
+      for (int t = r; t < s.n_tiles; t += k) {
+        double v[2];
+        tile_update_xr(s, t, alpha, v);
+        put_parts(s, t, kSlotXR, v, 2);
+      }
+      if (!team_sync(bar, k, err)) break;
+      {
+        double o[2];
+        get_sums<2>(s, kSlotXR, o);
+        NLGB_SCALAR(scalar_after_xr(st, o[0], o[1]));
+      }
+      ++done_iters;
+      if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
+      const double beta = st->beta;
+      for (int t = r; t < s.n_tiles; t += k) tile_update_p(s, t, beta);
+      if (!team_sync(bar, k, err)) break;
+    } else {
+      // FP32 PCG iteration with FP64 reliable updates; same phase order as
+      // the graph solver: p update, SpMV + p.q, c/r update, [update].
+      {
+        const double beta = st->beta;
+        for (int t = r; t < s.n_tiles; t += k) tile_mx_update_p(s, t, beta);
+        if (!team_sync(bar, k, err)) break;
+      }
+      for (int t = r; t < s.n_tiles; t += k) {
+        double v[1];
+        NLGB_TPR_SWITCH(v[0] = tile_mx_spmv_pq<T, true>(s, t));
+        put_parts(s, t, kSlotPQ, v, 1);
+      }
+      if (!team_sync(bar, k, err)) break;
+      {
+        double o[1];
+        get_sums<1>(s, kSlotPQ, o);
+        NLGB_SCALAR(scalar_after_pq(st, o[0]));
+      }
+      if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
+      const double alpha = st->alpha;
+      for (int t = r; t < s.n_tiles; t += k) {
+        double v[2];
+        tile_mx_update_cr(s, t, alpha, v);
+        put_parts(s, t, kSlotXR, v, 2);
+      }
+      if (!team_sync(bar, k, err)) break;
+      {
+        double o[2];
+        get_sums<2>(s, kSlotXR, o);
+        NLGB_SCALAR(scalar_after_mx_cr(st, o[0], o[1]));
+      }
+      ++done_iters;
+      if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
+      if (st->mode == 0) {
+        // reliable update: x += c, r = b - A x in FP64, FP32 residual replaced
+        for (int t = r; t < s.n_tiles; t += k) tile_mx_apply(s, t);
+        if (!team_sync(bar, k, err)) break;
+        for (int t = r; t < s.n_tiles; t += k) {
+          double v[4];
+          NLGB_TPR_SWITCH(tile_mx_outer<T, true>(s, t, v));
+          put_parts(s, t, kSlotInit, v, 4);
+        }
+        if (!team_sync(bar, k, err)) break;
+        double o[4];
+        get_sums<4>(s, kSlotInit, o);
+        NLGB_SCALAR(scalar_after_outer(st, o[0], o[1], o[2], o[3]));
+        if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
+      }
+    }
+  }
+  if (*((volatile int*)err) != 0 && st->stage != 3) {
+    NLGB_SCALAR(st->status = ST_DEVICE_ERR; st->stage = 3);
+    return;
+  }
+  if (st->stage == 2) {
+    // final true residual (FP64) of the returned x; x = 0 when b == 0
+    for (int t = r; t < s.n_tiles; t += k) {
+      double v[1] = {0.0};
+      if (st->zero_rhs) {
+        tile_zero_x(s, t);
+      } else {
+        NLGB_TPR_SWITCH(v[0] = tile_true_rr<T, true>(s, t));
+      }
+      put_parts(s, t, kSlotFinal, v, 1);
+    }
+    if (!team_sync(bar, k, err)) { NLGB_SCALAR(st->status = ST_DEVICE_ERR; st->stage = 3); return; }
+    double o[1];
+    get_sums<1>(s, kSlotFinal, o);
+    NLGB_SCALAR(st->rr_true = o[0]; st->stage = 3);
+  }
+}
+
+__global__ void __launch_bounds__(kCTA) k_batch(BatchArgs a) {
+  __shared__ SysView sv;
+  __shared__ SysState sst;
+  __shared__ int pick;
+  const int cta = blockIdx.x;
+  auto load = [&](int sys) {
+    if (threadIdx.x == 0) {
+      sv = a.views[sys];
+      sst = *sv.st;
+    }
+    __syncthreads();
+  };
+  auto store = [&](bool rank0) {
+    __syncthreads();
+    if (rank0 && threadIdx.x == 0) {
+      *sv.st = sst;
+      __threadfence();
+    }
+    __syncthreads();
+  };
+  if (cta < a.team_ctas) {
+    const int team = a.cta_team[cta];
+    const TeamDesc td = a.teams[team];
+    const int r = cta - td.cta_begin;
+    for (int j = td.sys_begin; j < td.sys_end; ++j) {
+      load(a.team_sys[j]);
+      if (sst.stage != 3) run_system(sv, &sst, r, td.k, a.bars + team, a.err, a.budget);
+      store(r == 0);
+    }
+  } else {
+    while (true) {
+      if (threadIdx.x == 0) pick = (int)atomicAdd(a.queue_head, 1u);
+      __syncthreads();
+      const int q = pick;
+      __syncthreads();
+      if (q >= a.n_queue) break;
+      load(a.queue[q]);
+      if (sst.stage != 3) run_system(sv, &sst, 0, 1, nullptr, a.err, a.budget);
+      store(true);
+    }
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host side.
+// ---------------------------------------------------------------------------
+BatchRunner::~BatchRunner() {
+  cudaFree(d_views_); cudaFree(d_teams_); cudaFree(d_cta_team_); cudaFree(d_team_sys_);
+  cudaFree(d_queue_); cudaFree(d_bars_); cudaFree(d_ctl_);
+  if (h_err_) cudaFreeHost(h_err_);
+  if (ev0_) cudaEventDestroy(ev0_);
+  if (ev1_) cudaEventDestroy(ev1_);
+}
+
+cudaError_t BatchRunner::init(cudaStream_t s) {
+  stream_ = s;
+  int dev = 0;
+  NLGB_CUDA_TRY(cudaGetDevice(&dev));
+  NLGB_CUDA_TRY(cudaDeviceGetAttribute(&n_sm_, cudaDevAttrMultiProcessorCount, dev));
+  int per_sm = 0;
+  NLGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, kCTA, 0));
+  per_sm_ = std::max(1, per_sm);
+  grid_ = n_sm_ * per_sm_;
+  NLGB_CUDA_TRY(cudaMalloc(&d_ctl_, 2 * sizeof(int)));
+  NLGB_CUDA_TRY(cudaMallocHost(&h_err_, sizeof(int)));
+  *h_err_ = 0;
+  NLGB_CUDA_TRY(cudaEventCreate(&ev0_));
+  NLGB_CUDA_TRY(cudaEventCreate(&ev1_));
+  return cudaSuccess;
+}
+
+template <typename T>
+static cudaError_t ensure(T*& p, size_t& cap, size_t n) {
+  if (n <= cap && p) return cudaSuccess;
+  cudaFree(p);
+  p = nullptr;
+  cap = std::max<size_t>(n, 16);
+  return cudaMalloc(&p, cap * sizeof(T));
+}
+
+void BatchRunner::plan(const std::vector<SysView>& views, const std::vector<long long>& work,
+                       int reserve_queue_ctas) {
+  // Large systems: more tiles than a CTA should carry per phase.
+  teams_.clear(); cta_team_.clear(); team_sys_.clear(); queue_.clear();
+  const int n = (int)views.size();
+  std::vector<int> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::sort(order.begin(), order.end(), [&](int a, int b) { return work[a] > work[b]; });
+  std::vector<int> large;
+  for (int i : order) {
+    if (views[i].n_tiles >= kLargeTiles) large.push_back(i);
+    else queue_.push_back(i);
+  }
+  const int avail = std::max(0, grid_ - (queue_.empty() ? 0 : std::max(reserve_queue_ctas, 1)));
+  if (!large.empty() && avail > 0) {
+    // CTAs proportional to work, at least 2 and at most one per 2 tiles.
+    long long total = 0;
+    for (int i : large) total += std::max(1LL, work[i]);
+    std::vector<int> kk(large.size());
+    int used = 0;
+    for (size_t t = 0; t < large.size(); ++t) {
+      const int i = large[t];
+      long long want = (long long)((double)avail * (double)std::max(1LL, work[i]) / (double)total);
+      want = std::min<long long>(want, std::max(1, views[i].n_tiles / 2));
+      kk[t] = (int)std::max(2LL, want);
+      used += kk[t];
+    }
+    // Too many CTAs requested (minimum of 2 each): trim the largest teams,
+    // then send what still does not fit to the queue.
+    while (used > avail) {
+      size_t big = std::max_element(kk.begin(), kk.end()) - kk.begin();
+      if (kk[big] <= 2) break;
+      kk[big] -= 1;
+      used -= 1;
+    }
+    int cta = 0;
+    for (size_t t = 0; t < large.size(); ++t) {
+      if (cta + kk[t] > avail) { queue_.push_back(large[t]); continue; }
+      TeamDesc td;
+      td.cta_begin = cta;
+      td.k = kk[t];
+      td.sys_begin = (int)team_sys_.size();
+      team_sys_.push_back(large[t]);
+      td.sys_end = (int)team_sys_.size();
+      for (int c = 0; c < td.k; ++c) cta_team_.push_back((int)teams_.size());
+      teams_.push_back(td);
+      cta += td.k;
+    }
+  } else {
+    for (int i : large) queue_.push_back(i);
+  }
+}
+
+cudaError_t BatchRunner::run(const std::vector<SysView>& views, const std::vector<long long>& work,
+                             long long budget, BatchLaunchStats* stats) {
+  NLGB_CUDA_TRY(launch(views, work, budget));
+  return finish(stats);
+}
+
+cudaError_t BatchRunner::launch(const std::vector<SysView>& views, const std::vector<long long>& work,
+                                long long budget) {
+  pending_ = false;
+  if (views.empty()) return cudaSuccess;
+  plan(views, work, std::max(n_sm_, (int)std::min<size_t>(views.size(), (size_t)grid_ / 2)));
+  NLGB_CUDA_TRY(ensure(d_views_, cap_views_, views.size()));
+  NLGB_CUDA_TRY(ensure(d_teams_, cap_teams_, teams_.size()));
+  NLGB_CUDA_TRY(ensure(d_cta_team_, cap_cta_team_, cta_team_.size()));
+  NLGB_CUDA_TRY(ensure(d_team_sys_, cap_team_sys_, team_sys_.size()));
+  NLGB_CUDA_TRY(ensure(d_queue_, cap_queue_, queue_.size()));
+  NLGB_CUDA_TRY(ensure(d_bars_, cap_bars_, teams_.size()));
+  cudaStream_t s = stream_;
+  NLGB_CUDA_TRY(cudaMemcpyAsync(d_views_, views.data(), views.size() * sizeof(SysView), cudaMemcpyHostToDevice, s));
+  if (!teams_.empty()) {
+    NLGB_CUDA_TRY(cudaMemcpyAsync(d_teams_, teams_.data(), teams_.size() * sizeof(TeamDesc), cudaMemcpyHostToDevice, s));
+    NLGB_CUDA_TRY(cudaMemcpyAsync(d_cta_team_, cta_team_.data(), cta_team_.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    NLGB_CUDA_TRY(cudaMemcpyAsync(d_team_sys_, team_sys_.data(), team_sys_.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    NLGB_CUDA_TRY(cudaMemsetAsync(d_bars_, 0, teams_.size() * sizeof(TeamBar), s));
+  }
+  if (!queue_.empty())
+    NLGB_CUDA_TRY(cudaMemcpyAsync(d_queue_, queue_.data(), queue_.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+  NLGB_CUDA_TRY(cudaMemsetAsync(d_ctl_, 0, 2 * sizeof(int), s));
+  BatchArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.views = d_views_;
+  a.teams = d_teams_;
+  a.cta_team = d_cta_team_;
+  a.team_sys = d_team_sys_;
+  a.queue = d_queue_;
+  a.bars = d_bars_;
+  a.err = d_ctl_;
+  a.queue_head = reinterpret_cast<unsigned int*>(d_ctl_ + 1);
+  a.team_ctas = (int)cta_team_.size();
+  a.n_queue = (int)queue_.size();
+  a.budget = budget;
+  // Grid: every team CTA plus queue workers, never more than can be resident.
+  const int workers = queue_.empty() ? 0 : std::min(grid_ - a.team_ctas, (int)queue_.size());
+  const int grid = a.team_ctas + std::max(0, workers);
+  void* args[] = {&a};
+  NLGB_CUDA_TRY(cudaEventRecord(ev0_, s));
+  NLGB_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_batch, dim3(grid), dim3(kCTA), args, 0, s));
+  NLGB_CUDA_TRY(cudaEventRecord(ev1_, s));
+  NLGB_CUDA_TRY(cudaMemcpyAsync(h_err_, d_ctl_, sizeof(int), cudaMemcpyDeviceToHost, s));
+  last_grid_ = grid;
+  last_workers_ = workers;
+  pending_ = true;
+  return cudaSuccess;
+}
+
+cudaError_t BatchRunner::finish(BatchLaunchStats* stats) {
+  if (!pending_) {
+    if (stats) *stats = BatchLaunchStats();
+    return cudaSuccess;
+  }
+  pending_ = false;
+  NLGB_CUDA_TRY(cudaStreamSynchronize(stream_));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ev0_, ev1_);
+  const int err = *h_err_;
+  if (stats) {
+    stats->ms = ms;
+    stats->n_teams = (int)teams_.size();
+    stats->team_ctas = (int)cta_team_.size();
+    stats->queue_ctas = last_workers_;
+    stats->error = err;
+    stats->grid = last_grid_;
+  }
+  if (err) {
+    set_error("batched solve: a team barrier timed out");
+    return cudaErrorLaunchTimeout;
+  }
+  return cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------
+// Per-system device slot.
+// ---------------------------------------------------------------------------
+static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+size_t SystemSlot::bytes_for(int n, int tile_rows, bool mixed) {
+  const size_t n8 = align256((size_t)std::max(2, n + 2) * sizeof(double));
+  const size_t n4 = align256((size_t)std::max(4, n + 4) * sizeof(float));
+  const int n_tiles = std::max(1, (n + tile_rows - 1) / tile_rows);
+  const size_t parts = align256((size_t)n_tiles * kParts * sizeof(double));
+  const size_t st = align256(sizeof(SysState));
+  return mixed ? (2 * n8 + 4 * n4 + parts + st) : (5 * n8 + parts + st);
+}
+
+cudaError_t SystemSlot::alloc(DeviceCRS* Am, bool mx, cudaStream_t s) {
+  A = Am;
+  mixed = mx;
+  const int n = A->n;
+  bytes = bytes_for(n, A->tile_rows, mixed);
+  NLGB_CUDA_TRY(cudaMallocAsync(&block, bytes, s));
+  char* p = static_cast<char*>(block);
+  const size_t n8 = align256((size_t)std::max(2, n + 2) * sizeof(double));
+  const size_t n4 = align256((size_t)std::max(4, n + 4) * sizeof(float));
+  std::memset(&view, 0, sizeof(view));
+  view.n = n;
+  view.tile_rows = A->tile_rows;
+  view.n_tiles = std::max(1, (n + A->tile_rows - 1) / A->tile_rows);
+  view.tpr = A->tpr;
+  view.rp = A->rp; view.ci = A->ci; view.va = A->va; view.va32 = A->va32;
+  view.dinv = A->dinv; view.dinv32 = A->dinv32;
+  view.b = reinterpret_cast<double*>(p); p += n8;
+  view.x = reinterpret_cast<double*>(p); p += n8;
+  if (mixed) {
+    view.r32 = reinterpret_cast<float*>(p); p += n4;
+    view.p32 = reinterpret_cast<float*>(p); p += n4;
+    view.q32 = reinterpret_cast<float*>(p); p += n4;
+    view.c32 = reinterpret_cast<float*>(p); p += n4;
+  } else {
+    view.r = reinterpret_cast<double*>(p); p += n8;
+    view.p = reinterpret_cast<double*>(p); p += n8;
+    view.q = reinterpret_cast<double*>(p); p += n8;
+  }
+  view.part = reinterpret_cast<double*>(p);
+  p += align256((size_t)view.n_tiles * kParts * sizeof(double));
+  view.st = reinterpret_cast<SysState*>(p);
+  return cudaSuccess;
+}
+
+cudaError_t SystemSlot::start(const double* b, const double* x0, const SolveParams& prm,
+                              cudaStream_t s) {
+  const size_t n = (size_t)view.n;
+  NLGB_CUDA_TRY(cudaMemcpyAsync(const_cast<double*>(view.b), b, n * sizeof(double), cudaMemcpyDefault, s));
+  if (x0) NLGB_CUDA_TRY(cudaMemcpyAsync(view.x, x0, n * sizeof(double), cudaMemcpyDefault, s));
+  else NLGB_CUDA_TRY(cudaMemsetAsync(view.x, 0, n * sizeof(double), s));
+  if (mixed) {
+    NLGB_CUDA_TRY(cudaMemsetAsync(view.p32, 0, n * sizeof(float), s));
+    NLGB_CUDA_TRY(cudaMemsetAsync(view.c32, 0, n * sizeof(float), s));
+  }
+  SysState h;
+  std::memset(&h, 0, sizeof(h));
+  const long long max_iter = prm.max_iter >= 0 ? prm.max_iter : 5LL * view.n;
+  h.thresh2 = prm.eps * prm.eps;
+  h.max_iter = max_iter;
+  h.status = ST_RUNNING;
+  h.max_outer = std::max(1, prm.max_outer);
+  h.in_thresh2 = prm.inner_eps * prm.inner_eps;
+  h.in_max = (int)std::max(1LL, std::min<long long>(max_iter, 1000));
+  h.precision = mixed ? 1 : 0;
+  h.stage = 0;
+  // cudaMemcpyAsync from pageable memory is staged synchronously, so the
+  // stack copy may go out of scope after the call.
+  NLGB_CUDA_TRY(cudaMemcpyAsync(view.st, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+  return cudaSuccess;
+}
+
+void SystemSlot::release(cudaStream_t s) {
+  if (block) cudaFreeAsync(block, s);
+  block = nullptr;
+}
+
+}  // namespace nlgb

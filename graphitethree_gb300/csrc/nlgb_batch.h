@@ -1,0 +1,112 @@
+// nlgb_batch.h -- host/device interface of the persistent batched solver.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "nlgb_core.cuh"
+
+namespace nlgb {
+
+// Systems with at least this many tiles get a multi-CTA team; smaller ones
+// are popped from the queue by single CTAs.
+constexpr int kLargeTiles = 16;
+
+struct TeamBar {
+  unsigned int count;
+  unsigned int gen;
+};
+
+struct TeamDesc {
+  int cta_begin;
+  int k;          // CTAs in the team
+  int sys_begin;  // range in team_sys
+  int sys_end;
+};
+
+struct BatchArgs {
+  const SysView* views;
+  const TeamDesc* teams;
+  const int* cta_team;       // team of each team CTA
+  const int* team_sys;       // system indices handled by teams, grouped by team
+  const int* queue;          // system indices handled by queue workers
+  TeamBar* bars;
+  int* err;                  // nonzero: a barrier timed out
+  unsigned int* queue_head;
+  int team_ctas;
+  int n_queue;
+  long long budget;          // iterations per system in this launch (<= 0: no limit)
+};
+
+struct BatchLaunchStats {
+  double ms = 0;
+  int n_teams = 0;
+  int team_ctas = 0;
+  int queue_ctas = 0;
+  int grid = 0;
+  int error = 0;
+};
+
+// Device storage of one system's Krylov state: a single stream-ordered
+// allocation (cudaMallocAsync, pooled) carved into 256-byte aligned arrays.
+// FP64 plain: b, x, r, p, q; mixed: b, x, r32, p32, q32, c32; plus the tile
+// partials and the SysState.
+struct SolveParams;
+struct DeviceCRS;
+struct SystemSlot {
+  DeviceCRS* A = nullptr;
+  void* block = nullptr;
+  size_t bytes = 0;
+  bool mixed = false;
+  SysView view{};
+  static size_t bytes_for(int n, int tile_rows, bool mixed);
+  cudaError_t alloc(DeviceCRS* A, bool mixed, cudaStream_t s);
+  // b, x0: host or device vectors of n doubles (x0 may be null: zero start).
+  cudaError_t start(const double* b, const double* x0, const SolveParams& prm, cudaStream_t s);
+  void release(cudaStream_t s);
+};
+
+// Launches the persistent kernel over a set of resident systems.  Each
+// system's SysState (device) must be initialised by the caller (status
+// ST_RUNNING, stage 0, thresholds, max_iter, precision); the state is read
+// at the start and written back at the end of every launch, so a system can
+// be advanced over several launches (epochs) with identical results.
+class BatchRunner {
+ public:
+  BatchRunner() = default;
+  ~BatchRunner();
+  BatchRunner(const BatchRunner&) = delete;
+  BatchRunner& operator=(const BatchRunner&) = delete;
+
+  cudaError_t init(cudaStream_t s);
+  // work[i]: relative cost estimate of system i (rows x expected iterations).
+  // run() = launch() + finish().  Between the two the host may queue other
+  // work (uploads of new requests) on other streams.
+  cudaError_t run(const std::vector<SysView>& views, const std::vector<long long>& work,
+                  long long budget, BatchLaunchStats* stats);
+  cudaError_t launch(const std::vector<SysView>& views, const std::vector<long long>& work,
+                     long long budget);
+  cudaError_t finish(BatchLaunchStats* stats);
+  int max_grid() const { return grid_; }
+
+ private:
+  void plan(const std::vector<SysView>& views, const std::vector<long long>& work,
+            int reserve_queue_ctas);
+
+  cudaStream_t stream_ = nullptr;
+  int n_sm_ = 0, per_sm_ = 0, grid_ = 0;
+  std::vector<TeamDesc> teams_;
+  std::vector<int> cta_team_, team_sys_, queue_;
+  SysView* d_views_ = nullptr;
+  TeamDesc* d_teams_ = nullptr;
+  int *d_cta_team_ = nullptr, *d_team_sys_ = nullptr, *d_queue_ = nullptr, *d_ctl_ = nullptr;
+  TeamBar* d_bars_ = nullptr;
+  size_t cap_views_ = 0, cap_teams_ = 0, cap_cta_team_ = 0, cap_team_sys_ = 0, cap_queue_ = 0,
+         cap_bars_ = 0;
+  cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+  int* h_err_ = nullptr;           // pinned
+  int last_grid_ = 0, last_workers_ = 0;
+  bool pending_ = false;
+};
+
+}  // namespace nlgb

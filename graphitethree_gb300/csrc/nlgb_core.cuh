@@ -21,7 +21,14 @@ namespace nlgb {
 
 constexpr int kCTA = 256;            // threads per CTA for every solver kernel
 constexpr int kWarps = kCTA / 32;
-constexpr int kParts = 4;            // partial-sum slots per tile
+constexpr int kParts = 8;            // partial-sum slots per tile
+// Slots used by each phase.  Consecutive phases use disjoint slots, so in the
+// persistent kernel a CTA may start writing the next phase's partials while
+// a slower CTA of its team is still reducing the previous phase's.
+constexpr int kSlotPQ = 0;           // p.q                  (1 value)
+constexpr int kSlotXR = 1;           // r.z, r.r             (2 values)
+constexpr int kSlotFinal = 3;        // ||b - A x||^2        (1 value)
+constexpr int kSlotInit = 4;         // b.b, r.z, r.r / mixed outer: 4 values
 
 enum : int {
   ST_RUNNING = 0,
@@ -55,6 +62,8 @@ struct __align__(16) SysState {
   int zero_rhs;                // b == 0: the solution is x = 0
   int stall;                   // mixed: outer steps in a row without progress
   unsigned int cnt[4];         // last-CTA counters of the phase kernels
+  int stage;                   // batched: 0 start, 1 iterating, 2 final residual due, 3 done
+  int precision;               // batched: 0 FP64, 1 mixed
 };
 
 // Everything a tile procedure needs about one system.
@@ -325,8 +334,10 @@ __device__ __forceinline__ void tile_mx_apply(const SysView& s, int tile) {
     });
 }
 
-// Outer step: r64 = b - A64 x (FP64), r32 = float(r64), p32 = D^-1 r32.
-// Returns (b.b, ||r64||^2, r32.z32, ||r32||^2) -- all accumulated in FP64.
+// Reliable update: r64 = b - A64 x (FP64), r32 = float(r64).  The search
+// direction p32 is kept (the Krylov recurrence continues on the corrected
+// residual).  Returns (b.b, ||r64||^2, r32.z32, ||r32||^2), all accumulated
+// in FP64.
 template <int T, bool kCoh = false>
 __device__ void tile_mx_outer(const SysView& s, int tile, double (&out)[4]) {
   const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
@@ -343,7 +354,6 @@ __device__ void tile_mx_outer(const SysView& s, int tile, double (&out)[4]) {
       const float r32 = float(ri);
       const float z32 = s.dinv32[row] * r32;
       s.r32[row] = r32;
-      s.p32[row] = z32;
       out[0] = fma(bi, bi, out[0]);
       out[1] = fma(ri, ri, out[1]);
       out[2] = fma(double(z32), double(r32), out[2]);
@@ -466,7 +476,18 @@ __device__ __forceinline__ void scalar_after_xr(SysState* st, double rz, double 
   st->rho = rz;
 }
 
-// Mixed: after the FP64 outer residual.  Returns through st->mode / status.
+// Mixed precision = FP32 PCG with FP64 reliable updates (defect correction
+// that keeps the Krylov direction): the inner iteration runs on FP32 values
+// and vectors; whenever its FP32 residual has dropped by in_thresh since the
+// last update (or claims convergence), the FP32 correction is added to the
+// FP64 solution, the true residual b - A x is recomputed in FP64 and replaces
+// the FP32 residual, and the iteration continues with the same p.  Restarted
+// refinement (a fresh inner PCG per outer step) loses the Krylov space each
+// time and stagnates on the ill-conditioned LSCM normal equations; the
+// continued recurrence keeps FP64-like iteration counts.
+//
+// After a reliable update (FP64 residual rr64, new FP32 residual's r.z and
+// r.r).  The first call (outer == 0) is the initial residual.
 __device__ __forceinline__ void scalar_after_outer(SysState* st, double bb, double rr64,
                                                    double rz32, double rr32) {
   if (st->outer == 0) st->bnorm2 = bb;
@@ -481,29 +502,32 @@ __device__ __forceinline__ void scalar_after_outer(SysState* st, double bb, doub
   if (rr64 <= st->thresh2 * bb0) { st->status = ST_CONVERGED; return; }
   if (st->iter >= st->max_iter) { st->status = ST_MAX_ITER; return; }
   if (st->outer >= st->max_outer) { st->status = ST_STAGNATION; return; }
-  // Stagnation: three outer steps in a row without halving the residual.
-  if (st->outer > 0 && rr64 > 0.25 * st->rr64_prev) {
+  // Stagnation: many updates in a row that do not improve on the best
+  // true residual seen so far.
+  if (st->outer > 0 && !(rr64 < st->rr64_prev)) {
     st->stall += 1;
-    if (st->stall >= 3) { st->status = ST_STAGNATION; return; }
+    if (st->stall >= 8) { st->status = ST_STAGNATION; return; }
   } else {
     st->stall = 0;
+    st->rr64_prev = rr64;
   }
-  st->rr64_prev = rr64;
-  st->outer += 1;
   if (!finite_pos(rz32) || !finite_pos(rr32)) { st->status = ST_BREAKDOWN; return; }
+  st->beta = (st->outer == 0) ? 0.0 : rz32 / st->rho;
   st->rho = rz32;
-  st->in_rr0 = rr32;
+  st->in_rr0 = rr32;     // FP32 residual^2 right after this update
   st->in_iter = 0;
+  st->outer += 1;
   st->mode = 1;
 }
 
-// Mixed inner: after the FP32 vector update.  mode -> 0 ends the inner solve.
+// After the FP32 vector update: either continue (beta from the FP32
+// residual) or request a reliable update (mode -> 0).
 __device__ __forceinline__ void scalar_after_mx_cr(SysState* st, double rz, double rr) {
   st->iter += 1;
   st->in_iter += 1;
   if (!(rr <= 1.0e300)) { st->status = ST_BREAKDOWN; return; }
-  if (rr <= st->in_thresh2 * st->in_rr0 || st->in_iter >= st->in_max ||
-      st->iter >= st->max_iter || !finite_pos(rz)) {
+  if (rr <= st->in_thresh2 * st->in_rr0 || rr <= st->thresh2 * st->bnorm2 ||
+      st->in_iter >= st->in_max || st->iter >= st->max_iter || !finite_pos(rz)) {
     st->mode = 0;
     return;
   }

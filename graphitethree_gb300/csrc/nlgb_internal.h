@@ -59,8 +59,8 @@ struct SolveParams {
   double eps = 1e-10;
   long long max_iter = -1;     // -1: 5 n
   int precision = 0;           // 0 FP64, 1 mixed
-  double inner_eps = 1e-5;
-  int max_outer = 40;
+  double inner_eps = 0.1;      // mixed: reliable update when the FP32 residual fell by this factor
+  int max_outer = 100000;      // mixed: cap on reliable updates
   int tpr = 0;                 // 0: autotuned
 };
 

@@ -26,12 +26,12 @@ namespace nlgb {
 // every thread of the CTA that arrived last.
 // ---------------------------------------------------------------------------
 template <int K>
-__device__ __forceinline__ bool publish_elect(const SysView& s, int tile, const double (&v)[K],
+__device__ __forceinline__ bool publish_elect(const SysView& s, int tile, const double (&v)[K], int slot,
                                               unsigned int* counter) {
   __shared__ int am_last;
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int k = 0; k < K; ++k) __stcg(s.part + (size_t)tile * kParts + k, v[k]);
+    for (int k = 0; k < K; ++k) __stcg(s.part + (size_t)tile * kParts + slot + k, v[k]);
     __threadfence();
     const unsigned int prev = atomicAdd(counter, 1u);
     am_last = (prev == (unsigned int)s.n_tiles - 1u);
@@ -52,8 +52,8 @@ template <int T>
 __global__ void __launch_bounds__(kCTA) k_init(SysView s) {
   double v[3];
   tile_residual<T>(s, blockIdx.x, v);
-  if (publish_elect<3>(s, blockIdx.x, v, &s.st->cnt[0])) {
-    const int comp[3] = {0, 1, 2};
+  if (publish_elect<3>(s, blockIdx.x, v, kSlotInit, &s.st->cnt[0])) {
+    const int comp[3] = {kSlotInit, kSlotInit + 1, kSlotInit + 2};
     double o[3];
     canon_reduce<3>(s.part, s.n_tiles, comp, o);
     if (threadIdx.x == 0) scalar_after_init(s.st, o[0], o[1], o[2]);
@@ -64,8 +64,8 @@ template <int T>
 __global__ void __launch_bounds__(kCTA) k_spmv_pq(SysView s) {
   if (ld_status(s.st) != ST_RUNNING) return;
   double v[1] = {tile_spmv_pq<T>(s, blockIdx.x)};
-  if (publish_elect<1>(s, blockIdx.x, v, &s.st->cnt[1])) {
-    const int comp[1] = {0};
+  if (publish_elect<1>(s, blockIdx.x, v, kSlotPQ, &s.st->cnt[1])) {
+    const int comp[1] = {kSlotPQ};
     double o[1];
     canon_reduce<1>(s.part, s.n_tiles, comp, o);
     if (threadIdx.x == 0) scalar_after_pq(s.st, o[0]);
@@ -77,8 +77,8 @@ __global__ void __launch_bounds__(kCTA) k_update_xr(SysView s) {
   const double alpha = __ldcg(&s.st->alpha);
   double v[2];
   tile_update_xr(s, blockIdx.x, alpha, v);
-  if (publish_elect<2>(s, blockIdx.x, v, &s.st->cnt[2])) {
-    const int comp[2] = {0, 1};
+  if (publish_elect<2>(s, blockIdx.x, v, kSlotXR, &s.st->cnt[2])) {
+    const int comp[2] = {kSlotXR, kSlotXR + 1};
     double o[2];
     canon_reduce<2>(s.part, s.n_tiles, comp, o);
     if (threadIdx.x == 0) scalar_after_xr(s.st, o[0], o[1]);
@@ -116,8 +116,8 @@ __global__ void __launch_bounds__(kCTA) k_final(SysView s) {
   } else {
     v[0] = tile_true_rr<T>(s, blockIdx.x);
   }
-  if (publish_elect<1>(s, blockIdx.x, v, &s.st->cnt[3])) {
-    const int comp[1] = {0};
+  if (publish_elect<1>(s, blockIdx.x, v, kSlotFinal, &s.st->cnt[3])) {
+    const int comp[1] = {kSlotFinal};
     double o[1];
     canon_reduce<1>(s.part, s.n_tiles, comp, o);
     if (threadIdx.x == 0) s.st->rr_true = o[0];
@@ -127,25 +127,23 @@ __global__ void __launch_bounds__(kCTA) k_final(SysView s) {
 // ---------------------------------------------------------------------------
 // Mixed-precision kernels.
 // ---------------------------------------------------------------------------
+// Reliable update, part 1: x += c, c = 0 (only when an update is due).
 __global__ void __launch_bounds__(kCTA) k_mx_apply(SysView s) {
-  if (ld_status(s.st) != ST_RUNNING) return;
+  if (ld_status(s.st) != ST_RUNNING || ld_mode(s.st) != 0) return;
   tile_mx_apply(s, blockIdx.x);
 }
 
+// Reliable update, part 2: FP64 true residual, FP32 residual replaced.
 template <int T>
-__global__ void __launch_bounds__(kCTA) k_mx_outer(SysView s, cudaGraphConditionalHandle h_in) {
-  if (ld_status(s.st) != ST_RUNNING) return;
+__global__ void __launch_bounds__(kCTA) k_mx_outer(SysView s) {
+  if (ld_status(s.st) != ST_RUNNING || ld_mode(s.st) != 0) return;
   double v[4];
   tile_mx_outer<T>(s, blockIdx.x, v);
-  if (publish_elect<4>(s, blockIdx.x, v, &s.st->cnt[0])) {
-    const int comp[4] = {0, 1, 2, 3};
+  if (publish_elect<4>(s, blockIdx.x, v, kSlotInit, &s.st->cnt[0])) {
+    const int comp[4] = {kSlotInit, kSlotInit + 1, kSlotInit + 2, kSlotInit + 3};
     double o[4];
     canon_reduce<4>(s.part, s.n_tiles, comp, o);
-    if (threadIdx.x == 0) {
-      scalar_after_outer(s.st, o[0], o[1], o[2], o[3]);
-      const bool inner = s.st->status == ST_RUNNING && s.st->mode == 1;
-      cudaGraphSetConditional(h_in, inner ? 1u : 0u);
-    }
+    if (threadIdx.x == 0) scalar_after_outer(s.st, o[0], o[1], o[2], o[3]);
   }
 }
 
@@ -153,24 +151,30 @@ template <int T>
 __global__ void __launch_bounds__(kCTA) k_mx_spmv_pq(SysView s) {
   if (ld_status(s.st) != ST_RUNNING || ld_mode(s.st) != 1) return;
   double v[1] = {tile_mx_spmv_pq<T>(s, blockIdx.x)};
-  if (publish_elect<1>(s, blockIdx.x, v, &s.st->cnt[1])) {
-    const int comp[1] = {0};
+  if (publish_elect<1>(s, blockIdx.x, v, kSlotPQ, &s.st->cnt[1])) {
+    const int comp[1] = {kSlotPQ};
     double o[1];
     canon_reduce<1>(s.part, s.n_tiles, comp, o);
     if (threadIdx.x == 0) scalar_after_pq(s.st, o[0]);
   }
 }
 
-__global__ void __launch_bounds__(kCTA) k_mx_update_cr(SysView s) {
+// c += a p, r -= a q; the last CTA decides whether a reliable update is due
+// and sets the condition of the IF node that runs it.
+__global__ void __launch_bounds__(kCTA) k_mx_update_cr(SysView s, cudaGraphConditionalHandle h_upd) {
   if (ld_status(s.st) != ST_RUNNING || ld_mode(s.st) != 1) return;
   const double alpha = __ldcg(&s.st->alpha);
   double v[2];
   tile_mx_update_cr(s, blockIdx.x, alpha, v);
-  if (publish_elect<2>(s, blockIdx.x, v, &s.st->cnt[2])) {
-    const int comp[2] = {0, 1};
+  if (publish_elect<2>(s, blockIdx.x, v, kSlotXR, &s.st->cnt[2])) {
+    const int comp[2] = {kSlotXR, kSlotXR + 1};
     double o[2];
     canon_reduce<2>(s.part, s.n_tiles, comp, o);
-    if (threadIdx.x == 0) scalar_after_mx_cr(s.st, o[0], o[1]);
+    if (threadIdx.x == 0) {
+      scalar_after_mx_cr(s.st, o[0], o[1]);
+      const bool upd = s.st->status == ST_RUNNING && s.st->mode == 0;
+      cudaGraphSetConditional(h_upd, upd ? 1u : 0u);
+    }
   }
 }
 
@@ -245,9 +249,10 @@ static int grid_for(long long n, int threads) {
 }
 
 TuneChoice autotune(int n, long long nnz, int max_row, const int* hist33) {
-  // Threads per row: the smallest power of two covering ~half of the typical
-  // row (each lane then does about two fused multiply-adds, which keeps two
-  // independent loads in flight per lane), raised when long rows dominate.
+  // Threads per row: the smallest power of two with at most ~4 nonzeros per
+  // lane for the typical row (measured on GB300 with the 7-nonzero cotangent
+  // Laplacian: 2 threads/row 4.3 TB/s, 4 -> 2.6, 8 -> 1.4), raised when
+  // long rows dominate.
   long long cnt = 0, acc = 0;
   for (int b = 0; b < 33; ++b) { cnt += hist33 ? hist33[b] : 0; acc += hist33 ? (long long)hist33[b] * b : 0; }
   const double mean = n > 0 ? double(nnz) / double(n) : 0.0;
@@ -261,10 +266,12 @@ TuneChoice autotune(int n, long long nnz, int max_row, const int* hist33) {
   }
   const double typical = std::max(mean, 0.75 * double(p90 == 32 ? std::max(32, max_row) : p90));
   int tpr = 1;
-  while (tpr < 32 && tpr * 2 < typical) tpr *= 2;
-  // Tile rows: about one resident wave of CTAs on 152 SMs, 512..4096 rows.
+  while (tpr < 32 && tpr * 4 < typical) tpr *= 2;
+  // Tile rows: enough tiles for about one resident wave of CTAs on the 152
+  // SMs (more, smaller tiles for mid-size systems, which are latency-bound),
+  // 128..4096 rows.
   long long want = (long long)n / (152LL * 6);
-  int tile = 512;
+  int tile = 128;
   while (tile < 4096 && tile < want) tile *= 2;
   (void)acc;
   return TuneChoice{tpr, tile};
@@ -386,19 +393,25 @@ static cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, cudaGraphNod
   return cudaGraphAddKernelNode(node, g, dep ? &dep : nullptr, dep ? 1 : 0, &kp);
 }
 
-static cudaError_t add_while(cudaGraph_t g, cudaGraphNode_t* node, cudaGraphNode_t dep,
-                             cudaGraphConditionalHandle h, cudaGraph_t* body) {
+static cudaError_t add_cond(cudaGraph_t g, cudaGraphNode_t* node, cudaGraphNode_t dep,
+                            cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+                            cudaGraph_t* body) {
   alignas(cudaGraphNodeParams) unsigned char raw[sizeof(cudaGraphNodeParams)];
   std::memset(raw, 0, sizeof(raw));
   cudaGraphNodeParams* cp = reinterpret_cast<cudaGraphNodeParams*>(raw);
   cp->type = cudaGraphNodeTypeConditional;
   cp->conditional.handle = h;
-  cp->conditional.type = cudaGraphCondTypeWhile;
+  cp->conditional.type = type;
   cp->conditional.size = 1;
   cudaError_t e = cudaGraphAddNode(node, g, dep ? &dep : nullptr, nullptr, dep ? 1 : 0, cp);
   if (e != cudaSuccess) return e;
   *body = cp->conditional.phGraph_out[0];
   return cudaSuccess;
+}
+
+static cudaError_t add_while(cudaGraph_t g, cudaGraphNode_t* node, cudaGraphNode_t dep,
+                             cudaGraphConditionalHandle h, cudaGraph_t* body) {
+  return add_cond(g, node, dep, h, cudaGraphCondTypeWhile, body);
 }
 
 template <int T> struct PlainKernels {
@@ -421,6 +434,7 @@ static KernelSet kernels_for(int tpr) {
 
 constexpr int kUnrollPlain = 4;   // CG iterations per while-body pass
 constexpr int kUnrollInner = 4;
+constexpr long long kMaxItersBetweenUpdates = 1000;   // mixed: forced reliable update
 
 PcgSolver::~PcgSolver() { release(); }
 
@@ -526,37 +540,38 @@ cudaError_t PcgSolver::build_mixed_graph() {
   SysView v = make_view(A_, tile_rows_, n_tiles_, b_, x_, r_, p_, q_, r32_, p32_, q32_, c32_,
                         part_, st_, abort_flag_);
   const KernelSet ks = kernels_for(tpr_);
+  // [initial FP64 residual] -> while { ( p update ; q = A32 p, p.q ;
+  //   c/r update -> IF(update due) { x += c ; FP64 residual } ) x U ; guard }
+  // -> final FP64 residual.
   cudaGraph_t g;
   NLGB_CUDA_TRY(cudaGraphCreate(&g, 0));
-  cudaGraphConditionalHandle h_out;
-  NLGB_CUDA_TRY(cudaGraphConditionalHandleCreate(&h_out, g, 1u, cudaGraphCondAssignDefault));
+  cudaGraphConditionalHandle h_loop;
+  NLGB_CUDA_TRY(cudaGraphConditionalHandleCreate(&h_loop, g, 1u, cudaGraphCondAssignDefault));
   void* a1[] = {&v};
-  cudaGraphNode_t n_outer_loop, n_fin;
-  cudaGraph_t obody;
-  NLGB_CUDA_TRY(add_while(g, &n_outer_loop, nullptr, h_out, &obody));
-  cudaGraphConditionalHandle h_in;
-  NLGB_CUDA_TRY(cudaGraphConditionalHandleCreate(&h_in, obody, 0u, cudaGraphCondAssignDefault));
-  cudaGraphNode_t n_apply, n_outer, n_inner_loop, n_og;
-  NLGB_CUDA_TRY(add_kernel(obody, &n_apply, nullptr, (const void*)k_mx_apply, n_tiles_, kCTA, a1));
-  void* ao[] = {&v, &h_in};
-  NLGB_CUDA_TRY(add_kernel(obody, &n_outer, n_apply, ks.mx_outer, n_tiles_, kCTA, ao));
-  cudaGraph_t ibody;
-  NLGB_CUDA_TRY(add_while(obody, &n_inner_loop, n_outer, h_in, &ibody));
+  cudaGraphNode_t n_first, n_loop, n_fin;
+  NLGB_CUDA_TRY(add_kernel(g, &n_first, nullptr, ks.mx_outer, n_tiles_, kCTA, a1));
+  cudaGraph_t body;
+  NLGB_CUDA_TRY(add_while(g, &n_loop, n_first, h_loop, &body));
   cudaGraphNode_t prev = nullptr;
+  cudaGraphConditionalHandle h_upd[kUnrollInner];
   for (int u = 0; u < kUnrollInner; ++u) {
-    cudaGraphNode_t n1, n2, n3;
-    NLGB_CUDA_TRY(add_kernel(ibody, &n1, prev, ks.mx_spmv, n_tiles_, kCTA, a1));
-    NLGB_CUDA_TRY(add_kernel(ibody, &n2, n1, (const void*)k_mx_update_cr, n_tiles_, kCTA, a1));
-    NLGB_CUDA_TRY(add_kernel(ibody, &n3, n2, (const void*)k_mx_update_p, n_tiles_, kCTA, a1));
-    prev = n3;
+    NLGB_CUDA_TRY(cudaGraphConditionalHandleCreate(&h_upd[u], body, 0u, cudaGraphCondAssignDefault));
+    cudaGraphNode_t n1, n2, n3, n_if, n4, n5;
+    NLGB_CUDA_TRY(add_kernel(body, &n1, prev, (const void*)k_mx_update_p, n_tiles_, kCTA, a1));
+    NLGB_CUDA_TRY(add_kernel(body, &n2, n1, ks.mx_spmv, n_tiles_, kCTA, a1));
+    void* acr[] = {&v, &h_upd[u]};
+    NLGB_CUDA_TRY(add_kernel(body, &n3, n2, (const void*)k_mx_update_cr, n_tiles_, kCTA, acr));
+    cudaGraph_t ubody;
+    NLGB_CUDA_TRY(add_cond(body, &n_if, n3, h_upd[u], cudaGraphCondTypeIf, &ubody));
+    NLGB_CUDA_TRY(add_kernel(ubody, &n4, nullptr, (const void*)k_mx_apply, n_tiles_, kCTA, a1));
+    NLGB_CUDA_TRY(add_kernel(ubody, &n5, n4, ks.mx_outer, n_tiles_, kCTA, a1));
+    prev = n_if;
   }
-  int need_inner = 1, need_any = -1;
-  void* agi[] = {&v, &h_in, &need_inner};
-  cudaGraphNode_t n_ig;
-  NLGB_CUDA_TRY(add_kernel(ibody, &n_ig, prev, (const void*)k_guard, 1, 1, agi));
-  void* ago[] = {&v, &h_out, &need_any};
-  NLGB_CUDA_TRY(add_kernel(obody, &n_og, n_inner_loop, (const void*)k_guard, 1, 1, ago));
-  NLGB_CUDA_TRY(add_kernel(g, &n_fin, n_outer_loop, ks.fin, n_tiles_, kCTA, a1));
+  int need_any = -1;
+  void* ag[] = {&v, &h_loop, &need_any};
+  cudaGraphNode_t n_g;
+  NLGB_CUDA_TRY(add_kernel(body, &n_g, prev, (const void*)k_guard, 1, 1, ag));
+  NLGB_CUDA_TRY(add_kernel(g, &n_fin, n_loop, ks.fin, n_tiles_, kCTA, a1));
   cudaError_t e = cudaGraphInstantiate(&mixed_exec_, g, 0);
   cudaGraphDestroy(g);
   NLGB_CUDA_TRY(e);
@@ -581,8 +596,9 @@ cudaError_t PcgSolver::solve(const double* b, double* x, const SolveParams& prm,
   h->mode = 0;
   h->max_outer = std::max(1, prm.max_outer);
   h->in_thresh2 = prm.inner_eps * prm.inner_eps;
-  h->in_max = (int)std::min<long long>(max_iter, 1LL << 30);
-  h->in_max = std::max(1, h->in_max);
+  // a reliable update at least every kMaxItersBetweenUpdates iterations
+  h->in_max = (int)std::max(1LL, std::min<long long>(max_iter, kMaxItersBetweenUpdates));
+  h->precision = mixed ? 1 : 0;
   // Hard cap on while-body passes: enough for max_iter iterations plus the
   // outer steps; reached only if the scalar logic failed to stop the loop.
   const int unroll = mixed ? kUnrollInner : kUnrollPlain;
@@ -590,7 +606,10 @@ cudaError_t PcgSolver::solve(const double* b, double* x, const SolveParams& prm,
   NLGB_CUDA_TRY(cudaMemcpyAsync(st_, h, sizeof(SysState), cudaMemcpyHostToDevice, stream_));
   NLGB_CUDA_TRY(cudaMemcpyAsync(b_, b, (size_t)n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
   NLGB_CUDA_TRY(cudaMemcpyAsync(x_, x, (size_t)n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
-  if (mixed) NLGB_CUDA_TRY(cudaMemsetAsync(c32_, 0, (size_t)n_ * sizeof(float), stream_));
+  if (mixed) {
+    NLGB_CUDA_TRY(cudaMemsetAsync(c32_, 0, (size_t)n_ * sizeof(float), stream_));
+    NLGB_CUDA_TRY(cudaMemsetAsync(p32_, 0, (size_t)n_ * sizeof(float), stream_));
+  }
   NLGB_CUDA_TRY(cudaEventRecord(ev0_, stream_));
   NLGB_CUDA_TRY(cudaGraphLaunch(mixed ? mixed_exec_ : plain_exec_, stream_));
   NLGB_CUDA_TRY(cudaEventRecord(ev1_, stream_));

@@ -114,7 +114,7 @@ class Matrix:
         return y
 
     def solve(self, b, x0=None, eps: float = 1e-10, max_iter: int = -1, precision: str = "double",
-              inner_eps: float = 1e-5, max_outer: int = 40):
+              inner_eps: float = 0.1, max_outer: int = 100000):
         """Solve A x = b.  Host numpy arrays in and out.  Returns (x, SolveInfo)."""
         L = _lib.load()
         b = np.ascontiguousarray(b, np.float64)
@@ -127,7 +127,7 @@ class Matrix:
                             r.rel_residual, r.true_rel_residual, r.seconds)
 
     def solve_device(self, b_ptr: int, x_ptr: int, eps: float = 1e-10, max_iter: int = -1,
-                     precision: str = "double", inner_eps: float = 1e-5, max_outer: int = 40):
+                     precision: str = "double", inner_eps: float = 0.1, max_outer: int = 100000):
         """Solve with device pointers (e.g. torch tensors' data_ptr())."""
         L = _lib.load()
         p = _lib.NlgbParams(eps, max_iter, PRECISION[precision], inner_eps, max_outer)
@@ -136,6 +136,28 @@ class Matrix:
                             ctypes.byref(r)), "nlgb_solve")
         return SolveInfo(STATUS.get(r.status, str(r.status)), r.iterations, r.refinement_steps,
                          r.rel_residual, r.true_rel_residual, r.seconds)
+
+
+def batch_solve(mats, bs, x0s=None, eps: float = 1e-10, max_iter: int = -1,
+                precision: str = "double", inner_eps: float = 0.1, max_outer: int = 100000):
+    """Solve many systems in one persistent-kernel launch.  mats: list of
+    Matrix (may repeat), bs: list of host vectors.  Returns (xs, infos,
+    kernel_seconds)."""
+    L = _lib.load()
+    n = len(mats)
+    bs = [np.ascontiguousarray(b, np.float64) for b in bs]
+    xs = [np.zeros(m.n) if x0s is None else np.array(x0s[i], np.float64, copy=True)
+          for i, m in enumerate(mats)]
+    A = (ctypes.c_void_p * n)(*[m.handle for m in mats])
+    B = (ctypes.c_void_p * n)(*[b.ctypes.data for b in bs])
+    X = (ctypes.c_void_p * n)(*[x.ctypes.data for x in xs])
+    p = _lib.NlgbParams(eps, max_iter, PRECISION[precision], inner_eps, max_outer)
+    R = (_lib.NlgbResult * n)()
+    secs = ctypes.c_double()
+    _check(L.nlgb_batch_solve(n, A, B, X, ctypes.byref(p), R, ctypes.byref(secs)), "nlgb_batch_solve")
+    infos = [SolveInfo(STATUS.get(r.status, str(r.status)), r.iterations, r.refinement_steps,
+                       r.rel_residual, r.true_rel_residual, r.seconds) for r in R]
+    return xs, infos, secs.value
 
 
 def assemble(rs: RowStream):

@@ -86,13 +86,13 @@ typedef void*          NLContext;
 #define NL_NB_SYSTEMS          0x10e
 /* library-specific parameters */
 #define NL_GB300_PRECISION         0x1a0 /* NL_GB300_PRECISION_DOUBLE/_MIXED */
-#define NL_GB300_INNER_THRESHOLD   0x1a1 /* mixed: inner FP32 PCG tolerance (default 1e-5) */
+#define NL_GB300_INNER_THRESHOLD   0x1a1 /* mixed: FP64 reliable update once the FP32 residual fell by this factor (default 0.1) */
 #define NL_GB300_REFINEMENT_STEPS  0x1a2 /* query: outer FP64 refinement steps used */
 #define NL_GB300_STATUS            0x1a3 /* query: NL_GB300_STATUS_* of the last solve */
 #define NL_GB300_TRUE_RESIDUAL     0x1a4 /* query: ||b-Ax||/||b|| recomputed in FP64 */
 #define NL_GB300_THREADS_PER_ROW   0x1a5 /* 0 = autotune (default), else 1..32 */
 #define NL_GB300_ASSEMBLY_TIME     0x1a6 /* query: seconds spent in GPU assembly */
-#define NL_GB300_MAX_REFINEMENT    0x1a7 /* mixed: cap on outer steps (default 40) */
+#define NL_GB300_MAX_REFINEMENT    0x1a7 /* mixed: cap on FP64 reliable updates (default 100000) */
 
 #define NL_GB300_PRECISION_DOUBLE 0x0
 #define NL_GB300_PRECISION_MIXED  0x1

@@ -32,8 +32,8 @@ typedef struct {
     double    eps;            /* stop when ||b-Ax|| <= eps ||b||           */
     long long max_iter;       /* < 0: 5 n                                  */
     int       precision;      /* NL_GB300_PRECISION_DOUBLE / _MIXED        */
-    double    inner_eps;      /* mixed: inner FP32 tolerance (1e-5)        */
-    int       max_outer;      /* mixed: refinement cap (40)                */
+    double    inner_eps;      /* mixed: reliable-update factor (0.1)       */
+    int       max_outer;      /* mixed: cap on reliable updates (100000)   */
 } nlgb_params;
 
 typedef struct {
@@ -59,7 +59,7 @@ void        nlgb_matrix_destroy(nlgb_matrix A);
 int         nlgb_matrix_info(nlgb_matrix A, int* n_rows, long long* nnz, int* threads_per_row,
                              int* tile_rows);
 /* Override the autotuner (threads_per_row in {1,2,4,8,16,32}, tile_rows a
- * multiple of 512; 0 keeps the current value). */
+ * power of two in [64, 2^20]; 0 keeps the current value). */
 int         nlgb_matrix_set_layout(nlgb_matrix A, int threads_per_row, int tile_rows);
 /* Copy the CRS arrays back to host buffers of size n+1 / nnz / nnz. */
 int         nlgb_matrix_download(nlgb_matrix A, int* rp, int* ci, double* va);
@@ -79,6 +79,18 @@ int nlgb_spmv32_timed(nlgb_matrix A, const float* x, float* y, int reps, double*
  * x holds the initial guess on entry and the solution on exit. */
 int nlgb_solve(nlgb_matrix A, const double* b, double* x, const nlgb_params* prm,
                nlgb_result* res);
+
+/* ---- many independent solves in one persistent-kernel launch ----
+ * The batched form of nlSolveSystemIterative for many uneven systems, e.g.
+ * the per-chart LSCM solves of mesh_make_atlas (called at
+ * src/lib/OGF/mesh/commands/mesh_grob_surface_commands.cpp:724).  A[i] may
+ * repeat (several right-hand sides of one matrix).  b[i], x[i]: host or
+ * device vectors of A[i]'s size; x[i] is the initial guess on entry.  Each
+ * system converges (or stops) on its own; results are bit-identical to
+ * nlgb_solve on the same system.  *kernel_seconds: device time of the
+ * launch (CUDA events). */
+int nlgb_batch_solve(int n_sys, const nlgb_matrix* A, const double* const* b, double* const* x,
+                     const nlgb_params* prm, nlgb_result* res, double* kernel_seconds);
 
 /* ---- least-squares / square assembly on the GPU (nlEnd(NL_MATRIX) of an
  * NL_LEAST_SQUARES context, voxel_grob_transport_commands.cpp:232-279) ----

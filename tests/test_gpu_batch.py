@@ -1,0 +1,63 @@
+"""Batched persistent-kernel solver: every system's result must be
+bit-identical to the single-system solver on the same system (same tiles,
+same canonical reductions, same scalar steps), whatever the team layout and
+the rest of the batch; and correct against the oracle."""
+import numpy as np
+import pytest
+
+from graphitethree_gb300 import solver, systems
+
+pytestmark = pytest.mark.gpu
+
+
+def _mix():
+    """Uneven systems: tiny and small (queue workers) and larger (teams)."""
+    out = []
+    for nx, ny, seed in [(12, 9, 1), (40, 33, 2), (90, 70, 3)]:
+        fs = systems.fairing_system(nx, ny, seed=seed)
+        out.append((solver.Matrix(fs.rp, fs.ci, fs.va), fs.rhs[0]))
+        out.append((out[-1][0], fs.rhs[2]))            # second RHS, same matrix
+    for side, seed in [(10, 4), (24, 5), (64, 6)]:
+        M, rhs, _ = solver.assemble(systems.lscm_system(side, side + 3, seed=seed))
+        out.append((M, rhs[0]))
+    return out
+
+
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+def test_batch_bit_identical_to_single(gpu_ok, precision):
+    items = _mix()
+    xs, infos, secs = solver.batch_solve([m for m, _ in items], [b for _, b in items],
+                                         precision=precision)
+    assert secs > 0
+    for (M, b), x, info in zip(items, xs, infos):
+        x1, i1 = M.solve(b, precision=precision)
+        assert info.status == "converged", info
+        assert info.iterations == i1.iterations, (info, i1)
+        assert np.array_equal(x, x1)
+
+
+def test_batch_matches_oracle(gpu_ok, oracle_mod):
+    rs = systems.lscm_system(50, 41, seed=9)
+    rp, ci, va, rhs = oracle_mod.assemble_rowstream(rs)
+    M, grhs, _ = solver.assemble(rs)
+    fs = systems.fairing_system(80, 80, seed=3)
+    F = solver.Matrix(fs.rp, fs.ci, fs.va)
+    for precision in ("double", "mixed"):
+        xs, infos, _ = solver.batch_solve([M, F, F, F], [grhs[0], *fs.rhs], precision=precision)
+        xd = oracle_mod.direct_solve(rp, ci, va, rhs[0])
+        assert np.linalg.norm(xs[0] - xd) / np.linalg.norm(xd) <= 1e-8
+        for k in range(3):
+            xf = oracle_mod.direct_solve(fs.rp, fs.ci, fs.va, fs.rhs[k])
+            assert np.linalg.norm(xs[1 + k] - xf) / np.linalg.norm(xf) <= 1e-8
+            if precision == "mixed":
+                assert infos[1 + k].true_rel_residual <= 1e-10
+
+
+def test_batch_edge_cases(gpu_ok):
+    fs = systems.fairing_system(30, 30, seed=1)
+    F = solver.Matrix(fs.rp, fs.ci, fs.va)
+    xs, infos, _ = solver.batch_solve([F, F], [np.zeros(fs.n), fs.rhs[0]], max_iter=5)
+    assert infos[0].status == "converged" and infos[0].iterations == 0 and not xs[0].any()
+    assert infos[1].status == "max_iter" and infos[1].iterations == 5
+    xs, infos, _ = solver.batch_solve([], [])
+    assert xs == [] and infos == []
