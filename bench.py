@@ -1,0 +1,344 @@
+#!/usr/bin/env python3
+"""Benchmark: solves/s and p99 latency at relative residual 1e-10 on the
+serving stream (batched mixed-precision server vs plain FP64 GPU PCG).
+
+Workload (one "step"): a seeded sample of R requests drawn from the serving
+stream's distribution -- LSCM parameterisation or cotangent-Laplacian
+fairing (3 right-hand sides) with probability 1/2 each, vertex counts
+log-uniform in [1e3, 1e6], square-ish grid patches with the seeded bump
+model, Poisson arrivals at `--rate` per second -- submitted through the C ABI
+(nlgb_server_submit_rows / _crs with host buffers) to the continuous-batching
+server (HBM budget 150 GB, mixed precision with FP64 fallback) and drained.
+Every step re-submits the same sample from scratch (assembly, upload, solve,
+download: nothing is cached).
+
+Reported:
+  value       R / (device time of the server's persistent-kernel epochs) --
+              throughput with the inputs resident in HBM;
+  e2e         R / (first arrival -> last result on the host), through the
+              C ABI with host buffers (uploads and downloads included);
+  latency     p50 / p99 from arrival to result on the host;
+  plain_fp64  the same sample through the serial FP64 server (graph-captured
+              single-system PCG, one request at a time);
+  roofline    achieved algorithmic GB/s of the persistent kernel (bytes per
+              request from its iteration counts) vs the measured HBM peak;
+  spmv_fp64   the FP64 CRS SpMV on the 2048^2 cotangent Laplacian (4.2M
+              rows, 29.3M nonzeros) vs the measured HBM peak;
+  cpu_baseline  the CPU oracle (C, OpenMP, FP64 Jacobi-PCG on host cores)
+              on a bounded prefix of the same sample.
+`--impl reference` runs only the CPU reference arm (the oracle port: the
+reference's own OpenNL source is not in the checkout) and prints its line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+os.environ.setdefault("NLGB_QUIET", "1")
+
+import numpy as np  # noqa: E402
+
+METRIC = "solves/s & p99 latency at rel-residual 1e-10: batched mixed vs plain FP64 GPU"
+HBM_FALLBACK_GBS = 6800.0
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--requests", type=int, default=12)
+    p.add_argument("--seed", type=int, default=20261203)
+    p.add_argument("--rate", type=float, default=1000.0)
+    p.add_argument("--eps", type=float, default=1e-10)
+    p.add_argument("--budget-gb", type=float, default=150.0)
+    p.add_argument("--cpu-seconds", type=float, default=20.0)
+    p.add_argument("--no-plain", action="store_true")
+    p.add_argument("--no-spmv", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def measured_peak():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            d = json.loads(f.read_text())
+            return float(d["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (of measured)"
+        except Exception:
+            pass
+    return HBM_FALLBACK_GBS, "fallback 6.8 TB/s (of fallback)"
+
+
+def build_sample(R, seed, rate):
+    from graphitethree_gb300 import systems
+    reqs = systems.request_stream(R, seed, rate, 1_000, 1_000_000)
+    objs = []
+    for r in reqs:
+        if r.kind == "lscm":
+            objs.append(("rows", systems.lscm_system(r.nx, r.ny, r.seed)))
+        else:
+            objs.append(("square", systems.fairing_system(r.nx, r.ny, r.seed, lam=1e-2, n_rhs=3)))
+    return reqs, objs
+
+
+def io_bytes(objs):
+    h2d = d2h = 0
+    for kind, o in objs:
+        if kind == "rows":
+            h2d += o.row_ptr.nbytes + o.var.nbytes + o.val.nbytes + o.rhs.nbytes + o.values.nbytes
+            d2h += int((o.locked == 0).sum()) * 8 * o.n_systems
+        else:
+            h2d += o.rp.nbytes + o.ci.nbytes + o.va.nbytes + o.rhs.nbytes
+            d2h += o.rhs.nbytes
+    return int(h2d), int(d2h)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                         text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm, mx, reasons = [], 0.0, set()
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                                "sw_power_cap"], f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def serve(objs, reqs, precision, mode, eps, budget, rate_scale=1.0):
+    """Submit the sample with its Poisson arrival offsets and drain."""
+    from graphitethree_gb300 import solver
+    srv = solver.Server(budget_bytes=budget, precision=precision, mode=mode, eps=eps)
+    srv.reset_clock()
+    tickets = []
+    for r, (kind, o) in zip(reqs, objs):
+        arr = r.arrival * rate_scale
+        tickets.append(srv.submit_rows(o, arr) if kind == "rows" else srv.submit_square(o, arr))
+    results = []
+    for t in tickets:
+        x, infos, lat = srv.wait(t)
+        results.append((infos, lat))
+    st = srv.stats()
+    srv.close()
+    return st, results
+
+
+def spmv_roofline(peak):
+    import ctypes
+    from graphitethree_gb300 import _lib, solver, systems
+    fs = systems.fairing_system(2048, 2048, seed=2)
+    A = solver.Matrix(fs.rp, fs.ci, fs.va)
+    L = _lib.load()
+    import torch
+    x = torch.randn(A.n, dtype=torch.float64, device="cuda")
+    y = torch.empty_like(x)
+    ms = ctypes.c_double()
+    L.nlgb_spmv_timed(A.handle, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr()), 10, ctypes.byref(ms))
+    L.nlgb_spmv_timed(A.handle, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr()), 100, ctypes.byref(ms))
+    algo = 12 * A.nnz + 20 * A.n + 4
+    gbs = algo / (ms.value * 1e-3) / 1e9
+    out = {"kernel": "k_spmv<1,double,double>", "matrix": "cotangent Laplacian + 1e-2 I, 2048^2 grid",
+           "rows": A.n, "nnz": A.nnz, "threads_per_row": A.threads_per_row, "tile_rows": A.tile_rows,
+           "algo_bytes_per_launch": algo, "us_per_launch": ms.value * 1e3, "achieved": gbs,
+           "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+           "note": "x (33.5 MB) is gathered through L2; matrix (352 MB) > L2 (129 MB)"}
+    A.close()
+    return out
+
+
+def cpu_arm(objs, reqs, budget_s, eps):
+    """Oracle FP64 Jacobi-PCG (C, OpenMP on all host cores) on a bounded
+    prefix of the sample, in arrival order."""
+    from oracle import oracle
+    threads = oracle.max_threads()
+    t_total = 0.0
+    done = 0
+    sizes = []
+    for (kind, o) in objs:
+        t0 = time.perf_counter()
+        rp, ci, va, rhs = oracle.assemble_rowstream(o if kind == "rows" else o.to_rows())
+        for s in range(rhs.shape[0]):
+            oracle.pcg(rp, ci, va, rhs[s], eps=eps, nthreads=threads)
+        t_total += time.perf_counter() - t0
+        done += 1
+        sizes.append(int(rp.shape[0] - 1))
+        if t_total >= budget_s:
+            break
+    return {"value": done / t_total if t_total > 0 else 0.0, "unit": "solves/s", "cores": threads,
+            "kind": "port",
+            "sample": f"first {done} of the {len(objs)} sampled requests (unknowns {sizes}), "
+                      f"CPU assembly + FP64 Jacobi-PCG to 1e-10, {t_total:.1f} s"}
+
+
+def run_reference(args):
+    reqs, objs = build_sample(args.requests, args.seed, args.rate)
+    # bounded: each step solves a prefix of the sample within ~cpu_seconds / steps
+    vals = []
+    per_step = max(2.0, args.cpu_seconds / max(1, args.steps + args.warmup))
+    res = None
+    for i in range(args.warmup + args.steps):
+        r = cpu_arm(objs, reqs, per_step, args.eps)
+        if i >= args.warmup:
+            vals.append(r["value"])
+            res = r
+    v = float(statistics.median(vals)) if vals else 0.0
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded serving-stream sample)",
+            "config": config(args),
+            "cpu_baseline": {**res, "value": v},
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def config(args):
+    return {"workload": f"serving-stream sample: {args.requests} requests, LSCM / cotangent fairing "
+                        f"(3 RHS) 50/50, vertices log-uniform [1e3,1e6], Poisson arrivals "
+                        f"{args.rate:g}/s, seed {args.seed}",
+            "requests": args.requests, "rate_per_s": args.rate, "rel_residual": args.eps,
+            "hbm_budget_gb": args.budget_gb, "precision": "mixed FP32/FP64 with FP64 fallback",
+            "l2": "inputs larger than L2 for the large requests; every step re-uploads and "
+                  "re-assembles (no cached data)"}
+
+
+def main():
+    args = parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+    from graphitethree_gb300 import _lib, solver
+    if not solver.device_available():
+        raise SystemExit("bench.py: no CUDA device")
+    if world > 1:
+        # replicas only: each rank serves its own copy of the stream on its GPU
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    L = _lib.load()
+    peak, peak_src = measured_peak()
+    budget = args.budget_gb * 1e9
+    reqs, objs = build_sample(args.requests, args.seed + 7919 * rank, args.rate)
+    h2d, d2h = io_bytes(objs)
+    R = len(objs)
+
+    for _ in range(args.warmup):
+        serve(objs, reqs, "mixed", "batched", args.eps, budget)
+    clocks = ClockSampler()
+    clocks.start()
+    launches0 = L.nlgb_kernel_launches()
+    steps = []
+    t_wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        st, results = serve(objs, reqs, "mixed", "batched", args.eps, budget)
+        steps.append((st, results))
+    t_wall = time.perf_counter() - t_wall0
+    launches = L.nlgb_kernel_launches() - launches0
+    clk = clocks.stop()
+
+    kern = [s["kernel_s"] for s, _ in steps]
+    walls = [s["wall_s"] for s, _ in steps]
+    value = R / statistics.median(kern)
+    e2e = R / statistics.median(walls)
+    lat = [l for _, res in steps for _, l in res]
+    p50 = float(np.percentile(lat, 50))
+    p99 = float(np.percentile(lat, 99))
+    st_last, res_last = steps[-1]
+    achieved = st_last["algo_bytes"] / st_last["kernel_s"] / 1e9 if st_last["kernel_s"] > 0 else 0.0
+    statuses = [i.status for infos, _ in res_last for i in infos]
+    true_res = [i.true_rel_residual for infos, _ in res_last for i in infos]
+
+    plain = None
+    if not args.no_plain:
+        stp, resp = serve(objs, reqs, "double", "serial", args.eps, budget)
+        latp = [l for _, l in resp]
+        plain = {"solves_per_s_e2e": R / stp["wall_s"], "solves_per_s_device": R / stp["kernel_s"],
+                 "p50_latency_s": float(np.percentile(latp, 50)),
+                 "p99_latency_s": float(np.percentile(latp, 99)),
+                 "achieved_GBs": stp["algo_bytes"] / stp["kernel_s"] / 1e9,
+                 "speedup_e2e_batched_mixed_over_plain": e2e / (R / stp["wall_s"]),
+                 "speedup_device": value / (R / stp["kernel_s"])}
+    spmv = None if args.no_spmv else spmv_roofline(peak)
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        cpu = cpu_arm(objs, reqs, args.cpu_seconds, args.eps)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_wall / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64",
+        "data": "synthetic (seeded serving-stream sample; no public dataset)",
+        "config": config(args),
+        "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "latency": {"p50_s": p50, "p99_s": p99, "unit": "s"},
+        "plain_fp64": plain,
+        "roofline": {"bound": "hbm", "kernel": "k_batch (persistent batched PCG)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_source": peak_src,
+                     "algo_bytes_per_step": st_last["algo_bytes"],
+                     "kernel_s_per_step": st_last["kernel_s"], "epochs_per_step": st_last["epochs"]},
+        "spmv_fp64": spmv,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "gpu_launches": int(launches),
+        "parity": {"all_converged": all(s == "converged" for s in statuses),
+                   "max_true_rel_residual": max(true_res) if true_res else None,
+                   "iterations_per_step": st_last["iterations"]},
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -57,7 +57,22 @@ class NlgbParams(C.Structure):
 class NlgbResult(C.Structure):
     _fields_ = [("status", C.c_int), ("iterations", C.c_longlong), ("refinement_steps", C.c_int),
                 ("rel_residual", C.c_double), ("true_rel_residual", C.c_double),
-                ("seconds", C.c_double)]
+                ("seconds", C.c_double), ("algo_bytes", C.c_double)]
+
+
+class NlgbServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("mode", C.c_int), ("precision", C.c_int),
+                ("eps", C.c_double), ("max_iter", C.c_longlong), ("inner_eps", C.c_double),
+                ("epoch_iters", C.c_longlong), ("max_systems", C.c_int)]
+
+
+class NlgbServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("completed", C.c_longlong), ("failed", C.c_longlong),
+                ("rejected", C.c_longlong), ("p50_latency_s", C.c_double),
+                ("p99_latency_s", C.c_double), ("mean_latency_s", C.c_double),
+                ("max_latency_s", C.c_double), ("solves_per_s", C.c_double), ("wall_s", C.c_double),
+                ("kernel_s", C.c_double), ("epochs", C.c_longlong), ("iterations", C.c_longlong),
+                ("algo_bytes", C.c_double), ("peak_bytes", C.c_size_t), ("budget_bytes", C.c_size_t)]
 
 
 _SIGS = {
@@ -111,6 +126,7 @@ _SIGS = {
                                           C.c_double, C.c_uint, C.c_uint]),
     # nl_gb300.h
     "nlgb_device_available": (C.c_int, []),
+    "nlgb_kernel_launches": (C.c_longlong, []),
     "nlgb_last_error": (C.c_char_p, []),
     "nlgb_default_params": (None, [C.POINTER(NlgbParams)]),
     "nlgb_matrix_create": (C.c_void_p, [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -130,6 +146,20 @@ _SIGS = {
                                    C.POINTER(NlgbResult), f64p]),
     "nlgb_assemble": (C.c_int, [C.c_int, C.c_longlong, i64p, i32p, f64p, f64p, f64p, C.c_int,
                                 C.c_int, f64p, C.c_int, C.POINTER(C.c_void_p), f64p, f64p]),
+    "nlgb_server_default_config": (None, [C.POINTER(NlgbServerConfig)]),
+    "nlgb_server_create": (C.c_void_p, [C.POINTER(NlgbServerConfig)]),
+    "nlgb_server_reset_clock": (None, [C.c_void_p]),
+    "nlgb_server_now": (C.c_double, [C.c_void_p]),
+    "nlgb_server_submit_crs": (C.c_longlong, [C.c_void_p, C.c_int, i32p, i32p, f64p, C.c_int, f64p,
+                                              f64p, f64p, C.c_double]),
+    "nlgb_server_submit_rows": (C.c_longlong, [C.c_void_p, C.c_int, C.c_longlong, i64p, i32p, f64p,
+                                               f64p, f64p, C.c_int, C.c_int, f64p, C.c_int, f64p,
+                                               f64p, C.c_double]),
+    "nlgb_server_wait": (C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(NlgbResult), f64p]),
+    "nlgb_server_drain": (C.c_int, [C.c_void_p]),
+    "nlgb_server_get_stats": (C.c_int, [C.c_void_p, C.POINTER(NlgbServerStats)]),
+    "nlgb_server_abort": (None, [C.c_void_p]),
+    "nlgb_server_destroy": (None, [C.c_void_p]),
     "nlgb_add_rows": (C.c_int, [C.c_longlong, i64p, i32p, f64p, f64p, f64p]),
     "nlgb_set_variables": (C.c_int, [f64p, u8p]),
     "nlgb_get_variables": (C.c_int, [f64p]),

@@ -17,6 +17,7 @@
 #include "nlgb_internal.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -34,6 +35,10 @@ static thread_local NLenum g_error_code = NL_NO_ERROR;
 
 void set_error(const std::string& msg) { g_error = msg; }
 const char* last_error() { return g_error.c_str(); }
+
+static std::atomic<long long> g_launches{0};
+void count_launches(long long k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 static bool quiet() {
   static int q = -1;

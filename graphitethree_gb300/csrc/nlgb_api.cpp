@@ -81,6 +81,7 @@ cudaError_t matrix_stream(nlgb_matrix M) {
 extern "C" {
 
 int nlgb_device_available(void) { return ensure_ready() ? 1 : 0; }
+long long nlgb_kernel_launches(void) { return launch_count(); }
 const char* nlgb_last_error(void) { return last_error(); }
 
 void nlgb_default_params(nlgb_params* p) {
@@ -266,6 +267,7 @@ int nlgb_solve(nlgb_matrix A, const double* b, double* x, const nlgb_params* prm
     res->rel_residual = r.rel_residual;
     res->true_rel_residual = r.true_rel_residual;
     res->seconds = r.seconds;
+    res->algo_bytes = r.algo_bytes;
   }
   return NLGB_OK;
 }
@@ -326,6 +328,7 @@ int nlgb_batch_solve(int n_sys, const nlgb_matrix* A, const double* const* b, do
         res[i].rel_residual = h.bnorm2 > 0 ? std::sqrt(h.rr / h.bnorm2) : 0.0;
         res[i].true_rel_residual = h.bnorm2 > 0 ? std::sqrt(h.rr_true / h.bnorm2) : 0.0;
         res[i].seconds = st.ms * 1e-3;
+        res[i].algo_bytes = algo_bytes(A[i]->A.n, A[i]->A.nnz, h);
       }
     }
     for (auto& sl : slots) sl.release(s);

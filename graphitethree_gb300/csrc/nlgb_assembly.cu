@@ -335,13 +335,17 @@ cudaError_t exclusive_scan(const In* in, long long n, long long* out, long long*
   long long* offs = nullptr;
   NLGB_CUDA_TRY(cudaMallocAsync(&sums, (size_t)tiles * sizeof(long long), s));
   NLGB_CUDA_TRY(cudaMallocAsync(&offs, (size_t)(tiles + 1) * sizeof(long long), s));
-  if (n > 0) k_scan_tiles<In><<<(unsigned)tiles, kAsmCTA, 0, s>>>(in, n, out, sums);
+  if (n > 0) {
+    k_scan_tiles<In><<<(unsigned)tiles, kAsmCTA, 0, s>>>(in, n, out, sums);
+    count_launches(1);
+  }
   NLGB_CUDA_TRY(cudaGetLastError());
   long long tot = 0;
   if (tiles > 1) {
     long long t2 = 0;
     NLGB_CUDA_TRY(exclusive_scan<long long>(sums, tiles, offs, &t2, s));
     k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(out, n, offs);
+    count_launches(1);
     NLGB_CUDA_TRY(cudaGetLastError());
     tot = t2;
   } else {
@@ -393,15 +397,19 @@ cudaError_t assemble_normal_equations(const LSRowsDevice& R, DeviceCRS& out, dou
   NLGB_CUDA_TRY(cudaMemsetAsync(cursor.p, 0, sizeof(int) * (nf + 1), s));
   if (R.n_rows > 0) {
     k_rows_prepare<<<blocks_for(R.n_rows), 256, 0, s>>>(R, sbuf.p, nfree.p);
+    count_launches(1);
     k_col_count<<<blocks_for(R.n_rows), 256, 0, s>>>(R, colcnt.p);
+    count_launches(1);
   }
   NLGB_CUDA_TRY(cudaGetLastError());
   long long n_free_coefs = 0;
   NLGB_CUDA_TRY(exclusive_scan<int>(colcnt.p, nf + 1, colptr.p, &n_free_coefs, s));
   NLGB_CUDA_TRY(colrow.alloc(n_free_coefs, s));
   NLGB_CUDA_TRY(colwa.alloc(n_free_coefs, s));
-  if (R.n_rows > 0)
+  if (R.n_rows > 0) {
     k_col_scatter<<<blocks_for(R.n_rows), 256, 0, s>>>(R, colptr.p, cursor.p, colrow.p, colwa.p);
+    count_launches(1);
+  }
   NLGB_CUDA_TRY(cand.alloc(nf + 1, s));
   NLGB_CUDA_TRY(row_nnz.alloc(nf + 1, s));
   NLGB_CUDA_TRY(big.alloc(nf + 1, s));
@@ -412,7 +420,9 @@ cudaError_t assemble_normal_equations(const LSRowsDevice& R, DeviceCRS& out, dou
   NLGB_CUDA_TRY(cudaMemsetAsync(row_nnz.p, 0, sizeof(int) * (nf + 1), s));
   if (nf > 0) {
     k_cand_count<<<blocks_for(nf), 256, 0, s>>>(nf, colptr.p, colrow.p, nfree.p, cand.p);
+    count_launches(1);
     k_collect_big<<<blocks_for(nf), 256, 0, s>>>(nf, cand.p, kWarpCap, big.p, big_n.p);
+    count_launches(1);
   }
   NLGB_CUDA_TRY(cudaGetLastError());
   int n_big = 0;
@@ -431,12 +441,15 @@ cudaError_t assemble_normal_equations(const LSRowsDevice& R, DeviceCRS& out, dou
   auto run_merge = [&](int numeric) -> cudaError_t {
     M.numeric = numeric;
     M.rows = nullptr; M.n_rows_list = 0;
-    if (nf > 0)
+    if (nf > 0) {
       k_merge<32, kWarpCap><<<blocks_for(nf, kWarpGroups), kAsmCTA, smem_warp, s>>>(M);
+      count_launches(1);
+    }
     NLGB_CUDA_TRY(cudaGetLastError());
     if (n_big > 0) {
       M.rows = big.p; M.n_rows_list = n_big;
       k_merge<kAsmCTA, kBlockCap><<<(unsigned)n_big, kAsmCTA, smem_block, s>>>(M);
+      count_launches(1);
       NLGB_CUDA_TRY(cudaGetLastError());
     }
     return cudaSuccess;
@@ -462,9 +475,11 @@ cudaError_t assemble_normal_equations(const LSRowsDevice& R, DeviceCRS& out, dou
   NLGB_CUDA_TRY(cudaMalloc(&out.ci, sizeof(int) * std::max(1LL, nnz)));
   NLGB_CUDA_TRY(cudaMalloc(&out.va, sizeof(double) * std::max(1LL, nnz)));
   k_to_int<<<blocks_for(nf + 1), 256, 0, s>>>(rp64.p, out.rp, nf + 1);
+  count_launches(1);
   NLGB_CUDA_TRY(cudaGetLastError());
   // RHS of variables without any row stays 0.
   k_zero<<<blocks_for((long long)R.n_systems * nf), 256, 0, s>>>(rhs_out, (long long)R.n_systems * nf);
+  count_launches(1);
   M.rp = out.rp; M.ci = out.ci; M.va = out.va;
   NLGB_CUDA_TRY(run_merge(1));
   NLGB_CUDA_TRY(cudaStreamSynchronize(s));
@@ -507,7 +522,9 @@ cudaError_t assemble_square(const LSRowsDevice& R, DeviceCRS& out, double* rhs_o
   NLGB_CUDA_TRY(cudaMemsetAsync(cnt.p, 0, sizeof(int) * (n + 1), s));
   if (n > 0) {
     k_rows_prepare<<<blocks_for(n), 256, 0, s>>>(R, sbuf.p, nfree.p);
+    count_launches(1);
     k_square_count<<<blocks_for(n), 256, 0, s>>>(R, cnt.p);
+    count_launches(1);
   }
   NLGB_CUDA_TRY(cudaGetLastError());
   long long nnz = 0;
@@ -522,7 +539,11 @@ cudaError_t assemble_square(const LSRowsDevice& R, DeviceCRS& out, double* rhs_o
   NLGB_CUDA_TRY(cudaMalloc(&out.ci, sizeof(int) * std::max(1LL, nnz)));
   NLGB_CUDA_TRY(cudaMalloc(&out.va, sizeof(double) * std::max(1LL, nnz)));
   k_to_int<<<blocks_for(n + 1), 256, 0, s>>>(rp64.p, out.rp, n + 1);
-  if (n > 0) k_square_fill<<<blocks_for(n), 256, 0, s>>>(R, rp64.p, out.ci, out.va, sbuf.p, rhs_out);
+  count_launches(1);
+  if (n > 0) {
+    k_square_fill<<<blocks_for(n), 256, 0, s>>>(R, rp64.p, out.ci, out.va, sbuf.p, rhs_out);
+    count_launches(1);
+  }
   NLGB_CUDA_TRY(cudaGetLastError());
   NLGB_CUDA_TRY(cudaStreamSynchronize(s));
   return cudaSuccess;

@@ -107,8 +107,8 @@ __device__ void get_sums(const SysView& s, int slot, double (&o)[K]) {
 
 // One system, run by a team (rank r of k CTAs) for at most `budget`
 // iterations.  st: the CTA's shared-memory copy of the system state.
-__device__ void run_system(const SysView& s, SysState* st, int r, int k, TeamBar* bar, int* err,
-                           long long budget) {
+__device__ void run_system_once(const SysView& s, SysState* st, int r, int k, TeamBar* bar, int* err,
+                                long long budget) {
   const bool mixed = st->precision == 1;
   long long done_iters = 0;
   if (st->stage == 0) {
@@ -214,7 +214,14 @@ __device__ void run_system(const SysView& s, SysState* st, int r, int k, TeamBar
         if (!team_sync(bar, k, err)) break;
         double o[4];
         get_sums<4>(s, kSlotInit, o);
-        NLGB_SCALAR(scalar_after_outer(st, o[0], o[1], o[2], o[3]));
+        NLGB_SCALAR(scalar_after_outer(st, o[0], o[1], o[2], o[3]);
+                    // FP32 cannot track this system: continue it in FP64
+                    // from the current x (same rule as the graph solver).
+                    if (st->status == ST_STAGNATION && !st->fell_back) {
+                      st->status = ST_RUNNING; st->precision = 0; st->fell_back = 1;
+                      st->stage = 0; st->mode = 0; st->iter_at_fallback = st->iter;
+                    });
+        if (st->stage == 0) break;
         if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
       }
     }
@@ -239,6 +246,15 @@ __device__ void run_system(const SysView& s, SysState* st, int r, int k, TeamBar
     get_sums<1>(s, kSlotFinal, o);
     NLGB_SCALAR(st->rr_true = o[0]; st->stage = 3);
   }
+}
+
+// One system; a mixed system that falls back to FP64 restarts here at stage
+// 0 with precision 0 (its FP32 iterations stay counted).
+__device__ void run_system(const SysView& s, SysState* st, int r, int k, TeamBar* bar, int* err,
+                           long long budget) {
+  run_system_once(s, st, r, k, bar, err, budget);
+  if (st->stage == 0 && st->fell_back && st->precision == 0)
+    run_system_once(s, st, r, k, bar, err, budget);
 }
 
 __global__ void __launch_bounds__(kCTA) k_batch(BatchArgs a) {
@@ -284,6 +300,11 @@ __global__ void __launch_bounds__(kCTA) k_batch(BatchArgs a) {
   }
 }
 
+__global__ void k_gather_states(const SysView* views, int n, SysState* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = *views[i].st;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -293,6 +314,7 @@ BatchRunner::~BatchRunner() {
   cudaFree(d_views_); cudaFree(d_teams_); cudaFree(d_cta_team_); cudaFree(d_team_sys_);
   cudaFree(d_queue_); cudaFree(d_bars_); cudaFree(d_ctl_);
   if (h_err_) cudaFreeHost(h_err_);
+  cudaFree(d_states_);
   if (ev0_) cudaEventDestroy(ev0_);
   if (ev1_) cudaEventDestroy(ev1_);
 }
@@ -456,6 +478,17 @@ cudaError_t BatchRunner::finish(BatchLaunchStats* stats) {
   return cudaSuccess;
 }
 
+cudaError_t BatchRunner::gather_states(SysState* out, int n) {
+  if (n <= 0) return cudaSuccess;
+  NLGB_CUDA_TRY(ensure(d_states_, cap_states_, (size_t)n));
+  k_gather_states<<<(n + 127) / 128, 128, 0, stream_>>>(d_views_, n, d_states_);
+  count_launches(1);
+  NLGB_CUDA_TRY(cudaGetLastError());
+  NLGB_CUDA_TRY(cudaMemcpyAsync(out, d_states_, sizeof(SysState) * n, cudaMemcpyDeviceToHost, stream_));
+  NLGB_CUDA_TRY(cudaStreamSynchronize(stream_));
+  return cudaSuccess;
+}
+
 // ---------------------------------------------------------------------------
 // Per-system device slot.
 // ---------------------------------------------------------------------------
@@ -467,7 +500,8 @@ size_t SystemSlot::bytes_for(int n, int tile_rows, bool mixed) {
   const int n_tiles = std::max(1, (n + tile_rows - 1) / tile_rows);
   const size_t parts = align256((size_t)n_tiles * kParts * sizeof(double));
   const size_t st = align256(sizeof(SysState));
-  return mixed ? (2 * n8 + 4 * n4 + parts + st) : (5 * n8 + parts + st);
+  // mixed systems also carry the FP64 r, p, q of a possible FP64 fallback
+  return mixed ? (5 * n8 + 4 * n4 + parts + st) : (5 * n8 + parts + st);
 }
 
 cudaError_t SystemSlot::alloc(DeviceCRS* Am, bool mx, cudaStream_t s) {
@@ -488,15 +522,14 @@ cudaError_t SystemSlot::alloc(DeviceCRS* Am, bool mx, cudaStream_t s) {
   view.dinv = A->dinv; view.dinv32 = A->dinv32;
   view.b = reinterpret_cast<double*>(p); p += n8;
   view.x = reinterpret_cast<double*>(p); p += n8;
+  view.r = reinterpret_cast<double*>(p); p += n8;
+  view.p = reinterpret_cast<double*>(p); p += n8;
+  view.q = reinterpret_cast<double*>(p); p += n8;
   if (mixed) {
     view.r32 = reinterpret_cast<float*>(p); p += n4;
     view.p32 = reinterpret_cast<float*>(p); p += n4;
     view.q32 = reinterpret_cast<float*>(p); p += n4;
     view.c32 = reinterpret_cast<float*>(p); p += n4;
-  } else {
-    view.r = reinterpret_cast<double*>(p); p += n8;
-    view.p = reinterpret_cast<double*>(p); p += n8;
-    view.q = reinterpret_cast<double*>(p); p += n8;
   }
   view.part = reinterpret_cast<double*>(p);
   p += align256((size_t)view.n_tiles * kParts * sizeof(double));

@@ -87,6 +87,9 @@ class BatchRunner {
   cudaError_t launch(const std::vector<SysView>& views, const std::vector<long long>& work,
                      long long budget);
   cudaError_t finish(BatchLaunchStats* stats);
+  // Copy the SysState of every system of the last launch into `out`
+  // (host, pinned or pageable; views.size() entries), one transfer.
+  cudaError_t gather_states(SysState* out, int n);
   int max_grid() const { return grid_; }
 
  private:
@@ -105,6 +108,8 @@ class BatchRunner {
          cap_bars_ = 0;
   cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
   int* h_err_ = nullptr;           // pinned
+  SysState* d_states_ = nullptr;
+  size_t cap_states_ = 0;
   int last_grid_ = 0, last_workers_ = 0;
   bool pending_ = false;
 };

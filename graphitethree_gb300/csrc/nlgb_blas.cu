@@ -61,7 +61,9 @@ cudaError_t dev_dot(const double* x, const double* y, long long n, double* out_h
   double* part = nullptr;
   NLGB_CUDA_TRY(cudaMallocAsync(&part, sizeof(double) * (nb + 1), s));
   k_dot_part<<<nb, kT, 0, s>>>(x, y, n, part);
+  count_launches(1);
   k_sum_parts<<<1, kT, 0, s>>>(part, nb, part + nb);
+  count_launches(1);
   NLGB_CUDA_TRY(cudaGetLastError());
   NLGB_CUDA_TRY(cudaMemcpyAsync(out_host, part + nb, sizeof(double), cudaMemcpyDeviceToHost, s));
   NLGB_CUDA_TRY(cudaFreeAsync(part, s));
@@ -70,15 +72,24 @@ cudaError_t dev_dot(const double* x, const double* y, long long n, double* out_h
 }
 
 cudaError_t dev_axpy(long long n, double a, const double* x, double* y, cudaStream_t s) {
-  if (n > 0) k_axpy<<<blocks(n), kT, 0, s>>>(n, a, x, y);
+  if (n > 0) {
+    k_axpy<<<blocks(n), kT, 0, s>>>(n, a, x, y);
+    count_launches(1);
+  }
   return cudaGetLastError();
 }
 cudaError_t dev_scal(long long n, double a, double* x, cudaStream_t s) {
-  if (n > 0) k_scal<<<blocks(n), kT, 0, s>>>(n, a, x);
+  if (n > 0) {
+    k_scal<<<blocks(n), kT, 0, s>>>(n, a, x);
+    count_launches(1);
+  }
   return cudaGetLastError();
 }
 cudaError_t dev_mul(long long n, const double* x, double* y, cudaStream_t s) {
-  if (n > 0) k_mul<<<blocks(n), kT, 0, s>>>(n, x, y);
+  if (n > 0) {
+    k_mul<<<blocks(n), kT, 0, s>>>(n, x, y);
+    count_launches(1);
+  }
   return cudaGetLastError();
 }
 

@@ -64,7 +64,27 @@ struct __align__(16) SysState {
   unsigned int cnt[4];         // last-CTA counters of the phase kernels
   int stage;                   // batched: 0 start, 1 iterating, 2 final residual due, 3 done
   int precision;               // batched: 0 FP64, 1 mixed
+  int fell_back;               // mixed system continued in FP64 (FP32 could not track it)
+  int pad_;
+  long long iter_at_fallback;  // FP32 iterations done before the FP64 fallback
 };
+
+// Algorithmic HBM bytes of one solve (n rows, z nonzeros), from its final
+// state: per FP64 PCG iteration 12z + 108n (CRS values + int32 columns, row
+// pointers, x gather, q; x/p/r/q/D^-1 vector passes); per FP32 iteration
+// 8z + 56n; per FP64 reliable update 12z + 52n; plus the initial residual
+// (12z + 36n) and the final true residual (12z + 16n).
+inline __host__ __device__ double algo_bytes(long long n, long long z, const SysState& h) {
+  const bool mixed_used = h.outer > 0;
+  const double it32 = mixed_used ? double(h.fell_back ? h.iter_at_fallback : h.iter) : 0.0;
+  const double it64 = double(h.iter) - it32;
+  const double N = double(n), Z = double(z);
+  double b = (12.0 * Z + 36.0 * N) + (12.0 * Z + 16.0 * N);
+  b += it64 * (12.0 * Z + 108.0 * N) + it32 * (8.0 * Z + 56.0 * N);
+  b += double(h.outer) * (12.0 * Z + 52.0 * N);
+  if (h.fell_back) b += 12.0 * Z + 36.0 * N;   // FP64 restart residual
+  return b;
+}
 
 // Everything a tile procedure needs about one system.
 struct SysView {
@@ -168,6 +188,47 @@ __device__ __forceinline__ A row_dot(const int* __restrict__ rp, const int* __re
   return subwarp_sum<T, A>(sum);
 }
 
+// Rows [lo, hi) of a tile with T threads per row, two passes at a time so
+// every sub-warp keeps two independent gather chains in flight (the
+// persistent kernel and mid-size systems are latency-bound).  epi(row, sum)
+// is called by the row's lane 0 in the same order as a one-pass-at-a-time
+// loop, so per-thread accumulations in epi are unchanged.
+template <int T, typename VT, typename XT, typename A, bool kCoh, typename Epi>
+__device__ __forceinline__ void tile_rows_dot(const int* __restrict__ rp, const int* __restrict__ ci,
+                                              const VT* __restrict__ va, const XT* __restrict__ x,
+                                              int lo, int hi, Epi&& epi) {
+  const int sub = threadIdx.x / T, lane = threadIdx.x % T;
+  constexpr int RPP = kCTA / T;
+  for (int base = lo; base < hi; base += 2 * RPP) {
+    const int ra = base + sub, rb = ra + RPP;
+    const bool oka = ra < hi, okb = rb < hi;
+    A sa = A(0), sb = A(0);
+    int ka = 0, ea = 0, kb = 0, eb = 0;
+    if (oka) { ka = __ldg(rp + ra) + lane; ea = __ldg(rp + ra + 1); }
+    if (okb) { kb = __ldg(rp + rb) + lane; eb = __ldg(rp + rb + 1); }
+    while (ka < ea || kb < eb) {
+      if (ka < ea) {
+        const int c = __ldg(ci + ka);
+        const XT xc = kCoh ? __ldcg(x + c) : __ldg(x + c);
+        sa = fma(A(__ldg(va + ka)), A(xc), sa);
+        ka += T;
+      }
+      if (kb < eb) {
+        const int c = __ldg(ci + kb);
+        const XT xc = kCoh ? __ldcg(x + c) : __ldg(x + c);
+        sb = fma(A(__ldg(va + kb)), A(xc), sb);
+        kb += T;
+      }
+    }
+    sa = subwarp_sum<T, A>(sa);
+    sb = subwarp_sum<T, A>(sb);
+    if (lane == 0) {
+      if (oka) epi(ra, sa);
+      if (okb) epi(rb, sb);
+    }
+  }
+}
+
 __device__ __forceinline__ int tile_lo(const SysView& s, int tile) { return tile * s.tile_rows; }
 __device__ __forceinline__ int tile_hi(const SysView& s, int tile) {
   const int h = (tile + 1) * s.tile_rows;
@@ -182,18 +243,12 @@ __device__ __forceinline__ int tile_hi(const SysView& s, int tile) {
 template <int T, bool kCoh = false>
 __device__ double tile_spmv_pq(const SysView& s, int tile) {
   const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
-  const int sub = threadIdx.x / T, lane = threadIdx.x % T;
-  constexpr int RPP = kCTA / T;  // rows per pass
   double acc[1] = {0.0};
-  for (int base = lo; base < hi; base += RPP) {
-    const int row = base + sub;
-    const bool valid = row < hi;
-    const double qv = row_dot<T, double, double, double, kCoh>(s.rp, s.ci, s.va, s.p, row, valid, lane);
-    if (valid && lane == 0) {
+  tile_rows_dot<T, double, double, double, kCoh>(s.rp, s.ci, s.va, s.p, lo, hi,
+    [&](int row, double qv) {
       s.q[row] = qv;
       acc[0] = fma(__ldcg(s.p + row), qv, acc[0]);
-    }
-  }
+    });
   block_sum<1>(acc);
   return acc[0];
 }
@@ -202,14 +257,9 @@ __device__ double tile_spmv_pq(const SysView& s, int tile) {
 template <int T, bool kCoh = false>
 __device__ void tile_residual(const SysView& s, int tile, double (&out)[3]) {
   const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
-  const int sub = threadIdx.x / T, lane = threadIdx.x % T;
-  constexpr int RPP = kCTA / T;
   out[0] = out[1] = out[2] = 0.0;
-  for (int base = lo; base < hi; base += RPP) {
-    const int row = base + sub;
-    const bool valid = row < hi;
-    const double ax = row_dot<T, double, double, double, kCoh>(s.rp, s.ci, s.va, s.x, row, valid, lane);
-    if (valid && lane == 0) {
+  tile_rows_dot<T, double, double, double, kCoh>(s.rp, s.ci, s.va, s.x, lo, hi,
+    [&](int row, double ax) {
       const double bi = s.b[row];
       const double ri = bi - ax;
       const double zi = s.dinv[row] * ri;
@@ -218,8 +268,7 @@ __device__ void tile_residual(const SysView& s, int tile, double (&out)[3]) {
       out[0] = fma(bi, bi, out[0]);
       out[1] = fma(zi, ri, out[1]);
       out[2] = fma(ri, ri, out[2]);
-    }
-  }
+    });
   block_sum<3>(out);
 }
 
@@ -293,18 +342,12 @@ __device__ __forceinline__ void tile_zero_x(const SysView& s, int tile) {
 template <int T, bool kCoh = false>
 __device__ double tile_true_rr(const SysView& s, int tile) {
   const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
-  const int sub = threadIdx.x / T, lane = threadIdx.x % T;
-  constexpr int RPP = kCTA / T;
   double acc[1] = {0.0};
-  for (int base = lo; base < hi; base += RPP) {
-    const int row = base + sub;
-    const bool valid = row < hi;
-    const double ax = row_dot<T, double, double, double, kCoh>(s.rp, s.ci, s.va, s.x, row, valid, lane);
-    if (valid && lane == 0) {
+  tile_rows_dot<T, double, double, double, kCoh>(s.rp, s.ci, s.va, s.x, lo, hi,
+    [&](int row, double ax) {
       const double ri = s.b[row] - ax;
       acc[0] = fma(ri, ri, acc[0]);
-    }
-  }
+    });
   block_sum<1>(acc);
   return acc[0];
 }
@@ -341,14 +384,9 @@ __device__ __forceinline__ void tile_mx_apply(const SysView& s, int tile) {
 template <int T, bool kCoh = false>
 __device__ void tile_mx_outer(const SysView& s, int tile, double (&out)[4]) {
   const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
-  const int sub = threadIdx.x / T, lane = threadIdx.x % T;
-  constexpr int RPP = kCTA / T;
   out[0] = out[1] = out[2] = out[3] = 0.0;
-  for (int base = lo; base < hi; base += RPP) {
-    const int row = base + sub;
-    const bool valid = row < hi;
-    const double ax = row_dot<T, double, double, double, kCoh>(s.rp, s.ci, s.va, s.x, row, valid, lane);
-    if (valid && lane == 0) {
+  tile_rows_dot<T, double, double, double, kCoh>(s.rp, s.ci, s.va, s.x, lo, hi,
+    [&](int row, double ax) {
       const double bi = s.b[row];
       const double ri = bi - ax;
       const float r32 = float(ri);
@@ -358,8 +396,7 @@ __device__ void tile_mx_outer(const SysView& s, int tile, double (&out)[4]) {
       out[1] = fma(ri, ri, out[1]);
       out[2] = fma(double(z32), double(r32), out[2]);
       out[3] = fma(double(r32), double(r32), out[3]);
-    }
-  }
+    });
   block_sum<4>(out);
 }
 
@@ -367,18 +404,12 @@ __device__ void tile_mx_outer(const SysView& s, int tile, double (&out)[4]) {
 template <int T, bool kCoh = false>
 __device__ double tile_mx_spmv_pq(const SysView& s, int tile) {
   const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
-  const int sub = threadIdx.x / T, lane = threadIdx.x % T;
-  constexpr int RPP = kCTA / T;
   double acc[1] = {0.0};
-  for (int base = lo; base < hi; base += RPP) {
-    const int row = base + sub;
-    const bool valid = row < hi;
-    const float qv = row_dot<T, float, float, float, kCoh>(s.rp, s.ci, s.va32, s.p32, row, valid, lane);
-    if (valid && lane == 0) {
+  tile_rows_dot<T, float, float, float, kCoh>(s.rp, s.ci, s.va32, s.p32, lo, hi,
+    [&](int row, float qv) {
       s.q32[row] = qv;
       acc[0] = fma(double(__ldcg(s.p32 + row)), double(qv), acc[0]);
-    }
-  }
+    });
   block_sum<1>(acc);
   return acc[0];
 }
@@ -448,7 +479,7 @@ __device__ __forceinline__ void scalar_after_init(SysState* st, double bb, doubl
   st->bnorm2 = bb;
   st->rho = rz;
   st->rr = rr;
-  st->iter = 0;
+  if (!st->fell_back) st->iter = 0;   // a fallback keeps counting the FP32 iterations
   if (!(bb > 0.0)) {             // b == 0 (or NaN): x = 0 is the solution
     st->zero_rhs = (bb == 0.0);
     st->status = (bb == 0.0) ? ST_CONVERGED : ST_BREAKDOWN;
@@ -502,15 +533,18 @@ __device__ __forceinline__ void scalar_after_outer(SysState* st, double bb, doub
   if (rr64 <= st->thresh2 * bb0) { st->status = ST_CONVERGED; return; }
   if (st->iter >= st->max_iter) { st->status = ST_MAX_ITER; return; }
   if (st->outer >= st->max_outer) { st->status = ST_STAGNATION; return; }
-  // Stagnation: many updates in a row that do not improve on the best
-  // true residual seen so far.
-  if (st->outer > 0 && !(rr64 < st->rr64_prev)) {
-    st->stall += 1;
-    if (st->stall >= 8) { st->status = ST_STAGNATION; return; }
-  } else {
-    st->stall = 0;
-    st->rr64_prev = rr64;
+  // FP32 not tracking the FP64 system: an update is due after the FP32
+  // residual fell by in_thresh (0.1 by default), so a healthy update shrinks
+  // the true residual by about as much.  Two updates in a row that shrink it
+  // by less than 2x mean the FP32-rounded matrix is too far from the FP64
+  // one (kappa * u32 ~ 1, e.g. LSCM normal equations): report STAGNATION so
+  // the caller continues this system in FP64 from the current x.
+  if (st->outer > 0) {
+    if (rr64 > 0.25 * st->rr64_prev) st->stall += 1;
+    else st->stall = 0;
   }
+  st->rr64_prev = rr64;
+  if (st->stall >= 2) { st->status = ST_STAGNATION; return; }
   if (!finite_pos(rz32) || !finite_pos(rr32)) { st->status = ST_BREAKDOWN; return; }
   st->beta = (st->outer == 0) ? 0.0 : rz32 / st->rho;
   st->rho = rz32;

@@ -12,6 +12,11 @@ namespace nlgb {
 void set_error(const std::string& msg);
 const char* last_error();
 
+// Process-wide count of kernels launched by the library (host launches plus
+// the kernel nodes executed by the solver graphs).
+void count_launches(long long k);
+long long launch_count();
+
 #define NLGB_CUDA_TRY(expr)                                                     \
   do {                                                                          \
     cudaError_t e_ = (expr);                                                    \
@@ -71,6 +76,7 @@ struct SolveResult {
   double rel_residual = 0;       // recursive (plain) / true FP64 (mixed) at stop
   double true_rel_residual = 0;  // ||b - A x|| / ||b|| recomputed in FP64
   double seconds = 0;
+  double algo_bytes = 0;         // algorithmic HBM bytes of the solve
 };
 
 // Plain FP64 or mixed FP32/FP64-refined Jacobi-PCG on one resident matrix.
@@ -91,6 +97,8 @@ class PcgSolver {
 
  private:
   cudaError_t alloc(bool mixed);
+  cudaError_t run_graph(bool mixed, const SolveParams& prm, long long max_iter, long long done,
+                        int outer, float* ms);
   cudaError_t build_plain_graph();
   cudaError_t build_mixed_graph();
   void release();
@@ -107,6 +115,7 @@ class PcgSolver {
   cudaGraphExec_t plain_exec_ = nullptr, mixed_exec_ = nullptr;
   cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
   bool mixed_alloc_ = false;
+  long long graph_launches_ = 0;
 };
 
 // Least-squares normal equations assembled on the GPU (row-merge into CRS).

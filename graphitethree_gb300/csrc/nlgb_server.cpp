@@ -1,0 +1,653 @@
+// nlgb_server.cpp -- solve server with HBM-budget admission and continuous
+// batching (include/nl_gb300.h, nlgb_server_*).
+//
+// In the reference every solve is a synchronous nlSolve under Graphite's
+// global command lock (src/lib/OGF/scene_graph/commands/commands.cpp:
+// 99-117), and an atlas is parameterised chart after chart
+// (mesh_grob_surface_commands.cpp:724).  Here one host thread owns the GPU:
+//   * requests become eligible at their arrival time (server clock);
+//   * admission is first-fit against the HBM budget (device footprint of
+//     the matrix, its FP32 copy, the Jacobi diagonal and every right-hand
+//     side's Krylov state), so large requests do not block small ones;
+//   * every epoch is one launch of the persistent batched kernel over all
+//     active systems for at most epoch_iters iterations each; while it runs,
+//     newly eligible requests are uploaded (and least-squares rows
+//     assembled) on a second stream; they join the next epoch;
+//   * after each epoch the states of all systems are gathered in one copy;
+//     finished requests are copied back to the caller's buffer and their
+//     device memory is released.
+// SERIAL mode is the baseline: one request at a time, each system solved by
+// the graph-captured single-system PCG.
+#include "../../include/nl.h"
+#include "../../include/nl_gb300.h"
+#include "nlgb_batch.h"
+#include "nlgb_internal.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+using namespace nlgb;
+using Clock = std::chrono::steady_clock;
+
+namespace {
+
+enum ReqState { R_FUTURE, R_PENDING, R_ACTIVE, R_DONE, R_FAILED };
+
+struct Req {
+  long long id = 0;
+  int kind = 0;                 // 0: CRS, 1: row stream
+  int least_squares = 1;
+  int n = 0;                    // unknowns per system
+  int n_rhs = 1;
+  // inputs (host copies, released once uploaded)
+  std::vector<int> rp, ci;
+  std::vector<double> va, b, x0;
+  long long n_rows = 0;
+  std::vector<long long> row_ptr;
+  std::vector<int> col;
+  std::vector<double> val, rhs, weight, xl;
+  int n_vars = 0;
+  bool has_weight = false, has_rhs = false, has_xl = false;
+  double* x_out = nullptr;
+  double arrival = 0.0;
+  // runtime
+  ReqState state = R_FUTURE;
+  size_t bytes = 0;
+  DeviceCRS A;
+  double* d_rhs = nullptr;      // assembled right-hand sides (row streams)
+  std::vector<SystemSlot> slots;
+  std::vector<int> sys_done;
+  std::vector<nlgb_result> res;
+  double t_done = 0.0;
+  int status = NL_GB300_STATUS_NONE;
+  std::string error;
+};
+
+double percentile(std::vector<double> v, double q) {
+  if (v.empty()) return 0.0;
+  std::sort(v.begin(), v.end());
+  const double pos = q * (double)(v.size() - 1);
+  const size_t i = (size_t)pos;
+  const double f = pos - (double)i;
+  return i + 1 < v.size() ? v[i] * (1.0 - f) + v[i + 1] * f : v[i];
+}
+
+size_t estimate_bytes(const Req& r, bool mixed) {
+  const size_t slot = SystemSlot::bytes_for(r.n, 128, mixed);
+  size_t nnz = 0, upload = 0;
+  if (r.kind == 0) {
+    nnz = (size_t)r.rp[r.n];
+  } else {
+    // normal-matrix nonzeros: about half the row-merge candidates
+    double cand = 0.0;
+    for (long long i = 0; i < r.n_rows; ++i) {
+      const double k = double(r.row_ptr[i + 1] - r.row_ptr[i]);
+      cand += k * k;
+    }
+    nnz = r.least_squares ? (size_t)(0.5 * cand) : (size_t)r.row_ptr[r.n_rows];
+    upload = (size_t)r.row_ptr[r.n_rows] * 24 + (size_t)r.n_rows * (16 + 8 * r.n_rhs) +
+             (size_t)r.n_vars * 8 * r.n_rhs + (size_t)r.n * 8 * r.n_rhs;
+  }
+  const size_t mat = (size_t)(r.n + 1) * 4 + nnz * (12 + (mixed ? 4 : 0)) + (size_t)r.n * 12;
+  return mat + upload + (size_t)r.n_rhs * slot;
+}
+
+}  // namespace
+
+struct nlgb_server_s {
+  nlgb_server_config cfg;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::thread th;
+  bool stop = false;
+  bool aborting = false;
+  Clock::time_point origin = Clock::now();
+  long long next_id = 0;
+  std::map<long long, std::unique_ptr<Req>> reqs;
+  std::deque<Req*> incoming;
+  // owned by the worker thread
+  std::vector<Req*> future, pending, active;
+  size_t used = 0;
+  // statistics (guarded by mu)
+  nlgb_server_stats st{};
+  std::vector<double> latencies;
+  double first_arrival = -1.0, last_done = 0.0;
+  std::string fatal;
+
+  double now() const { return std::chrono::duration<double>(Clock::now() - origin).count(); }
+};
+
+namespace {
+
+bool mixed_of(const nlgb_server_s* S) { return S->cfg.precision == NL_GB300_PRECISION_MIXED; }
+
+SolveParams params_of(const nlgb_server_s* S) {
+  SolveParams p;
+  p.eps = S->cfg.eps;
+  p.max_iter = S->cfg.max_iter;
+  p.precision = S->cfg.precision;
+  p.inner_eps = S->cfg.inner_eps;
+  p.max_outer = 100000;
+  return p;
+}
+
+// Upload / assemble a request on stream `s` and start its systems.
+bool admit(nlgb_server_s* S, Req* r, cudaStream_t s) {
+  const bool mixed = mixed_of(S);
+  cudaError_t e = cudaSuccess;
+  if (r->kind == 0) {
+    e = crs_upload(r->A, r->n, r->n, r->rp.data(), r->ci.data(), r->va.data(), s);
+  } else {
+    long long* drp = nullptr; int* dcol = nullptr;
+    double *dval = nullptr, *drhs = nullptr, *dw = nullptr, *dxl = nullptr;
+    const long long nc = r->row_ptr[r->n_rows];
+    auto up = [&](void** dst, const void* src, size_t bytes) {
+      if (e != cudaSuccess) return;
+      e = cudaMalloc(dst, std::max<size_t>(bytes, 8));
+      if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, s);
+    };
+    up((void**)&drp, r->row_ptr.data(), sizeof(long long) * (r->n_rows + 1));
+    up((void**)&dcol, r->col.data(), sizeof(int) * nc);
+    up((void**)&dval, r->val.data(), sizeof(double) * nc);
+    if (r->has_rhs) up((void**)&drhs, r->rhs.data(), sizeof(double) * r->rhs.size());
+    if (r->has_weight) up((void**)&dw, r->weight.data(), sizeof(double) * r->weight.size());
+    if (r->has_xl) up((void**)&dxl, r->xl.data(), sizeof(double) * r->xl.size());
+    else up((void**)&dxl, nullptr, 0);
+    if (e == cudaSuccess) e = cudaMalloc(&r->d_rhs, sizeof(double) * std::max<size_t>(1, (size_t)r->n_rhs * r->n));
+    if (e == cudaSuccess) {
+      LSRowsDevice R;
+      R.n_rows = r->n_rows; R.n_coefs = nc; R.n_free = r->n; R.n_vars = r->n_vars;
+      R.n_systems = r->n_rhs; R.row_ptr = drp; R.col = dcol; R.val = dval;
+      R.rhs = r->has_rhs ? drhs : nullptr; R.weight = r->has_weight ? dw : nullptr; R.xl = dxl;
+      e = r->least_squares ? assemble_normal_equations(R, r->A, r->d_rhs, s)
+                           : assemble_square(R, r->A, r->d_rhs, s);
+    }
+    cudaStreamSynchronize(s);
+    cudaFree(drp); cudaFree(dcol); cudaFree(dval); cudaFree(drhs); cudaFree(dw); cudaFree(dxl);
+  }
+  if (e == cudaSuccess) e = crs_prepare(r->A, mixed, s);
+  if (e == cudaSuccess) {
+    // true footprint now known
+    const size_t actual = (size_t)device_bytes(r->A) + (size_t)r->n_rhs * SystemSlot::bytes_for(r->n, r->A.tile_rows, mixed);
+    S->used = S->used - std::min(S->used, r->bytes) + actual;
+    r->bytes = actual;
+    r->slots.resize((size_t)r->n_rhs);
+    const SolveParams prm = params_of(S);
+    for (int k = 0; k < r->n_rhs && e == cudaSuccess; ++k) {
+      e = r->slots[k].alloc(&r->A, mixed, s);
+      if (e != cudaSuccess) break;
+      const double* bk = r->kind == 0 ? r->b.data() + (size_t)k * r->n : r->d_rhs + (size_t)k * r->n;
+      const double* xk = r->x0.empty() ? nullptr : r->x0.data() + (size_t)k * r->n;
+      e = r->slots[k].start(bk, xk, prm, s);
+    }
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  // host inputs are no longer needed
+  std::vector<int>().swap(r->rp); std::vector<int>().swap(r->ci); std::vector<double>().swap(r->va);
+  std::vector<double>().swap(r->b); std::vector<double>().swap(r->x0);
+  std::vector<long long>().swap(r->row_ptr); std::vector<int>().swap(r->col);
+  std::vector<double>().swap(r->val); std::vector<double>().swap(r->rhs);
+  std::vector<double>().swap(r->weight); std::vector<double>().swap(r->xl);
+  if (e != cudaSuccess) {
+    r->error = std::string("admission failed: ") + last_error();
+    return false;
+  }
+  r->sys_done.assign((size_t)r->n_rhs, 0);
+  r->res.assign((size_t)r->n_rhs, nlgb_result{});
+  return true;
+}
+
+void release(nlgb_server_s* S, Req* r, cudaStream_t s) {
+  for (auto& sl : r->slots) sl.release(s);
+  r->slots.clear();
+  cudaStreamSynchronize(s);
+  crs_free(r->A);
+  cudaFree(r->d_rhs);
+  r->d_rhs = nullptr;
+  S->used -= std::min(S->used, r->bytes);
+}
+
+void finish_request(nlgb_server_s* S, Req* r, bool ok) {
+  std::lock_guard<std::mutex> lk(S->mu);
+  r->t_done = S->now();
+  r->state = ok ? R_DONE : R_FAILED;
+  if (ok) {
+    S->st.completed += 1;
+    S->latencies.push_back(r->t_done - r->arrival);
+    S->last_done = std::max(S->last_done, r->t_done);
+    for (auto& x : r->res) {
+      S->st.iterations += x.iterations;
+      S->st.algo_bytes += x.algo_bytes;
+    }
+  } else {
+    S->st.failed += 1;
+  }
+  S->cv_done.notify_all();
+}
+
+void fill_result(nlgb_result& o, const SysState& h, double secs, long long n, long long nnz) {
+  o.algo_bytes = algo_bytes(n, nnz, h);
+  o.status = h.status;
+  o.iterations = h.iter;
+  o.refinement_steps = h.outer;
+  o.rel_residual = h.bnorm2 > 0 ? std::sqrt(h.rr / h.bnorm2) : 0.0;
+  o.true_rel_residual = h.bnorm2 > 0 ? std::sqrt(h.rr_true / h.bnorm2) : 0.0;
+  o.seconds = secs;
+}
+
+// Move submissions into the worker's lists and arrived requests to pending.
+// Returns false when the server is stopping and has nothing left.
+bool intake(nlgb_server_s* S, bool block_if_idle) {
+  std::unique_lock<std::mutex> lk(S->mu);
+  for (;;) {
+    while (!S->incoming.empty()) {
+      S->future.push_back(S->incoming.front());
+      S->incoming.pop_front();
+    }
+    const double t = S->now();
+    std::stable_sort(S->future.begin(), S->future.end(),
+                     [](const Req* a, const Req* b) { return a->arrival < b->arrival; });
+    size_t k = 0;
+    while (k < S->future.size() && S->future[k]->arrival <= t) {
+      S->future[k]->state = R_PENDING;
+      S->pending.push_back(S->future[k]);
+      ++k;
+    }
+    S->future.erase(S->future.begin(), S->future.begin() + (long)k);
+    const bool idle = S->active.empty() && S->pending.empty();
+    if (!idle || !block_if_idle) return true;
+    if (S->stop && S->future.empty()) return false;
+    if (S->future.empty()) {
+      S->cv_work.wait(lk, [&] { return S->stop || !S->incoming.empty(); });
+    } else {
+      const double wait_s = std::max(0.0, S->future.front()->arrival - S->now());
+      S->cv_work.wait_for(lk, std::chrono::duration<double>(wait_s),
+                          [&] { return S->stop || !S->incoming.empty(); });
+    }
+  }
+}
+
+void fail_all_waiting(nlgb_server_s* S, const char* why) {
+  std::vector<Req*> drop;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    for (Req* r : S->pending) drop.push_back(r);
+    for (Req* r : S->future) drop.push_back(r);
+    for (Req* r : S->incoming) drop.push_back(r);
+    S->pending.clear(); S->future.clear(); S->incoming.clear();
+  }
+  for (Req* r : drop) {
+    r->error = why;
+    r->status = NL_GB300_STATUS_ABORTED;
+    finish_request(S, r, false);
+  }
+}
+
+void worker_batched(nlgb_server_s* S) {
+  cudaStream_t sc = nullptr, su = nullptr;
+  cudaStreamCreateWithFlags(&sc, cudaStreamNonBlocking);
+  cudaStreamCreateWithFlags(&su, cudaStreamNonBlocking);
+  BatchRunner runner;
+  if (runner.init(sc) != cudaSuccess) {
+    S->fatal = last_error();
+    fail_all_waiting(S, "server could not start on the GPU");
+  }
+  const bool mixed = mixed_of(S);
+  std::vector<SysState> states;
+  std::vector<std::pair<Req*, int>> owner;   // system index -> (request, rhs)
+  int active_systems = 0;
+  auto admit_pending = [&]() {
+    // first fit in arrival order
+    for (size_t i = 0; i < S->pending.size();) {
+      Req* r = S->pending[i];
+      if (S->aborting) break;
+      const bool fits = S->used + r->bytes <= S->cfg.hbm_budget_bytes &&
+                        active_systems + r->n_rhs <= S->cfg.max_systems;
+      if (!fits) { ++i; continue; }
+      S->used += r->bytes;
+      {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->st.peak_bytes = std::max(S->st.peak_bytes, S->used);
+      }
+      S->pending.erase(S->pending.begin() + (long)i);
+      if (admit(S, r, su)) {
+        r->state = R_ACTIVE;
+        S->active.push_back(r);
+        active_systems += r->n_rhs;
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->st.peak_bytes = std::max(S->st.peak_bytes, S->used);
+      } else {
+        release(S, r, su);
+        finish_request(S, r, false);
+      }
+    }
+  };
+  while (S->fatal.empty()) {
+    if (!intake(S, true)) break;
+    if (S->aborting) fail_all_waiting(S, "server aborted");
+    admit_pending();
+    if (S->active.empty()) continue;
+    std::vector<SysView> views;
+    std::vector<long long> work;
+    owner.clear();
+    for (Req* r : S->active)
+      for (int k = 0; k < r->n_rhs; ++k) {
+        if (r->sys_done[k]) continue;
+        views.push_back(r->slots[k].view);
+        work.push_back((r->A.nnz + 8LL * r->A.n));
+        owner.push_back({r, k});
+      }
+    BatchLaunchStats bst;
+    cudaError_t e = runner.launch(views, work, S->aborting ? 1 : S->cfg.epoch_iters);
+    if (e == cudaSuccess) {
+      // overlap: admit what arrived meanwhile while the epoch runs
+      intake(S, false);
+      admit_pending();
+      e = runner.finish(&bst);
+    }
+    if (e == cudaSuccess) {
+      states.resize(views.size());
+      e = runner.gather_states(states.data(), (int)views.size());
+    }
+    if (e != cudaSuccess) {
+      S->fatal = last_error();
+      break;
+    }
+    {
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->st.kernel_s += bst.ms * 1e-3;
+      S->st.epochs += 1;
+    }
+    for (size_t i = 0; i < views.size(); ++i) {
+      Req* r = owner[i].first;
+      const int k = owner[i].second;
+      if (states[i].stage == 3 || S->aborting) {
+        SysState h = states[i];
+        if (h.stage != 3) h.status = ST_ABORTED;
+        r->sys_done[k] = 1;
+        fill_result(r->res[k], h, bst.ms * 1e-3, r->A.n, r->A.nnz);
+      }
+    }
+    for (size_t i = 0; i < S->active.size();) {
+      Req* r = S->active[i];
+      bool all = true;
+      for (int d : r->sys_done) all = all && d;
+      if (!all) { ++i; continue; }
+      bool ok = true;
+      for (int k = 0; k < r->n_rhs; ++k) {
+        if (cudaMemcpyAsync(r->x_out + (size_t)k * r->n, r->slots[k].view.x, sizeof(double) * r->n,
+                            cudaMemcpyDeviceToHost, su) != cudaSuccess) ok = false;
+        if (r->res[k].status != NL_GB300_STATUS_CONVERGED) r->status = r->res[k].status;
+      }
+      cudaStreamSynchronize(su);
+      if (r->status == NL_GB300_STATUS_NONE) r->status = NL_GB300_STATUS_CONVERGED;
+      release(S, r, su);
+      active_systems -= r->n_rhs;
+      S->active.erase(S->active.begin() + (long)i);
+      finish_request(S, r, ok);
+    }
+  }
+  if (!S->fatal.empty()) {
+    for (Req* r : S->active) { r->error = S->fatal; finish_request(S, r, false); }
+    S->active.clear();
+    fail_all_waiting(S, S->fatal.c_str());
+  }
+  cudaStreamSynchronize(sc);
+  cudaStreamDestroy(sc);
+  cudaStreamDestroy(su);
+}
+
+void worker_serial(nlgb_server_s* S) {
+  cudaStream_t s = nullptr;
+  cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  const SolveParams prm = params_of(S);
+  while (true) {
+    if (!intake(S, true)) break;
+    if (S->aborting) { fail_all_waiting(S, "server aborted"); continue; }
+    if (S->pending.empty()) continue;
+    Req* r = S->pending.front();
+    S->pending.erase(S->pending.begin());
+    r->bytes = estimate_bytes(*r, mixed_of(S));
+    S->used += r->bytes;
+    {
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->st.peak_bytes = std::max(S->st.peak_bytes, S->used);
+    }
+    // Reuse the admission upload/assembly, then solve each right-hand side
+    // with the graph-captured single-system solver.
+    bool ok = admit(S, r, s);
+    if (ok) {
+      PcgSolver pcg;
+      ok = pcg.bind(&r->A, s) == cudaSuccess;
+      for (int k = 0; ok && k < r->n_rhs; ++k) {
+        SolveResult sr;
+        const SysView& v = r->slots[k].view;
+        ok = pcg.solve(v.b, v.x, prm, &sr) == cudaSuccess &&
+             cudaMemcpyAsync(r->x_out + (size_t)k * r->n, v.x, sizeof(double) * r->n,
+                             cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+             cudaStreamSynchronize(s) == cudaSuccess;
+        nlgb_result& o = r->res[k];
+        o.status = sr.status; o.iterations = sr.iterations; o.refinement_steps = sr.outer_steps;
+        o.rel_residual = sr.rel_residual; o.true_rel_residual = sr.true_rel_residual;
+        o.seconds = sr.seconds;
+        o.algo_bytes = sr.algo_bytes;
+        if (sr.status != NL_GB300_STATUS_CONVERGED) r->status = sr.status;
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->st.kernel_s += sr.seconds;
+      }
+      if (r->status == NL_GB300_STATUS_NONE) r->status = NL_GB300_STATUS_CONVERGED;
+    }
+    release(S, r, s);
+    finish_request(S, r, ok);
+  }
+  cudaStreamDestroy(s);
+}
+
+long long enqueue(nlgb_server_s* S, std::unique_ptr<Req> r) {
+  if (r->bytes > S->cfg.hbm_budget_bytes) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->st.rejected += 1;
+    set_error("nlgb_server_submit: request footprint exceeds the HBM budget");
+    return NLGB_E_NOMEM;
+  }
+  std::lock_guard<std::mutex> lk(S->mu);
+  if (S->stop || S->aborting) {
+    set_error("nlgb_server_submit: server is stopping");
+    return NLGB_E_STATE;
+  }
+  const long long id = S->next_id++;
+  r->id = id;
+  if (r->arrival < 0) r->arrival = S->now();
+  if (S->first_arrival < 0 || r->arrival < S->first_arrival) S->first_arrival = r->arrival;
+  S->st.submitted += 1;
+  Req* raw = r.get();
+  S->reqs[id] = std::move(r);
+  S->incoming.push_back(raw);
+  S->cv_work.notify_all();
+  return id;
+}
+
+}  // namespace
+
+extern "C" {
+
+void nlgb_server_default_config(nlgb_server_config* c) {
+  if (!c) return;
+  c->hbm_budget_bytes = (size_t)150e9;
+  c->mode = NLGB_SERVER_BATCHED;
+  c->precision = NL_GB300_PRECISION_MIXED;
+  c->eps = 1e-10;
+  c->max_iter = -1;
+  c->inner_eps = 0.1;
+  c->epoch_iters = 256;
+  c->max_systems = 8192;
+}
+
+nlgb_server nlgb_server_create(const nlgb_server_config* cfg) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    set_error("nlgb_server_create: no CUDA device available");
+    return nullptr;
+  }
+  nlgb_server S = new nlgb_server_s();
+  nlgb_server_default_config(&S->cfg);
+  if (cfg) S->cfg = *cfg;
+  if (S->cfg.epoch_iters <= 0) S->cfg.epoch_iters = 256;
+  if (S->cfg.max_systems <= 0) S->cfg.max_systems = 8192;
+  if (S->cfg.precision != NL_GB300_PRECISION_MIXED && S->cfg.precision != NL_GB300_PRECISION_DOUBLE) {
+    set_error("nlgb_server_create: unknown precision");
+    delete S;
+    return nullptr;
+  }
+  S->st.budget_bytes = S->cfg.hbm_budget_bytes;
+  S->origin = Clock::now();
+  S->th = std::thread(S->cfg.mode == NLGB_SERVER_SERIAL ? worker_serial : worker_batched, S);
+  return S;
+}
+
+void nlgb_server_reset_clock(nlgb_server S) {
+  if (!S) return;
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->origin = Clock::now();
+}
+
+double nlgb_server_now(nlgb_server S) { return S ? S->now() : 0.0; }
+
+long long nlgb_server_submit_crs(nlgb_server S, int n, const int* rp, const int* ci,
+                                 const double* va, int n_rhs, const double* b, const double* x0,
+                                 double* x_out, double arrival_s) {
+  if (!S || n < 0 || !rp || !b || !x_out || n_rhs < 1) {
+    set_error("nlgb_server_submit_crs: bad arguments");
+    return NLGB_E_INVALID;
+  }
+  const long long nnz = rp[n];
+  if (rp[0] != 0 || nnz < 0) { set_error("nlgb_server_submit_crs: bad row pointers"); return NLGB_E_INVALID; }
+  for (int i = 0; i < n; ++i)
+    if (rp[i + 1] < rp[i]) { set_error("nlgb_server_submit_crs: row pointers not monotone"); return NLGB_E_INVALID; }
+  for (long long k = 0; k < nnz; ++k)
+    if (ci[k] < 0 || ci[k] >= n) { set_error("nlgb_server_submit_crs: column out of range"); return NLGB_E_INVALID; }
+  auto r = std::make_unique<Req>();
+  r->kind = 0;
+  r->n = n;
+  r->n_rhs = n_rhs;
+  r->rp.assign(rp, rp + n + 1);
+  r->ci.assign(ci, ci + nnz);
+  r->va.assign(va, va + nnz);
+  r->b.assign(b, b + (size_t)n * n_rhs);
+  if (x0) r->x0.assign(x0, x0 + (size_t)n * n_rhs);
+  r->x_out = x_out;
+  r->arrival = arrival_s;
+  r->bytes = estimate_bytes(*r, mixed_of(S));
+  return enqueue(S, std::move(r));
+}
+
+long long nlgb_server_submit_rows(nlgb_server S, int least_squares, long long n_rows,
+                                  const long long* row_ptr, const int* col, const double* val,
+                                  const double* rhs, const double* weight, int n_free, int n_vars,
+                                  const double* xl, int n_rhs, const double* x0, double* x_out,
+                                  double arrival_s) {
+  if (!S || n_rows < 0 || !row_ptr || n_free < 0 || n_vars < n_free || !x_out || n_rhs < 1) {
+    set_error("nlgb_server_submit_rows: bad arguments");
+    return NLGB_E_INVALID;
+  }
+  const long long nc = row_ptr[n_rows];
+  for (long long k = 0; k < nc; ++k) {
+    const int c = col[k];
+    if (c >= n_free || (c < 0 && (-(long long)c - 1) >= n_vars)) {
+      set_error("nlgb_server_submit_rows: coefficient index out of range");
+      return NLGB_E_INVALID;
+    }
+  }
+  if (!least_squares && n_rows != n_free) {
+    set_error("nlgb_server_submit_rows: a square system needs one row per free variable");
+    return NLGB_E_INVALID;
+  }
+  auto r = std::make_unique<Req>();
+  r->kind = 1;
+  r->least_squares = least_squares ? 1 : 0;
+  r->n = n_free;
+  r->n_vars = n_vars;
+  r->n_rhs = n_rhs;
+  r->n_rows = n_rows;
+  r->row_ptr.assign(row_ptr, row_ptr + n_rows + 1);
+  r->col.assign(col, col + nc);
+  r->val.assign(val, val + nc);
+  if (rhs) { r->rhs.assign(rhs, rhs + (size_t)n_rows * n_rhs); r->has_rhs = true; }
+  if (weight) { r->weight.assign(weight, weight + n_rows); r->has_weight = true; }
+  if (xl) { r->xl.assign(xl, xl + (size_t)n_vars * n_rhs); r->has_xl = true; }
+  if (x0) r->x0.assign(x0, x0 + (size_t)n_free * n_rhs);
+  r->x_out = x_out;
+  r->arrival = arrival_s;
+  r->bytes = estimate_bytes(*r, mixed_of(S));
+  return enqueue(S, std::move(r));
+}
+
+int nlgb_server_wait(nlgb_server S, long long ticket, nlgb_result* res, double* latency_s) {
+  if (!S) return NLGB_E_INVALID;
+  std::unique_lock<std::mutex> lk(S->mu);
+  auto it = S->reqs.find(ticket);
+  if (it == S->reqs.end()) { set_error("nlgb_server_wait: unknown ticket"); return NLGB_E_INVALID; }
+  Req* r = it->second.get();
+  S->cv_done.wait(lk, [&] { return r->state == R_DONE || r->state == R_FAILED; });
+  if (res)
+    for (int k = 0; k < r->n_rhs; ++k) res[k] = k < (int)r->res.size() ? r->res[k] : nlgb_result{};
+  if (latency_s) *latency_s = r->t_done - r->arrival;
+  if (r->state == R_FAILED) {
+    set_error(r->error.empty() ? "request failed" : r->error);
+    return NLGB_E_DEVICE;
+  }
+  return NLGB_OK;
+}
+
+int nlgb_server_drain(nlgb_server S) {
+  if (!S) return NLGB_E_INVALID;
+  std::unique_lock<std::mutex> lk(S->mu);
+  S->cv_done.wait(lk, [&] { return S->st.completed + S->st.failed >= S->st.submitted; });
+  return S->st.failed ? NLGB_E_DEVICE : NLGB_OK;
+}
+
+int nlgb_server_get_stats(nlgb_server S, nlgb_server_stats* out) {
+  if (!S || !out) return NLGB_E_INVALID;
+  std::lock_guard<std::mutex> lk(S->mu);
+  nlgb_server_stats st = S->st;
+  st.p50_latency_s = percentile(S->latencies, 0.50);
+  st.p99_latency_s = percentile(S->latencies, 0.99);
+  double sum = 0.0, mx = 0.0;
+  for (double l : S->latencies) { sum += l; mx = std::max(mx, l); }
+  st.mean_latency_s = S->latencies.empty() ? 0.0 : sum / S->latencies.size();
+  st.max_latency_s = mx;
+  st.wall_s = S->first_arrival >= 0 ? std::max(0.0, S->last_done - S->first_arrival) : 0.0;
+  st.solves_per_s = st.wall_s > 0 ? double(st.completed) / st.wall_s : 0.0;
+  *out = st;
+  return NLGB_OK;
+}
+
+void nlgb_server_abort(nlgb_server S) {
+  if (!S) return;
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->aborting = true;
+  S->cv_work.notify_all();
+}
+
+void nlgb_server_destroy(nlgb_server S) {
+  if (!S) return;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stop = true;
+    S->cv_work.notify_all();
+  }
+  if (S->th.joinable()) S->th.join();
+  delete S;
+}
+
+}  // extern "C"

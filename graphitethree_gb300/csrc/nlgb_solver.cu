@@ -192,14 +192,7 @@ __global__ void __launch_bounds__(kCTA) k_spmv(int n, int tile_rows, const int* 
                                                const X* __restrict__ x, X* __restrict__ y) {
   const int lo = blockIdx.x * tile_rows;
   const int hi = min(lo + tile_rows, n);
-  const int sub = threadIdx.x / T, lane = threadIdx.x % T;
-  constexpr int RPP = kCTA / T;
-  for (int base = lo; base < hi; base += RPP) {
-    const int row = base + sub;
-    const bool valid = row < hi;
-    const X v = row_dot<T, V, X, X>(rp, ci, va, x, row, valid, lane);
-    if (valid && lane == 0) y[row] = v;
-  }
+  tile_rows_dot<T, V, X, X, false>(rp, ci, va, x, lo, hi, [&](int row, X v) { y[row] = v; });
 }
 
 // dinv[i] = 1 / a_ii (1 when the diagonal is missing or zero); fp32 copies.
@@ -249,10 +242,11 @@ static int grid_for(long long n, int threads) {
 }
 
 TuneChoice autotune(int n, long long nnz, int max_row, const int* hist33) {
-  // Threads per row: the smallest power of two with at most ~4 nonzeros per
+  // Threads per row: the smallest power of two with at most ~8 nonzeros per
   // lane for the typical row (measured on GB300 with the 7-nonzero cotangent
-  // Laplacian: 2 threads/row 4.3 TB/s, 4 -> 2.6, 8 -> 1.4), raised when
-  // long rows dominate.
+  // Laplacian: 1 thread/row 5.25 TB/s, 2 -> 4.4, 4 -> 2.7, 8 -> 1.4; with the
+  // 14-nonzero LSCM normal matrix 2 threads/row is best), raised when long
+  // rows dominate.
   long long cnt = 0, acc = 0;
   for (int b = 0; b < 33; ++b) { cnt += hist33 ? hist33[b] : 0; acc += hist33 ? (long long)hist33[b] * b : 0; }
   const double mean = n > 0 ? double(nnz) / double(n) : 0.0;
@@ -266,13 +260,11 @@ TuneChoice autotune(int n, long long nnz, int max_row, const int* hist33) {
   }
   const double typical = std::max(mean, 0.75 * double(p90 == 32 ? std::max(32, max_row) : p90));
   int tpr = 1;
-  while (tpr < 32 && tpr * 4 < typical) tpr *= 2;
-  // Tile rows: enough tiles for about one resident wave of CTAs on the 152
-  // SMs (more, smaller tiles for mid-size systems, which are latency-bound),
-  // 128..4096 rows.
-  long long want = (long long)n / (152LL * 6);
-  int tile = 128;
-  while (tile < 4096 && tile < want) tile *= 2;
+  while (tpr < 32 && tpr * 8 < typical) tpr *= 2;
+  // Tile rows: small tiles keep many CTAs in flight (measured on GB300: the
+  // 4.2M-row Laplacian SpMV runs at 5.25 TB/s with 256-row tiles vs 4.93
+  // with 4096; the L2-resident 131k-row LSCM matrix is fastest at 128).
+  const int tile = n >= (1 << 20) ? 256 : 128;
   (void)acc;
   return TuneChoice{tpr, tile};
 }
@@ -281,7 +273,10 @@ cudaError_t row_histogram(const DeviceCRS& A, int* hist33_host, int* max_row, cu
   int* d = nullptr;
   NLGB_CUDA_TRY(cudaMallocAsync(&d, 34 * sizeof(int), s));
   NLGB_CUDA_TRY(cudaMemsetAsync(d, 0, 34 * sizeof(int), s));
-  if (A.n > 0) k_row_hist<<<grid_for(A.n, 256), 256, 0, s>>>(A.n, A.rp, d, d + 33);
+  if (A.n > 0) {
+    k_row_hist<<<grid_for(A.n, 256), 256, 0, s>>>(A.n, A.rp, d, d + 33);
+    count_launches(1);
+  }
   NLGB_CUDA_TRY(cudaGetLastError());
   int h[34];
   NLGB_CUDA_TRY(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s));
@@ -343,12 +338,18 @@ cudaError_t crs_prepare(DeviceCRS& A, bool need_fp32, cudaStream_t s) {
   if (!A.dinv) {
     NLGB_CUDA_TRY(cudaMalloc(&A.dinv, (size_t)std::max(1, A.n) * sizeof(double)));
     NLGB_CUDA_TRY(cudaMalloc(&A.dinv32, (size_t)std::max(1, A.n) * sizeof(float)));
-    if (A.n > 0) k_jacobi<<<(A.n + 255) / 256, 256, 0, s>>>(A.n, A.rp, A.ci, A.va, A.dinv, A.dinv32);
+    if (A.n > 0) {
+      k_jacobi<<<(A.n + 255) / 256, 256, 0, s>>>(A.n, A.rp, A.ci, A.va, A.dinv, A.dinv32);
+      count_launches(1);
+    }
     NLGB_CUDA_TRY(cudaGetLastError());
   }
   if (need_fp32 && !A.va32) {
     NLGB_CUDA_TRY(cudaMalloc(&A.va32, (size_t)std::max(1LL, A.nnz) * sizeof(float)));
-    if (A.nnz > 0) k_to_f32<<<grid_for(A.nnz, 256), 256, 0, s>>>(A.nnz, A.va, A.va32);
+    if (A.nnz > 0) {
+      k_to_f32<<<grid_for(A.nnz, 256), 256, 0, s>>>(A.nnz, A.va, A.va32);
+      count_launches(1);
+    }
     NLGB_CUDA_TRY(cudaGetLastError());
   }
   return cudaSuccess;
@@ -361,11 +362,17 @@ static cudaError_t spmv_dispatch(const DeviceCRS& A, const V* va, const X* x, X*
   const int grid = (A.n + tile - 1) / tile;
   switch (A.tpr > 0 ? A.tpr : 4) {
     case 1: k_spmv<1, V, X><<<grid, kCTA, 0, s>>>(A.n, tile, A.rp, A.ci, va, x, y); break;
+    count_launches(1);
     case 2: k_spmv<2, V, X><<<grid, kCTA, 0, s>>>(A.n, tile, A.rp, A.ci, va, x, y); break;
+    count_launches(1);
     case 4: k_spmv<4, V, X><<<grid, kCTA, 0, s>>>(A.n, tile, A.rp, A.ci, va, x, y); break;
+    count_launches(1);
     case 8: k_spmv<8, V, X><<<grid, kCTA, 0, s>>>(A.n, tile, A.rp, A.ci, va, x, y); break;
+    count_launches(1);
     case 16: k_spmv<16, V, X><<<grid, kCTA, 0, s>>>(A.n, tile, A.rp, A.ci, va, x, y); break;
+    count_launches(1);
     default: k_spmv<32, V, X><<<grid, kCTA, 0, s>>>(A.n, tile, A.rp, A.ci, va, x, y); break;
+    count_launches(1);
   }
   return cudaGetLastError();
 }
@@ -578,18 +585,15 @@ cudaError_t PcgSolver::build_mixed_graph() {
   return cudaSuccess;
 }
 
-cudaError_t PcgSolver::solve(const double* b, double* x, const SolveParams& prm, SolveResult* res) {
-  const bool mixed = prm.precision == 1;
-  if (mixed) {
-    NLGB_CUDA_TRY(crs_prepare(*A_, true, stream_));
-    NLGB_CUDA_TRY(alloc(true));
-  }
+// Runs one graph (mixed or plain) on the internal b_ / x_; `done` > 0
+// continues a mixed solve that fell back to FP64 after `done` iterations.
+// Leaves the final state in st_host_.
+cudaError_t PcgSolver::run_graph(bool mixed, const SolveParams& prm, long long max_iter,
+                                 long long done, int outer, float* ms) {
   if (mixed && !mixed_exec_) NLGB_CUDA_TRY(build_mixed_graph());
   if (!mixed && !plain_exec_) NLGB_CUDA_TRY(build_plain_graph());
-
   SysState* h = (SysState*)st_host_;
   std::memset(h, 0, sizeof(SysState));
-  const long long max_iter = prm.max_iter >= 0 ? prm.max_iter : 5LL * n_;
   h->thresh2 = prm.eps * prm.eps;
   h->max_iter = max_iter;
   h->status = ST_RUNNING;
@@ -599,13 +603,15 @@ cudaError_t PcgSolver::solve(const double* b, double* x, const SolveParams& prm,
   // a reliable update at least every kMaxItersBetweenUpdates iterations
   h->in_max = (int)std::max(1LL, std::min<long long>(max_iter, kMaxItersBetweenUpdates));
   h->precision = mixed ? 1 : 0;
+  h->iter = done;
+  h->outer = outer;
+  h->fell_back = done > 0 || outer > 0 ? 1 : 0;
+  h->iter_at_fallback = done;
   // Hard cap on while-body passes: enough for max_iter iterations plus the
   // outer steps; reached only if the scalar logic failed to stop the loop.
   const int unroll = mixed ? kUnrollInner : kUnrollPlain;
-  h->guard_cap = max_iter / unroll + 2LL * (h->max_outer + 2) + 4;
+  h->guard_cap = std::max(0LL, max_iter - done) / unroll + 2LL * (h->max_outer + 2) + 4;
   NLGB_CUDA_TRY(cudaMemcpyAsync(st_, h, sizeof(SysState), cudaMemcpyHostToDevice, stream_));
-  NLGB_CUDA_TRY(cudaMemcpyAsync(b_, b, (size_t)n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
-  NLGB_CUDA_TRY(cudaMemcpyAsync(x_, x, (size_t)n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
   if (mixed) {
     NLGB_CUDA_TRY(cudaMemsetAsync(c32_, 0, (size_t)n_ * sizeof(float), stream_));
     NLGB_CUDA_TRY(cudaMemsetAsync(p32_, 0, (size_t)n_ * sizeof(float), stream_));
@@ -613,11 +619,43 @@ cudaError_t PcgSolver::solve(const double* b, double* x, const SolveParams& prm,
   NLGB_CUDA_TRY(cudaEventRecord(ev0_, stream_));
   NLGB_CUDA_TRY(cudaGraphLaunch(mixed ? mixed_exec_ : plain_exec_, stream_));
   NLGB_CUDA_TRY(cudaEventRecord(ev1_, stream_));
-  NLGB_CUDA_TRY(cudaMemcpyAsync(x, x_, (size_t)n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
   NLGB_CUDA_TRY(cudaMemcpyAsync(h, st_, sizeof(SysState), cudaMemcpyDeviceToHost, stream_));
   NLGB_CUDA_TRY(cudaStreamSynchronize(stream_));
+  NLGB_CUDA_TRY(cudaEventElapsedTime(ms, ev0_, ev1_));
+  ++graph_launches_;
+  // Kernel nodes executed: every while-body pass runs all of its kernels
+  // (3 per unrolled iteration + the guard); the mixed graph adds 2 kernels
+  // per reliable update after the first; plus the first and final kernels.
+  const long long passes = h->guard;
+  long long k = 2 + passes * (3LL * unroll + 1);
+  if (mixed) k += 2LL * std::max(0, h->outer - outer - 1);
+  count_launches(k);
+  return cudaSuccess;
+}
+
+cudaError_t PcgSolver::solve(const double* b, double* x, const SolveParams& prm, SolveResult* res) {
+  const bool mixed = prm.precision == 1;
+  if (mixed) {
+    NLGB_CUDA_TRY(crs_prepare(*A_, true, stream_));
+    NLGB_CUDA_TRY(alloc(true));
+  }
+  const long long max_iter = prm.max_iter >= 0 ? prm.max_iter : 5LL * n_;
+  NLGB_CUDA_TRY(cudaMemcpyAsync(b_, b, (size_t)n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
+  NLGB_CUDA_TRY(cudaMemcpyAsync(x_, x, (size_t)n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
   float ms = 0.f;
-  NLGB_CUDA_TRY(cudaEventElapsedTime(&ms, ev0_, ev1_));
+  NLGB_CUDA_TRY(run_graph(mixed, prm, max_iter, 0, 0, &ms));
+  SysState* h = (SysState*)st_host_;
+  if (mixed && h->status == ST_STAGNATION && !h->fell_back) {
+    // FP32 cannot track this system (kappa * u32 ~ 1): continue it with the
+    // FP64 PCG from the current x, keeping the iteration count.
+    const long long done = h->iter;
+    const int outer = h->outer;
+    float ms2 = 0.f;
+    NLGB_CUDA_TRY(run_graph(false, prm, max_iter, done, outer, &ms2));
+    ms += ms2;
+  }
+  NLGB_CUDA_TRY(cudaMemcpyAsync(x, x_, (size_t)n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
+  NLGB_CUDA_TRY(cudaStreamSynchronize(stream_));
   if (res) {
     res->status = h->status;
     res->iterations = h->iter;
@@ -626,6 +664,7 @@ cudaError_t PcgSolver::solve(const double* b, double* x, const SolveParams& prm,
     res->rel_residual = bb > 0 ? std::sqrt(h->rr / bb) : 0.0;
     res->true_rel_residual = bb > 0 ? std::sqrt(h->rr_true / bb) : 0.0;
     res->seconds = ms * 1e-3;
+    res->algo_bytes = algo_bytes(n_, A_->nnz, *h);
   }
   return cudaSuccess;
 }

@@ -37,6 +37,7 @@ class SolveInfo:
     rel_residual: float
     true_rel_residual: float
     seconds: float
+    algo_bytes: float = 0.0
 
 
 def _ptr(a, t):
@@ -124,7 +125,7 @@ class Matrix:
         _check(L.nlgb_solve(self._h, _ptr(b, None), _ptr(x, None), ctypes.byref(p), ctypes.byref(r)),
                "nlgb_solve")
         return x, SolveInfo(STATUS.get(r.status, str(r.status)), r.iterations, r.refinement_steps,
-                            r.rel_residual, r.true_rel_residual, r.seconds)
+                            r.rel_residual, r.true_rel_residual, r.seconds, r.algo_bytes)
 
     def solve_device(self, b_ptr: int, x_ptr: int, eps: float = 1e-10, max_iter: int = -1,
                      precision: str = "double", inner_eps: float = 0.1, max_outer: int = 100000):
@@ -135,7 +136,7 @@ class Matrix:
         _check(L.nlgb_solve(self._h, ctypes.c_void_p(b_ptr), ctypes.c_void_p(x_ptr), ctypes.byref(p),
                             ctypes.byref(r)), "nlgb_solve")
         return SolveInfo(STATUS.get(r.status, str(r.status)), r.iterations, r.refinement_steps,
-                         r.rel_residual, r.true_rel_residual, r.seconds)
+                         r.rel_residual, r.true_rel_residual, r.seconds, r.algo_bytes)
 
 
 def batch_solve(mats, bs, x0s=None, eps: float = 1e-10, max_iter: int = -1,
@@ -156,8 +157,112 @@ def batch_solve(mats, bs, x0s=None, eps: float = 1e-10, max_iter: int = -1,
     secs = ctypes.c_double()
     _check(L.nlgb_batch_solve(n, A, B, X, ctypes.byref(p), R, ctypes.byref(secs)), "nlgb_batch_solve")
     infos = [SolveInfo(STATUS.get(r.status, str(r.status)), r.iterations, r.refinement_steps,
-                       r.rel_residual, r.true_rel_residual, r.seconds) for r in R]
+                       r.rel_residual, r.true_rel_residual, r.seconds, r.algo_bytes) for r in R]
     return xs, infos, secs.value
+
+
+class Server:
+    """Continuous-batching solve server (nl_gb300.h nlgb_server_*).
+
+    submit_* copy the inputs and return a ticket; the solution lands in a
+    host buffer owned by this object, returned by ``wait``."""
+
+    def __init__(self, budget_bytes: float = 150e9, precision: str = "mixed", mode: str = "batched",
+                 eps: float = 1e-10, epoch_iters: int = 256, inner_eps: float = 0.1,
+                 max_systems: int = 8192, max_iter: int = -1):
+        L = _lib.load()
+        cfg = _lib.NlgbServerConfig()
+        L.nlgb_server_default_config(ctypes.byref(cfg))
+        cfg.hbm_budget_bytes = int(budget_bytes)
+        cfg.mode = K["NLGB_SERVER_BATCHED"] if mode == "batched" else K["NLGB_SERVER_SERIAL"]
+        cfg.precision = PRECISION[precision]
+        cfg.eps = eps
+        cfg.epoch_iters = epoch_iters
+        cfg.inner_eps = inner_eps
+        cfg.max_systems = max_systems
+        cfg.max_iter = max_iter
+        h = L.nlgb_server_create(ctypes.byref(cfg))
+        if not h:
+            raise SolverError(f"nlgb_server_create failed: {_lib.last_error()}")
+        self._h = h
+        self._out = {}
+
+    def now(self) -> float:
+        return _lib.load().nlgb_server_now(self._h)
+
+    def reset_clock(self):
+        _lib.load().nlgb_server_reset_clock(self._h)
+
+    def submit_square(self, sq, arrival: float = -1.0, x0=None) -> int:
+        rp = np.ascontiguousarray(sq.rp, np.int32); ci = np.ascontiguousarray(sq.ci, np.int32)
+        va = np.ascontiguousarray(sq.va, np.float64); b = np.ascontiguousarray(sq.rhs, np.float64)
+        k = b.shape[0]
+        out = np.empty((k, sq.n), np.float64)
+        x0 = None if x0 is None else np.ascontiguousarray(x0, np.float64)
+        t = _lib.load().nlgb_server_submit_crs(
+            self._h, sq.n, rp.ctypes.data_as(_lib.i32p), ci.ctypes.data_as(_lib.i32p),
+            va.ctypes.data_as(_lib.f64p), k, b.ctypes.data_as(_lib.f64p),
+            None if x0 is None else x0.ctypes.data_as(_lib.f64p), out.ctypes.data_as(_lib.f64p),
+            float(arrival))
+        if t < 0:
+            raise SolverError(f"submit failed ({t}): {_lib.last_error()}")
+        self._out[t] = out
+        return t
+
+    def submit_rows(self, rs: RowStream, arrival: float = -1.0) -> int:
+        col = rs.encoded_cols()
+        n_free = int((rs.locked == 0).sum())
+        k = rs.n_systems
+        out = np.empty((k, n_free), np.float64)
+        rp = np.ascontiguousarray(rs.row_ptr, np.int64)
+        val = np.ascontiguousarray(rs.val, np.float64)
+        rhs = np.ascontiguousarray(rs.rhs.T, np.float64)
+        xl = np.ascontiguousarray(rs.values, np.float64)
+        w = None if rs.weight is None else np.ascontiguousarray(rs.weight, np.float64)
+        t = _lib.load().nlgb_server_submit_rows(
+            self._h, int(rs.least_squares), rs.n_rows, rp.ctypes.data_as(_lib.i64p),
+            col.ctypes.data_as(_lib.i32p), val.ctypes.data_as(_lib.f64p),
+            rhs.ctypes.data_as(_lib.f64p), None if w is None else w.ctypes.data_as(_lib.f64p),
+            n_free, rs.n_vars, xl.ctypes.data_as(_lib.f64p), k, None,
+            out.ctypes.data_as(_lib.f64p), float(arrival))
+        if t < 0:
+            raise SolverError(f"submit failed ({t}): {_lib.last_error()}")
+        self._out[t] = out
+        return t
+
+    def wait(self, ticket: int):
+        """Returns (solutions (n_rhs, n), [SolveInfo], latency_s)."""
+        out = self._out[ticket]
+        R = (_lib.NlgbResult * out.shape[0])()
+        lat = ctypes.c_double()
+        rc = _lib.load().nlgb_server_wait(self._h, ticket, R, ctypes.byref(lat))
+        infos = [SolveInfo(STATUS.get(r.status, str(r.status)), r.iterations, r.refinement_steps,
+                           r.rel_residual, r.true_rel_residual, r.seconds, r.algo_bytes) for r in R]
+        if rc != 0:
+            raise SolverError(f"request {ticket} failed: {_lib.last_error()}")
+        return out, infos, lat.value
+
+    def drain(self) -> int:
+        return _lib.load().nlgb_server_drain(self._h)
+
+    def stats(self) -> dict:
+        st = _lib.NlgbServerStats()
+        _check(_lib.load().nlgb_server_get_stats(self._h, ctypes.byref(st)), "stats")
+        return {f: getattr(st, f) for f, _ in st._fields_}
+
+    def abort(self):
+        _lib.load().nlgb_server_abort(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().nlgb_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def assemble(rs: RowStream):

@@ -43,10 +43,17 @@ typedef struct {
     double    rel_residual;       /* residual the stopping test used       */
     double    true_rel_residual;  /* ||b-Ax||/||b|| recomputed in FP64     */
     double    seconds;            /* device time of the iteration (events) */
+    double    algo_bytes;         /* algorithmic HBM bytes moved by the solve:
+                                     per FP64 iteration 12 nnz + 108 n, per FP32
+                                     iteration 8 nnz + 56 n, per reliable update
+                                     12 nnz + 52 n, + initial/final residuals */
 } nlgb_result;
 
 /* ---- device / errors ---- */
 int         nlgb_device_available(void);
+/* Kernels this library has launched in the process so far (host launches
+ * plus the kernel nodes executed inside the solver's CUDA graphs). */
+long long   nlgb_kernel_launches(void);
 const char* nlgb_last_error(void);
 void        nlgb_default_params(nlgb_params* p);
 
@@ -104,6 +111,79 @@ int nlgb_assemble(int least_squares, long long n_rows, const long long* row_ptr,
                   const double* val, const double* rhs, const double* weight, int n_free,
                   int n_vars, const double* xl, int n_systems, nlgb_matrix* A_out,
                   double* rhs_out, double* seconds);
+
+/* ---- solve server: continuous batching under an HBM budget ----
+ * No reference counterpart as a component: in Graphite every nlSolve is a
+ * synchronous call made under the global command lock
+ * (src/lib/OGF/scene_graph/commands/commands.cpp:99-117).  The server
+ * accepts solves of any size at any time, admits them while their device
+ * footprint fits the HBM budget, keeps their matrices and Krylov state
+ * resident until convergence and advances every admitted system together:
+ * each "epoch" is one persistent-kernel launch that runs every active system
+ * for up to epoch_iters iterations; requests arriving meanwhile are
+ * uploaded (and least-squares rows assembled) on a second stream while the
+ * epoch runs and join the next epoch.  A result does not depend on what else
+ * is in flight (bit-identical alone and in any mix). */
+typedef struct nlgb_server_s* nlgb_server;
+
+#define NLGB_SERVER_BATCHED 0   /* continuous batching, persistent kernel     */
+#define NLGB_SERVER_SERIAL  1   /* one request at a time, graph-captured PCG  */
+
+typedef struct {
+    size_t    hbm_budget_bytes;  /* admission limit (default 150e9)            */
+    int       mode;              /* NLGB_SERVER_BATCHED / NLGB_SERVER_SERIAL    */
+    int       precision;         /* NL_GB300_PRECISION_MIXED (default) / _DOUBLE */
+    double    eps;               /* relative residual (default 1e-10)          */
+    long long max_iter;          /* < 0: 5 n per system                         */
+    double    inner_eps;         /* mixed reliable-update factor (0.1)         */
+    long long epoch_iters;       /* iterations per system per epoch (256)      */
+    int       max_systems;       /* active systems at once (default 8192)      */
+} nlgb_server_config;
+
+typedef struct {
+    long long submitted, completed, failed, rejected;
+    double    p50_latency_s, p99_latency_s, mean_latency_s, max_latency_s;
+    double    solves_per_s;      /* completed / (last completion - first arrival) */
+    double    wall_s;            /* first arrival -> last completion           */
+    double    kernel_s;          /* device time of all epochs / serial solves  */
+    long long epochs;
+    long long iterations;        /* PCG iterations over all systems            */
+    double    algo_bytes;        /* algorithmic HBM bytes over all systems     */
+    size_t    peak_bytes;        /* peak admitted device footprint             */
+    size_t    budget_bytes;
+} nlgb_server_stats;
+
+void        nlgb_server_default_config(nlgb_server_config* cfg);
+nlgb_server nlgb_server_create(const nlgb_server_config* cfg);
+/* Restart the server clock at 0 (arrival times are relative to it). */
+void        nlgb_server_reset_clock(nlgb_server srv);
+double      nlgb_server_now(nlgb_server srv);
+/* Square SPD system in CRS form with n_rhs right-hand sides b[k*n + i]
+ * (x0: NULL or n_rhs*n initial guesses).  x_out (host, n_rhs*n) receives the
+ * solutions and must stay valid until nlgb_server_wait returns.  The input
+ * arrays are copied before the call returns.  arrival_s: time on the server
+ * clock before which the request is not admitted (< 0: now).  Returns a
+ * ticket >= 0 or a negative NLGB_E* code (e.g. a request larger than the
+ * whole budget is rejected with NLGB_E_NOMEM). */
+long long   nlgb_server_submit_crs(nlgb_server srv, int n, const int* rp, const int* ci,
+                                   const double* va, int n_rhs, const double* b, const double* x0,
+                                   double* x_out, double arrival_s);
+/* Least-squares (or square) row stream, assembled on the GPU at admission;
+ * same conventions as nlgb_assemble; x_out holds n_rhs * n_free values. */
+long long   nlgb_server_submit_rows(nlgb_server srv, int least_squares, long long n_rows,
+                                    const long long* row_ptr, const int* col, const double* val,
+                                    const double* rhs, const double* weight, int n_free,
+                                    int n_vars, const double* xl, int n_rhs, const double* x0,
+                                    double* x_out, double arrival_s);
+/* Block until the ticket completes; res: n_rhs entries (may be NULL). */
+int         nlgb_server_wait(nlgb_server srv, long long ticket, nlgb_result* res,
+                             double* latency_s);
+int         nlgb_server_drain(nlgb_server srv);
+int         nlgb_server_get_stats(nlgb_server srv, nlgb_server_stats* st);
+/* Stop admitting and abort: active systems stop at the next epoch boundary
+ * with NL_GB300_STATUS_ABORTED. */
+void        nlgb_server_abort(nlgb_server srv);
+void        nlgb_server_destroy(nlgb_server srv);
 
 /* ---- bulk rows for the current OpenNL context ----
  * Exactly equivalent to, for each row r: nlBegin(NL_ROW); nlCoefficient(

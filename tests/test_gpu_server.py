@@ -1,0 +1,112 @@
+"""Solve server: continuous batching under an HBM budget.  Each result must
+be the same alone and in the mix (bit-identical here, which is stronger than
+the 1e-8 solution tolerance the solver guarantees), admission must respect
+the budget, and failures must be reported, not hung."""
+import numpy as np
+import pytest
+
+from graphitethree_gb300 import solver, systems
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests():
+    reqs = []
+    for side, seed in [(40, 1), (18, 2), (70, 3)]:
+        reqs.append(("rows", systems.lscm_system(side, side - 3, seed=seed)))
+    for side, seed in [(50, 4), (25, 5), (90, 6)]:
+        reqs.append(("square", systems.fairing_system(side, side + 7, seed=seed)))
+    return reqs
+
+
+def _submit(srv, kind, obj, arrival=-1.0):
+    return srv.submit_rows(obj, arrival) if kind == "rows" else srv.submit_square(obj, arrival)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "double"])
+def test_result_same_alone_and_in_mix(gpu_ok, precision):
+    reqs = _requests()
+    alone = []
+    for kind, obj in reqs:
+        srv = solver.Server(precision=precision, budget_bytes=2e9)
+        t = _submit(srv, kind, obj)
+        x, infos, lat = srv.wait(t)
+        alone.append((x.copy(), [i.iterations for i in infos]))
+        srv.close()
+    srv = solver.Server(precision=precision, budget_bytes=2e9, epoch_iters=64)
+    tickets = [_submit(srv, kind, obj, arrival=0.002 * i) for i, (kind, obj) in enumerate(reqs)]
+    for t, (xa, ia) in zip(tickets, alone):
+        x, infos, lat = srv.wait(t)
+        assert all(i.status == "converged" for i in infos), infos
+        assert [i.iterations for i in infos] == ia
+        assert np.array_equal(x, xa)
+        assert lat >= 0
+    st = srv.stats()
+    assert st["completed"] == len(reqs) and st["failed"] == 0
+    assert st["epochs"] >= 2 and st["solves_per_s"] > 0
+    srv.close()
+
+
+def test_server_matches_oracle_and_single_solver(gpu_ok, oracle_mod):
+    rs = systems.lscm_system(45, 40, seed=7)
+    fs = systems.fairing_system(60, 60, seed=8)
+    srv = solver.Server(precision="mixed")
+    t1 = srv.submit_rows(rs)
+    t2 = srv.submit_square(fs)
+    x1, i1, _ = srv.wait(t1)
+    x2, i2, _ = srv.wait(t2)
+    rp, ci, va, rhs = oracle_mod.assemble_rowstream(rs)
+    xd = oracle_mod.direct_solve(rp, ci, va, rhs[0])
+    assert np.linalg.norm(x1[0] - xd) / np.linalg.norm(xd) <= 1e-8
+    for k in range(3):
+        xf = oracle_mod.direct_solve(fs.rp, fs.ci, fs.va, fs.rhs[k])
+        assert np.linalg.norm(x2[k] - xf) / np.linalg.norm(xf) <= 1e-8
+        assert i2[k].true_rel_residual <= 1e-10
+    # the mixed server equals the single-system mixed solver bit for bit
+    F = solver.Matrix(fs.rp, fs.ci, fs.va)
+    xs, info = F.solve(fs.rhs[1], precision="mixed")
+    assert np.array_equal(xs, x2[1])
+    srv.close()
+
+
+def test_budget_admission_queues_and_rejects(gpu_ok):
+    fs = [systems.fairing_system(64, 64, seed=s) for s in range(6)]
+    one = solver.Server(budget_bytes=1e9)
+    t = one.submit_square(fs[0])
+    one.wait(t)
+    foot = one.stats()["peak_bytes"]
+    one.close()
+    # room for about two requests at a time: all complete, peak stays in budget
+    srv = solver.Server(budget_bytes=int(2.5 * foot))
+    ts = [srv.submit_square(f) for f in fs]
+    for t in ts:
+        x, infos, _ = srv.wait(t)
+        assert all(i.status == "converged" for i in infos)
+    st = srv.stats()
+    assert st["peak_bytes"] <= 2.5 * foot and st["completed"] == 6
+    # a request larger than the whole budget is rejected up front
+    with pytest.raises(solver.SolverError):
+        srv.submit_square(systems.fairing_system(400, 400, seed=1))
+    assert srv.stats()["rejected"] == 1
+    srv.close()
+
+
+def test_serial_mode_equals_graph_solver(gpu_ok):
+    fs = systems.fairing_system(70, 50, seed=3)
+    srv = solver.Server(mode="serial", precision="double")
+    x, infos, _ = srv.wait(srv.submit_square(fs))
+    F = solver.Matrix(fs.rp, fs.ci, fs.va)
+    for k in range(3):
+        xk, ik = F.solve(fs.rhs[k])
+        assert np.array_equal(xk, x[k]) and ik.iterations == infos[k].iterations
+    srv.close()
+
+
+def test_abort_fails_waiting_requests(gpu_ok):
+    srv = solver.Server()
+    t = srv.submit_square(systems.fairing_system(30, 30, seed=1), arrival=3600.0)
+    srv.abort()
+    with pytest.raises(solver.SolverError):
+        srv.wait(t)
+    assert srv.stats()["failed"] == 1
+    srv.close()
