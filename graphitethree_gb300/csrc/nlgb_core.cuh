@@ -188,44 +188,21 @@ __device__ __forceinline__ A row_dot(const int* __restrict__ rp, const int* __re
   return subwarp_sum<T, A>(sum);
 }
 
-// Rows [lo, hi) of a tile with T threads per row, two passes at a time so
-// every sub-warp keeps two independent gather chains in flight (the
-// persistent kernel and mid-size systems are latency-bound).  epi(row, sum)
-// is called by the row's lane 0 in the same order as a one-pass-at-a-time
-// loop, so per-thread accumulations in epi are unchanged.
+// Rows [lo, hi) of a tile with T threads per row, one pass of kCTA/T rows at
+// a time; epi(row, sum) is called by the row's lane 0.  (Interleaving two
+// rows per sub-warp was measured slower on GB300: 2.96 vs 5.25 TB/s for the
+// 7-nonzero Laplacian SpMV.)
 template <int T, typename VT, typename XT, typename A, bool kCoh, typename Epi>
 __device__ __forceinline__ void tile_rows_dot(const int* __restrict__ rp, const int* __restrict__ ci,
                                               const VT* __restrict__ va, const XT* __restrict__ x,
                                               int lo, int hi, Epi&& epi) {
   const int sub = threadIdx.x / T, lane = threadIdx.x % T;
   constexpr int RPP = kCTA / T;
-  for (int base = lo; base < hi; base += 2 * RPP) {
-    const int ra = base + sub, rb = ra + RPP;
-    const bool oka = ra < hi, okb = rb < hi;
-    A sa = A(0), sb = A(0);
-    int ka = 0, ea = 0, kb = 0, eb = 0;
-    if (oka) { ka = __ldg(rp + ra) + lane; ea = __ldg(rp + ra + 1); }
-    if (okb) { kb = __ldg(rp + rb) + lane; eb = __ldg(rp + rb + 1); }
-    while (ka < ea || kb < eb) {
-      if (ka < ea) {
-        const int c = __ldg(ci + ka);
-        const XT xc = kCoh ? __ldcg(x + c) : __ldg(x + c);
-        sa = fma(A(__ldg(va + ka)), A(xc), sa);
-        ka += T;
-      }
-      if (kb < eb) {
-        const int c = __ldg(ci + kb);
-        const XT xc = kCoh ? __ldcg(x + c) : __ldg(x + c);
-        sb = fma(A(__ldg(va + kb)), A(xc), sb);
-        kb += T;
-      }
-    }
-    sa = subwarp_sum<T, A>(sa);
-    sb = subwarp_sum<T, A>(sb);
-    if (lane == 0) {
-      if (oka) epi(ra, sa);
-      if (okb) epi(rb, sb);
-    }
+  for (int base = lo; base < hi; base += RPP) {
+    const int row = base + sub;
+    const bool valid = row < hi;
+    const A v = row_dot<T, VT, XT, A, kCoh>(rp, ci, va, x, row, valid, lane);
+    if (valid && lane == 0) epi(row, v);
   }
 }
 

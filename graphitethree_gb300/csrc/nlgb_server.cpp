@@ -264,14 +264,17 @@ bool intake(nlgb_server_s* S, bool block_if_idle) {
     }
     S->future.erase(S->future.begin(), S->future.begin() + (long)k);
     const bool idle = S->active.empty() && S->pending.empty();
+    // aborting: hand back control so queued requests are failed at once
+    if (S->aborting && !S->future.empty()) return true;
     if (!idle || !block_if_idle) return true;
-    if (S->stop && S->future.empty()) return false;
     if (S->future.empty()) {
+      if (S->stop) return false;
+      // nothing queued: sleep until a submission or shutdown
       S->cv_work.wait(lk, [&] { return S->stop || !S->incoming.empty(); });
     } else {
       const double wait_s = std::max(0.0, S->future.front()->arrival - S->now());
       S->cv_work.wait_for(lk, std::chrono::duration<double>(wait_s),
-                          [&] { return S->stop || !S->incoming.empty(); });
+                          [&] { return S->stop || S->aborting || !S->incoming.empty(); });
     }
   }
 }
@@ -642,8 +645,10 @@ void nlgb_server_abort(nlgb_server S) {
 void nlgb_server_destroy(nlgb_server S) {
   if (!S) return;
   {
+    // requests still queued or in flight are aborted (callers drain first)
     std::lock_guard<std::mutex> lk(S->mu);
     S->stop = true;
+    S->aborting = true;
     S->cv_work.notify_all();
   }
   if (S->th.joinable()) S->th.join();

@@ -134,7 +134,9 @@ def test_pcg_matches_oracle_and_direct(gpu_ok, oracle_mod, precision, case):
     rp, ci, va, rhs = oracle_mod.assemble_rowstream(rs)
     vals, info = solver.solve_opennl(rs, precision=precision, eps=1e-10)
     assert info["ok"], info
-    assert info["true_error"] <= 1e-10 * (1.0 + 1e-6) or precision == "double"
+    # mixed stops on the true FP64 residual, unless it fell back to FP64 PCG
+    # (LSCM), which stops on the recursive residual like the plain solver
+    assert info["true_error"] <= 1.5e-10
     for s in range(rs.n_systems):
         x_gpu = vals[s][rs.locked == 0]
         x_dir = oracle_mod.direct_solve(rp, ci, va, rhs[s])

@@ -48,9 +48,12 @@ def test_result_same_alone_and_in_mix(gpu_ok, precision):
 
 
 def test_server_matches_oracle_and_single_solver(gpu_ok, oracle_mod):
+    # LSCM normal equations are ill-conditioned: compare with the direct
+    # solution at relative residual 1e-12 (at 1e-10 two correct CG runs can
+    # differ from it by more than 1e-8).
     rs = systems.lscm_system(45, 40, seed=7)
     fs = systems.fairing_system(60, 60, seed=8)
-    srv = solver.Server(precision="mixed")
+    srv = solver.Server(precision="mixed", eps=1e-12)
     t1 = srv.submit_rows(rs)
     t2 = srv.submit_square(fs)
     x1, i1, _ = srv.wait(t1)
@@ -61,10 +64,10 @@ def test_server_matches_oracle_and_single_solver(gpu_ok, oracle_mod):
     for k in range(3):
         xf = oracle_mod.direct_solve(fs.rp, fs.ci, fs.va, fs.rhs[k])
         assert np.linalg.norm(x2[k] - xf) / np.linalg.norm(xf) <= 1e-8
-        assert i2[k].true_rel_residual <= 1e-10
+        assert i2[k].true_rel_residual <= 1e-12
     # the mixed server equals the single-system mixed solver bit for bit
     F = solver.Matrix(fs.rp, fs.ci, fs.va)
-    xs, info = F.solve(fs.rhs[1], precision="mixed")
+    xs, info = F.solve(fs.rhs[1], precision="mixed", eps=1e-12)
     assert np.array_equal(xs, x2[1])
     srv.close()
 
