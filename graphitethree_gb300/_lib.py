@@ -141,6 +141,9 @@ _SIGS = {
     "nlgb_spmv32_timed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, f64p]),
     "nlgb_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(NlgbParams),
                              C.POINTER(NlgbResult)]),
+    "nlgb_solve_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.POINTER(NlgbParams), C.POINTER(NlgbResult),
+                                     C.c_void_p]),
     "nlgb_batch_solve": (C.c_int, [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
                                    C.POINTER(C.c_void_p), C.POINTER(NlgbParams),
                                    C.POINTER(NlgbResult), f64p]),

@@ -22,7 +22,8 @@ LIB_DIR = PKG / "lib"
 LIB_NAME = "libnl_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["nlgb_solver.cu", "nlgb_assembly.cu", "nlgb_blas.cu", "nlgb_batch.cu"]
+CU_SOURCES = ["nlgb_solver.cu", "nlgb_assembly.cu", "nlgb_blas.cu", "nlgb_batch.cu",
+              "nlgb_noalloc.cu"]
 CPP_SOURCES = ["nl_api.cpp", "nl_matrix_api.cpp", "nlgb_api.cpp", "nlgb_server.cpp"]
 
 

@@ -99,6 +99,23 @@ int nlgb_solve(nlgb_matrix A, const double* b, double* x, const nlgb_params* prm
 int nlgb_batch_solve(int n_sys, const nlgb_matrix* A, const double* const* b, double* const* x,
                      const nlgb_params* prm, nlgb_result* res, double* kernel_seconds);
 
+/* ---- one FP64 solve without any device allocation ----
+ * No counterpart in the reference: an addition for callers that cannot
+ * allocate GPU memory -- host applications that reserve all device memory
+ * for their own pools and must keep their footprint fixed, or interactive
+ * loops that cannot afford the device synchronisation cudaMalloc/cudaFree
+ * imply.  Same FP64 Jacobi-PCG as nlgb_solve (NL_GB300_PRECISION_DOUBLE
+ * only).  rp, ci, va (CRS, n x n), b and x are caller-owned DEVICE buffers
+ * (x 16-byte aligned; initial guess in, solution out); all scratch lives in
+ * one static device array of the library (8.1 MiB per GPU, kept until the
+ * process exits), so n is limited to 262144 rows (larger n: NLGB_E_INVALID).
+ * The first call on a device looks up the array's address with that device
+ * current.  Every call reuses the same array: calls that overlap on the GPU
+ * race and must be serialised by the caller.  stream: a cudaStream_t (NULL:
+ * the default stream); the call returns when the solve is finished. */
+int nlgb_solve_noalloc(int n, const int* rp, const int* ci, const double* va, const double* b,
+                       double* x, const nlgb_params* prm, nlgb_result* res, void* stream);
+
 /* ---- least-squares / square assembly on the GPU (nlEnd(NL_MATRIX) of an
  * NL_LEAST_SQUARES context, voxel_grob_transport_commands.cpp:232-279) ----
  * Row stream: row r has coefficients [row_ptr[r], row_ptr[r+1]) of
