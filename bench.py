@@ -66,7 +66,47 @@ def parse_args():
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-spmv", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--profile-case", choices=["spmv", "batch", "plain", "mixed"], default=None,
+                   help="run one small case for an ncu capture and exit")
     return p.parse_args()
+
+
+def profile_case(which):
+    """Small, bounded cases for ncu captures (a few hundred MB on the device).
+    spmv:  3 FP64 SpMVs on the 2048^2 cotangent Laplacian (k_spmv);
+    batch: one persistent-kernel launch over 8 mid-size systems, 300
+           iterations each (k_batch);
+    plain: 20 FP64 PCG iterations on the 2048^2 Laplacian (graph kernels);
+    mixed: 20 FP32/FP64 iterations on the same system."""
+    import ctypes
+    from graphitethree_gb300 import _lib, solver, systems
+    L = _lib.load()
+    if which in ("spmv", "plain", "mixed"):
+        fs = systems.fairing_system(2048, 2048, seed=2)
+        A = solver.Matrix(fs.rp, fs.ci, fs.va)
+        if which == "spmv":
+            import torch
+            x = torch.randn(A.n, dtype=torch.float64, device="cuda")
+            y = torch.empty_like(x)
+            ms = ctypes.c_double()
+            L.nlgb_spmv_timed(A.handle, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr()), 3,
+                              ctypes.byref(ms))
+            print(json.dumps({"case": "spmv", "us": ms.value * 1e3, "tpr": A.threads_per_row,
+                              "tile_rows": A.tile_rows}))
+        else:
+            x, info = A.solve(fs.rhs[0], max_iter=20, precision="double" if which == "plain" else "mixed")
+            print(json.dumps({"case": which, "iterations": info.iterations, "ms": info.seconds * 1e3}))
+        return
+    mats, bs = [], []
+    for s, side in enumerate((180, 150, 120, 90)):
+        M, rhs, _ = solver.assemble(systems.lscm_system(side, side, seed=s))
+        mats.append(M); bs.append(rhs[0])
+        fs = systems.fairing_system(side * 2, side * 2, seed=s)
+        F = solver.Matrix(fs.rp, fs.ci, fs.va)
+        mats.append(F); bs.append(fs.rhs[0])
+    xs, infos, ks = solver.batch_solve(mats, bs, precision="mixed", max_iter=300)
+    print(json.dumps({"case": "batch", "kernel_ms": ks * 1e3, "iterations": [i.iterations for i in infos],
+                      "algo_bytes": sum(i.algo_bytes for i in infos)}))
 
 
 def measured_peak():
@@ -261,6 +301,9 @@ def main():
     args = parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.profile_case:
+        profile_case(args.profile_case)
+        return
     if args.impl == "reference":
         if rank == 0:
             run_reference(args)
@@ -268,10 +311,14 @@ def main():
     from graphitethree_gb300 import _lib, solver
     if not solver.device_available():
         raise SystemExit("bench.py: no CUDA device")
+    dist = None
     if world > 1:
-        # replicas only: each rank serves its own copy of the stream on its GPU
+        # replicas only: each rank serves its own seeded stream sample on its
+        # GPU; no data-path collective, only a barrier and max-over-ranks timing
         import torch
+        import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
     L = _lib.load()
     peak, peak_src = measured_peak()
     budget = args.budget_gb * 1e9
@@ -281,6 +328,8 @@ def main():
 
     for _ in range(args.warmup):
         serve(objs, reqs, "mixed", "batched", args.eps, budget)
+    if dist is not None:
+        dist.barrier()
     clocks = ClockSampler()
     clocks.start()
     launches0 = L.nlgb_kernel_launches()
@@ -295,8 +344,15 @@ def main():
 
     kern = [s["kernel_s"] for s, _ in steps]
     walls = [s["wall_s"] for s, _ in steps]
-    value = R / statistics.median(kern)
-    e2e = R / statistics.median(walls)
+    k_med, w_med = statistics.median(kern), statistics.median(walls)
+    if dist is not None:
+        import torch
+        t = torch.tensor([k_med, w_med, t_wall], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        k_med, w_med, t_wall = (float(v) for v in t.tolist())
+        dist.barrier()
+    value = R * world / k_med
+    e2e = R * world / w_med
     lat = [l for _, res in steps for _, l in res]
     p50 = float(np.percentile(lat, 50))
     p99 = float(np.percentile(lat, 99))

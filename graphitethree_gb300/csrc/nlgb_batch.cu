@@ -39,8 +39,9 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
 constexpr unsigned long long kBarrierTimeoutNs = 4000000000ULL;   // 4 s
 
 // Team barrier.  k == 1: a CTA barrier.  Returns false (in every thread) if
-// the wait timed out or another CTA already flagged an error.
-__device__ bool team_sync(TeamBar* bar, int k, int* err) {
+// the wait timed out or another CTA already flagged an error.  r: rank of
+// this CTA in the team.
+__device__ bool team_sync(TeamBar* bar, int k, int r, int* err) {
   if (k == 1) {
     __syncthreads();
     return true;
@@ -51,12 +52,21 @@ __device__ bool team_sync(TeamBar* bar, int k, int* err) {
     ok = 1;
     const unsigned int gen = *((volatile unsigned int*)&bar->gen);
     __threadfence();
-    const unsigned int arrived = atomicAdd(&bar->count, 1u);
-    if (arrived == (unsigned int)k - 1u) {
-      bar->count = 0u;
+    const int g = r / kBarGroup;
+    const int n_groups = (k + kBarGroup - 1) / kBarGroup;
+    const unsigned int g_size = (unsigned int)min(kBarGroup, k - g * kBarGroup);
+    bool last = false;
+    if (atomicAdd(&bar->grp[g], 1u) == g_size - 1u) {
+      bar->grp[g] = 0u;
       __threadfence();
-      atomicAdd(&bar->gen, 1u);
-    } else {
+      if (atomicAdd(&bar->top, 1u) == (unsigned int)n_groups - 1u) {
+        bar->top = 0u;
+        __threadfence();
+        atomicAdd(&bar->gen, 1u);
+        last = true;
+      }
+    }
+    if (!last) {
       const unsigned long long t0 = globaltimer_ns();
       while (*((volatile unsigned int*)&bar->gen) == gen) {
         if (*((volatile int*)err) != 0) { ok = 0; break; }
@@ -118,7 +128,7 @@ __device__ void run_system_once(const SysView& s, SysState* st, int r, int k, Te
         NLGB_TPR_SWITCH(tile_residual<T, true>(s, t, v));
         put_parts(s, t, kSlotInit, v, 3);
       }
-      if (!team_sync(bar, k, err)) { NLGB_SCALAR(st->status = ST_DEVICE_ERR; st->stage = 3); return; }
+      if (!team_sync(bar, k, r, err)) { NLGB_SCALAR(st->status = ST_DEVICE_ERR; st->stage = 3); return; }
       double o[3];
       get_sums<3>(s, kSlotInit, o);
       NLGB_SCALAR(scalar_after_init(st, o[0], o[1], o[2]); st->stage = st->status == ST_RUNNING ? 1 : 2);
@@ -129,7 +139,7 @@ __device__ void run_system_once(const SysView& s, SysState* st, int r, int k, Te
         NLGB_TPR_SWITCH(tile_mx_outer<T, true>(s, t, v));
         put_parts(s, t, kSlotInit, v, 4);
       }
-      if (!team_sync(bar, k, err)) { NLGB_SCALAR(st->status = ST_DEVICE_ERR; st->stage = 3); return; }
+      if (!team_sync(bar, k, r, err)) { NLGB_SCALAR(st->status = ST_DEVICE_ERR; st->stage = 3); return; }
       double o[4];
       get_sums<4>(s, kSlotInit, o);
       NLGB_SCALAR(st->mode = 0; scalar_after_outer(st, o[0], o[1], o[2], o[3]);
@@ -144,7 +154,7 @@ __device__ void run_system_once(const SysView& s, SysState* st, int r, int k, Te
         NLGB_TPR_SWITCH(v[0] = tile_spmv_pq<T, true>(s, t));
         put_parts(s, t, kSlotPQ, v, 1);
       }
-      if (!team_sync(bar, k, err)) break;
+      if (!team_sync(bar, k, r, err)) break;
       {
         double o[1];
         get_sums<1>(s, kSlotPQ, o);
@@ -157,7 +167,7 @@ __device__ void run_system_once(const SysView& s, SysState* st, int r, int k, Te
         tile_update_xr(s, t, alpha, v);
         put_parts(s, t, kSlotXR, v, 2);
       }
-      if (!team_sync(bar, k, err)) break;
+      if (!team_sync(bar, k, r, err)) break;
       {
         double o[2];
         get_sums<2>(s, kSlotXR, o);
@@ -167,21 +177,21 @@ __device__ void run_system_once(const SysView& s, SysState* st, int r, int k, Te
       if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
       const double beta = st->beta;
       for (int t = r; t < s.n_tiles; t += k) tile_update_p(s, t, beta);
-      if (!team_sync(bar, k, err)) break;
+      if (!team_sync(bar, k, r, err)) break;
     } else {
       // FP32 PCG iteration with FP64 reliable updates; same phase order as
       // the graph solver: p update, SpMV + p.q, c/r update, [update].
       {
         const double beta = st->beta;
         for (int t = r; t < s.n_tiles; t += k) tile_mx_update_p(s, t, beta);
-        if (!team_sync(bar, k, err)) break;
+        if (!team_sync(bar, k, r, err)) break;
       }
       for (int t = r; t < s.n_tiles; t += k) {
         double v[1];
         NLGB_TPR_SWITCH(v[0] = tile_mx_spmv_pq<T, true>(s, t));
         put_parts(s, t, kSlotPQ, v, 1);
       }
-      if (!team_sync(bar, k, err)) break;
+      if (!team_sync(bar, k, r, err)) break;
       {
         double o[1];
         get_sums<1>(s, kSlotPQ, o);
@@ -194,7 +204,7 @@ __device__ void run_system_once(const SysView& s, SysState* st, int r, int k, Te
         tile_mx_update_cr(s, t, alpha, v);
         put_parts(s, t, kSlotXR, v, 2);
       }
-      if (!team_sync(bar, k, err)) break;
+      if (!team_sync(bar, k, r, err)) break;
       {
         double o[2];
         get_sums<2>(s, kSlotXR, o);
@@ -205,13 +215,13 @@ __device__ void run_system_once(const SysView& s, SysState* st, int r, int k, Te
       if (st->mode == 0) {
         // reliable update: x += c, r = b - A x in FP64, FP32 residual replaced
         for (int t = r; t < s.n_tiles; t += k) tile_mx_apply(s, t);
-        if (!team_sync(bar, k, err)) break;
+        if (!team_sync(bar, k, r, err)) break;
         for (int t = r; t < s.n_tiles; t += k) {
           double v[4];
           NLGB_TPR_SWITCH(tile_mx_outer<T, true>(s, t, v));
           put_parts(s, t, kSlotInit, v, 4);
         }
-        if (!team_sync(bar, k, err)) break;
+        if (!team_sync(bar, k, r, err)) break;
         double o[4];
         get_sums<4>(s, kSlotInit, o);
         NLGB_SCALAR(scalar_after_outer(st, o[0], o[1], o[2], o[3]);
@@ -241,7 +251,7 @@ __device__ void run_system_once(const SysView& s, SysState* st, int r, int k, Te
       }
       put_parts(s, t, kSlotFinal, v, 1);
     }
-    if (!team_sync(bar, k, err)) { NLGB_SCALAR(st->status = ST_DEVICE_ERR; st->stage = 3); return; }
+    if (!team_sync(bar, k, r, err)) { NLGB_SCALAR(st->status = ST_DEVICE_ERR; st->stage = 3); return; }
     double o[1];
     get_sums<1>(s, kSlotFinal, o);
     NLGB_SCALAR(st->rr_true = o[0]; st->stage = 3);
@@ -369,7 +379,7 @@ void BatchRunner::plan(const std::vector<SysView>& views, const std::vector<long
       const int i = large[t];
       long long want = (long long)((double)avail * (double)std::max(1LL, work[i]) / (double)total);
       want = std::min<long long>(want, std::max(1, views[i].n_tiles / 2));
-      kk[t] = (int)std::max(2LL, want);
+      kk[t] = (int)std::min<long long>(kBarGroup * kBarMaxGroups, std::max(2LL, want));
       used += kk[t];
     }
     // Too many CTAs requested (minimum of 2 each): trim the largest teams,

@@ -12,9 +12,15 @@ namespace nlgb {
 // are popped from the queue by single CTAs.
 constexpr int kLargeTiles = 16;
 
+// Two-level team barrier: CTAs arrive on the counter of their group of 32,
+// the last of each group on the top counter, the last overall advances gen.
+// At most 32 atomics in a row on one address instead of one per CTA.
+constexpr int kBarGroup = 32;
+constexpr int kBarMaxGroups = 64;   // teams of up to 2048 CTAs
 struct TeamBar {
-  unsigned int count;
   unsigned int gen;
+  unsigned int top;
+  unsigned int grp[kBarMaxGroups];
 };
 
 struct TeamDesc {

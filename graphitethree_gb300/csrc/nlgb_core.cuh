@@ -150,6 +150,9 @@ __device__ __forceinline__ void canon_reduce(const double* part, int n_tiles,
                                              const int (&comp)[K], double (&out)[K]) {
 #pragma unroll
   for (int k = 0; k < K; ++k) out[k] = 0.0;
+  // unrolled so the loads of one thread are in flight together (the sum
+  // order stays tile t, t+256, t+512, ...)
+#pragma unroll 8
   for (int t = threadIdx.x; t < n_tiles; t += kCTA) {
 #pragma unroll
     for (int k = 0; k < K; ++k) out[k] += __ldcg(part + (size_t)t * kParts + comp[k]);
@@ -189,9 +192,11 @@ __device__ __forceinline__ A row_dot(const int* __restrict__ rp, const int* __re
 }
 
 // Rows [lo, hi) of a tile with T threads per row, one pass of kCTA/T rows at
-// a time; epi(row, sum) is called by the row's lane 0.  (Interleaving two
-// rows per sub-warp was measured slower on GB300: 2.96 vs 5.25 TB/s for the
-// 7-nonzero Laplacian SpMV.)
+// a time; epi(row, sum) is called by the row's lane 0.  Measured on GB300 and
+// not kept: two rows per sub-warp in flight (2.96 vs 5.25 TB/s on the
+// 7-nonzero Laplacian SpMV) and a "stream" layout staging each tile's
+// nonzeros in shared memory (3.3 vs 5.2 TB/s there, 2.6 vs 4.4 on the
+// 14-nonzero LSCM normal matrix).
 template <int T, typename VT, typename XT, typename A, bool kCoh, typename Epi>
 __device__ __forceinline__ void tile_rows_dot(const int* __restrict__ rp, const int* __restrict__ ci,
                                               const VT* __restrict__ va, const XT* __restrict__ x,
@@ -385,7 +390,7 @@ __device__ double tile_mx_spmv_pq(const SysView& s, int tile) {
   tile_rows_dot<T, float, float, float, kCoh>(s.rp, s.ci, s.va32, s.p32, lo, hi,
     [&](int row, float qv) {
       s.q32[row] = qv;
-      acc[0] = fma(double(__ldcg(s.p32 + row)), double(qv), acc[0]);
+      acc[0] += double(__ldcg(s.p32 + row) * qv);   // FP32 product, FP64 accumulation
     });
   block_sum<1>(acc);
   return acc[0];
@@ -397,12 +402,18 @@ __device__ __forceinline__ void tile_mx_update_cr(const SysView& s, int tile, do
                                                   double (&out)[2]) {
   const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
   const float a = float(alpha);
-  double rz = 0.0, rr = 0.0;
+  // A thread owns at most a row pair of the tile (tiles are <= 2 * kCTA
+  // rows): its products are summed in FP32 (at most two terms, error of the
+  // order of the FP32 storage of r and z themselves), converted once, and
+  // everything across threads, tiles and the vector is accumulated in FP64.
+  // This keeps the GB300's small FP64 pipe (1/56 of FP32) off the hot loop.
+  float rz32 = 0.f, rr32 = 0.f;
   float2* c2 = reinterpret_cast<float2*>(s.c32);
   float2* r2 = reinterpret_cast<float2*>(s.r32);
   const float2* p2 = reinterpret_cast<const float2*>(s.p32);
   const float2* q2 = reinterpret_cast<const float2*>(s.q32);
   const float2* d2 = reinterpret_cast<const float2*>(s.dinv32);
+  double rz = 0.0, rr = 0.0;
   pair_loop(lo, hi,
     [&](int i2) {
       float2 cv = __ldcg(c2 + i2), rv = __ldcg(r2 + i2);
@@ -411,16 +422,18 @@ __device__ __forceinline__ void tile_mx_update_cr(const SysView& s, int tile, do
       rv.x = fmaf(-a, qv.x, rv.x); rv.y = fmaf(-a, qv.y, rv.y);
       c2[i2] = cv; r2[i2] = rv;
       const float zx = dv.x * rv.x, zy = dv.y * rv.y;
-      rz = fma(double(zx), double(rv.x), rz); rz = fma(double(zy), double(rv.y), rz);
-      rr = fma(double(rv.x), double(rv.x), rr); rr = fma(double(rv.y), double(rv.y), rr);
+      rz32 = fmaf(zy, rv.y, zx * rv.x);
+      rr32 = fmaf(rv.y, rv.y, rv.x * rv.x);
+      rz += double(rz32);
+      rr += double(rr32);
     },
     [&](int i) {
       s.c32[i] = fmaf(a, __ldcg(s.p32 + i), __ldcg(s.c32 + i));
       const float ri = fmaf(-a, __ldcg(s.q32 + i), __ldcg(s.r32 + i));
       s.r32[i] = ri;
       const float zi = s.dinv32[i] * ri;
-      rz = fma(double(zi), double(ri), rz);
-      rr = fma(double(ri), double(ri), rr);
+      rz += double(zi * ri);
+      rr += double(ri * ri);
     });
   out[0] = rz; out[1] = rr;
   block_sum<2>(out);

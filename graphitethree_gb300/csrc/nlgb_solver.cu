@@ -72,12 +72,44 @@ __global__ void __launch_bounds__(kCTA) k_spmv_pq(SysView s) {
   }
 }
 
+// Vector phases: each CTA handles kVecTiles consecutive tiles (the partial
+// of every tile is still computed and stored on its own, so the canonical
+// reduction is unchanged); fewer, fuller CTAs than one per 256-row tile.
+constexpr int kVecTiles = 4;
+__device__ __forceinline__ int vec_t0() { return blockIdx.x * kVecTiles; }
+__device__ __forceinline__ int vec_t1(const SysView& s) { return min(s.n_tiles, (int)(blockIdx.x + 1) * kVecTiles); }
+
+template <int K>
+__device__ __forceinline__ void store_parts(const SysView& s, int tile, const double (&v)[K], int slot) {
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) __stcg(s.part + (size_t)tile * kParts + slot + k, v[k]);
+  }
+}
+
+// Last-CTA election over the whole grid (partials already stored).
+__device__ __forceinline__ bool elect_last(unsigned int* counter) {
+  __shared__ int am_last;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned int prev = atomicAdd(counter, 1u);
+    am_last = (prev == gridDim.x - 1u);
+    if (am_last) *counter = 0u;
+  }
+  __syncthreads();
+  if (am_last) __threadfence();
+  return am_last != 0;
+}
+
 __global__ void __launch_bounds__(kCTA) k_update_xr(SysView s) {
   if (ld_status(s.st) != ST_RUNNING) return;
   const double alpha = __ldcg(&s.st->alpha);
-  double v[2];
-  tile_update_xr(s, blockIdx.x, alpha, v);
-  if (publish_elect<2>(s, blockIdx.x, v, kSlotXR, &s.st->cnt[2])) {
+  for (int t = vec_t0(), t1 = vec_t1(s); t < t1; ++t) {
+    double v[2];
+    tile_update_xr(s, t, alpha, v);
+    store_parts<2>(s, t, v, kSlotXR);
+  }
+  if (elect_last(&s.st->cnt[2])) {
     const int comp[2] = {kSlotXR, kSlotXR + 1};
     double o[2];
     canon_reduce<2>(s.part, s.n_tiles, comp, o);
@@ -87,7 +119,8 @@ __global__ void __launch_bounds__(kCTA) k_update_xr(SysView s) {
 
 __global__ void __launch_bounds__(kCTA) k_update_p(SysView s) {
   if (ld_status(s.st) != ST_RUNNING) return;
-  tile_update_p(s, blockIdx.x, __ldcg(&s.st->beta));
+  const double beta = __ldcg(&s.st->beta);
+  for (int t = vec_t0(), t1 = vec_t1(s); t < t1; ++t) tile_update_p(s, t, beta);
 }
 
 // Termination guard of a while-node body (single thread).
@@ -130,7 +163,7 @@ __global__ void __launch_bounds__(kCTA) k_final(SysView s) {
 // Reliable update, part 1: x += c, c = 0 (only when an update is due).
 __global__ void __launch_bounds__(kCTA) k_mx_apply(SysView s) {
   if (ld_status(s.st) != ST_RUNNING || ld_mode(s.st) != 0) return;
-  tile_mx_apply(s, blockIdx.x);
+  for (int t = vec_t0(), t1 = vec_t1(s); t < t1; ++t) tile_mx_apply(s, t);
 }
 
 // Reliable update, part 2: FP64 true residual, FP32 residual replaced.
@@ -164,9 +197,12 @@ __global__ void __launch_bounds__(kCTA) k_mx_spmv_pq(SysView s) {
 __global__ void __launch_bounds__(kCTA) k_mx_update_cr(SysView s, cudaGraphConditionalHandle h_upd) {
   if (ld_status(s.st) != ST_RUNNING || ld_mode(s.st) != 1) return;
   const double alpha = __ldcg(&s.st->alpha);
-  double v[2];
-  tile_mx_update_cr(s, blockIdx.x, alpha, v);
-  if (publish_elect<2>(s, blockIdx.x, v, kSlotXR, &s.st->cnt[2])) {
+  for (int t = vec_t0(), t1 = vec_t1(s); t < t1; ++t) {
+    double v[2];
+    tile_mx_update_cr(s, t, alpha, v);
+    store_parts<2>(s, t, v, kSlotXR);
+  }
+  if (elect_last(&s.st->cnt[2])) {
     const int comp[2] = {kSlotXR, kSlotXR + 1};
     double o[2];
     canon_reduce<2>(s.part, s.n_tiles, comp, o);
@@ -180,7 +216,8 @@ __global__ void __launch_bounds__(kCTA) k_mx_update_cr(SysView s, cudaGraphCondi
 
 __global__ void __launch_bounds__(kCTA) k_mx_update_p(SysView s) {
   if (ld_status(s.st) != ST_RUNNING || ld_mode(s.st) != 1) return;
-  tile_mx_update_p(s, blockIdx.x, __ldcg(&s.st->beta));
+  const double beta = __ldcg(&s.st->beta);
+  for (int t = vec_t0(), t1 = vec_t1(s); t < t1; ++t) tile_mx_update_p(s, t, beta);
 }
 
 // ---------------------------------------------------------------------------
@@ -262,9 +299,13 @@ TuneChoice autotune(int n, long long nnz, int max_row, const int* hist33) {
   int tpr = 1;
   while (tpr < 32 && tpr * 8 < typical) tpr *= 2;
   // Tile rows: small tiles keep many CTAs in flight (measured on GB300: the
-  // 4.2M-row Laplacian SpMV runs at 5.25 TB/s with 256-row tiles vs 4.93
-  // with 4096; the L2-resident 131k-row LSCM matrix is fastest at 128).
-  const int tile = n >= (1 << 20) ? 256 : 128;
+  // 4.2M-row Laplacian SpMV runs at 5.25 TB/s with 256-row tiles vs 5.0 with
+  // 1024 and 4.93 with 4096; the L2-resident 131k-row LSCM matrix is fastest
+  // at 128), but every scalar is a reduction over all tiles, done by one CTA
+  // per phase: ~10k tiles cost more than the SpMV itself on a 1.3M-row
+  // system.  So at most ~2k tiles: 128 rows up to 256k rows, then n / 2048.
+  int tile = 128;
+  while (tile < 4096 && (long long)tile * 2048 < n) tile *= 2;
   (void)acc;
   return TuneChoice{tpr, tile};
 }
@@ -528,8 +569,9 @@ cudaError_t PcgSolver::build_plain_graph() {
   for (int u = 0; u < kUnrollPlain; ++u) {
     cudaGraphNode_t n1, n2, n3;
     NLGB_CUDA_TRY(add_kernel(body, &n1, prev, ks.spmv, n_tiles_, kCTA, a1));
-    NLGB_CUDA_TRY(add_kernel(body, &n2, n1, (const void*)k_update_xr, n_tiles_, kCTA, a1));
-    NLGB_CUDA_TRY(add_kernel(body, &n3, n2, (const void*)k_update_p, n_tiles_, kCTA, a1));
+    const int vg = (n_tiles_ + kVecTiles - 1) / kVecTiles;
+    NLGB_CUDA_TRY(add_kernel(body, &n2, n1, (const void*)k_update_xr, vg, kCTA, a1));
+    NLGB_CUDA_TRY(add_kernel(body, &n3, n2, (const void*)k_update_p, vg, kCTA, a1));
     prev = n3;
   }
   int need_mode = -1;
@@ -564,13 +606,14 @@ cudaError_t PcgSolver::build_mixed_graph() {
   for (int u = 0; u < kUnrollInner; ++u) {
     NLGB_CUDA_TRY(cudaGraphConditionalHandleCreate(&h_upd[u], body, 0u, cudaGraphCondAssignDefault));
     cudaGraphNode_t n1, n2, n3, n_if, n4, n5;
-    NLGB_CUDA_TRY(add_kernel(body, &n1, prev, (const void*)k_mx_update_p, n_tiles_, kCTA, a1));
+    const int vg = (n_tiles_ + kVecTiles - 1) / kVecTiles;
+    NLGB_CUDA_TRY(add_kernel(body, &n1, prev, (const void*)k_mx_update_p, vg, kCTA, a1));
     NLGB_CUDA_TRY(add_kernel(body, &n2, n1, ks.mx_spmv, n_tiles_, kCTA, a1));
     void* acr[] = {&v, &h_upd[u]};
-    NLGB_CUDA_TRY(add_kernel(body, &n3, n2, (const void*)k_mx_update_cr, n_tiles_, kCTA, acr));
+    NLGB_CUDA_TRY(add_kernel(body, &n3, n2, (const void*)k_mx_update_cr, vg, kCTA, acr));
     cudaGraph_t ubody;
     NLGB_CUDA_TRY(add_cond(body, &n_if, n3, h_upd[u], cudaGraphCondTypeIf, &ubody));
-    NLGB_CUDA_TRY(add_kernel(ubody, &n4, nullptr, (const void*)k_mx_apply, n_tiles_, kCTA, a1));
+    NLGB_CUDA_TRY(add_kernel(ubody, &n4, nullptr, (const void*)k_mx_apply, vg, kCTA, a1));
     NLGB_CUDA_TRY(add_kernel(ubody, &n5, n4, ks.mx_outer, n_tiles_, kCTA, a1));
     prev = n_if;
   }

@@ -132,15 +132,19 @@ def test_pcg_matches_oracle_and_direct(gpu_ok, oracle_mod, precision, case):
     else:
         rs = systems.voxel_rows(10, 9, 8, seed=6, locked_fraction=0.3)
     rp, ci, va, rhs = oracle_mod.assemble_rowstream(rs)
-    vals, info = solver.solve_opennl(rs, precision=precision, eps=1e-10)
+    # The LSCM normal equations are ill-conditioned (kappa ~ 1e5 here): two
+    # correct CG runs stopped at 1e-10 can differ from the direct solution by
+    # more than 1e-8, so that case is compared at relative residual 1e-12.
+    eps = 1e-12 if case.startswith("lscm") else 1e-10
+    vals, info = solver.solve_opennl(rs, precision=precision, eps=eps)
     assert info["ok"], info
     # mixed stops on the true FP64 residual, unless it fell back to FP64 PCG
     # (LSCM), which stops on the recursive residual like the plain solver
-    assert info["true_error"] <= 1.5e-10
+    assert info["true_error"] <= 1.5 * eps
     for s in range(rs.n_systems):
         x_gpu = vals[s][rs.locked == 0]
         x_dir = oracle_mod.direct_solve(rp, ci, va, rhs[s])
-        x_cpu, st, it, rr = oracle_mod.pcg(rp, ci, va, rhs[s], eps=1e-10)
+        x_cpu, st, it, rr = oracle_mod.pcg(rp, ci, va, rhs[s], eps=eps)
         assert st == 1
         assert rel(x_gpu, x_dir) <= 1e-8, (case, precision, rel(x_gpu, x_dir))
         assert rel(x_gpu, x_cpu) <= 1e-8, (case, precision, rel(x_gpu, x_cpu))
