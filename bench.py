@@ -68,7 +68,67 @@ def parse_args():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--profile-case", choices=["spmv", "batch", "plain", "mixed"], default=None,
                    help="run one small case for an ncu capture and exit")
+    p.add_argument("--workload", choices=["serving", "configs"], default="serving",
+                   help="configs: measure the other benchmark configurations and exit")
     return p.parse_args()
+
+
+def measure_configs():
+    """Configs 1, 2, 3 (reduced: 256 charts) and 5 -- plain FP64 vs mixed,
+    serial vs batched -- one JSON line (device times from CUDA events)."""
+    from graphitethree_gb300 import meshes, solver, systems
+    out = {"workload": "configs"}
+    t_start = time.perf_counter()
+
+    def progress(msg):
+        print(f"[configs {time.perf_counter() - t_start:8.1f}s] {msg}", file=sys.stderr, flush=True)
+
+    def rec(info, n, z):
+        return {"status": info.status, "iterations": info.iterations,
+                "reliable_updates": info.refinement_steps, "ms": info.seconds * 1e3,
+                "true_rel_residual": info.true_rel_residual,
+                "GBs": info.algo_bytes / info.seconds / 1e9 if info.seconds > 0 else 0.0,
+                "us_per_iteration": 1e6 * info.seconds / max(1, info.iterations), "n": n, "nnz": z}
+
+    progress("config 1")
+    M1, rhs1, asm = solver.assemble(systems.lscm_system(256, 256, seed=1))
+    out["config1_lscm256"] = {"assembly_s": asm,
+                              "plain": rec(M1.solve(rhs1[0])[1], M1.n, M1.nnz),
+                              "mixed": rec(M1.solve(rhs1[0], precision="mixed")[1], M1.n, M1.nnz)}
+    progress("config 2")
+    fs = systems.fairing_system(2048, 2048, seed=2)
+    A = solver.Matrix(fs.rp, fs.ci, fs.va)
+    out["config2_fairing2048"] = {f"rhs{k}_{p}": rec(A.solve(fs.rhs[k], precision=p)[1], A.n, A.nnz)
+                                  for k in range(3) for p in ("double", "mixed")}
+    A.close()
+    progress("config 3: assembling charts")
+    nx, ny = meshes.chart_sizes(256, seed=3, side_min=16, side_max=512)
+    mats, bs, unknowns = [], [], 0
+    for c in range(256):
+        M, rhs, _ = solver.assemble(systems.lscm_system(int(nx[c]), int(ny[c]), seed=1000 + c))
+        mats.append(M); bs.append(rhs[0]); unknowns += M.n
+    c3 = {"charts": 256, "unknowns": unknowns,
+          "sides": "long side log-uniform [16,512], aspect log-uniform [1,4]"}
+    for p in ("double", "mixed"):
+        progress(f"config 3: batched {p} ({unknowns} unknowns)")
+        xs, infos, ks = solver.batch_solve(mats, bs, precision=p)
+        progress(f"config 3: batched {p} kernel {ks:.3f}s, max iterations "
+                 f"{max(i.iterations for i in infos)}")
+        c3[f"batched_{p}_s"] = ks
+        c3[f"batched_{p}_converged"] = sum(i.status == "converged" for i in infos)
+    progress("config 3: serial plain")
+    serial = 0.0
+    for M, b in zip(mats, bs):
+        serial += M.solve(b)[1].seconds
+    c3["serial_plain_s"] = serial
+    out["config3_charts_reduced"] = c3
+    progress("config 5")
+    f5 = systems.fairing_system(1024, 1024, seed=5, lam=1e-4, n_rhs=1, stretch_bands=16, rhs_normal=True)
+    A5 = solver.Matrix(f5.rp, f5.ci, f5.va)
+    out["config5_stretched"] = {"plain_1e-12": rec(A5.solve(f5.rhs[0], eps=1e-12)[1], A5.n, A5.nnz),
+                                "mixed_1e-12": rec(A5.solve(f5.rhs[0], eps=1e-12, precision="mixed")[1],
+                                                   A5.n, A5.nnz)}
+    print(json.dumps(out))
 
 
 def profile_case(which):
@@ -304,6 +364,9 @@ def main():
     if args.profile_case:
         profile_case(args.profile_case)
         return
+    if args.workload == "configs":
+        measure_configs()
+        return
     if args.impl == "reference":
         if rank == 0:
             run_reference(args)
@@ -346,10 +409,8 @@ def main():
     walls = [s["wall_s"] for s, _ in steps]
     k_med, w_med = statistics.median(kern), statistics.median(walls)
     if dist is not None:
-        import torch
-        t = torch.tensor([k_med, w_med, t_wall], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        k_med, w_med, t_wall = (float(v) for v in t.tolist())
+        from graphitethree_gb300.replicas import max_over_ranks
+        k_med, w_med, t_wall = max_over_ranks([k_med, w_med, t_wall], dist, device="cuda")
         dist.barrier()
     value = R * world / k_med
     e2e = R * world / w_med

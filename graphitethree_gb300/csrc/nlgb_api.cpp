@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -307,7 +308,9 @@ int nlgb_batch_solve(int n_sys, const nlgb_matrix* A, const double* const* b, do
         break;
       }
       views[i] = slots[i].view;
-      work[i] = M.nnz + 8LL * M.n;
+      // bytes per iteration x an iteration-count proxy: Jacobi-CG on a 2D
+      // mesh operator needs O(sqrt(kappa)) = O(sqrt(n)) iterations
+      work[i] = (long long)((double)(M.nnz + 8LL * M.n) * std::sqrt((double)std::max(1, M.n)));
     }
     BatchLaunchStats st;
     if (rc == NLGB_OK && runner.run(views, work, 0, &st) != cudaSuccess) rc = NLGB_E_DEVICE;

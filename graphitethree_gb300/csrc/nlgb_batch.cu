@@ -7,8 +7,10 @@
 // runs them one at a time is launch- and latency-bound on the small charts.
 //
 // Layout of one launch (grid = every co-resident CTA, cooperative launch):
-//   * large systems get a static "team" of k CTAs; the team synchronises its
-//     phases with a global-memory barrier (bounded spin, then an error flag);
+//   * large systems are run by "teams" of k CTAs; a team synchronises its
+//     phases with a global-memory barrier (bounded spin, then an error flag),
+//     runs the system it was planned for, then draws further large systems
+//     from a shared team queue (largest first) until it is empty;
 //   * every other CTA is a queue worker: it pops the next small system from
 //     an atomic queue and runs it alone (phases separated by __syncthreads).
 // Each system's iteration is the same sequence of tile procedures and scalar
@@ -23,6 +25,7 @@
 #include "nlgb_internal.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <numeric>
 
@@ -267,7 +270,9 @@ __device__ void run_system(const SysView& s, SysState* st, int r, int k, TeamBar
     run_system_once(s, st, r, k, bar, err, budget);
 }
 
-__global__ void __launch_bounds__(kCTA) k_batch(BatchArgs a) {
+// Four CTAs per SM (64 registers): stating the bound lets ptxas plan for it,
+// with far fewer spills than its own choice of the same 64 registers.
+__global__ void __launch_bounds__(kCTA, 4) k_batch(BatchArgs a) {
   __shared__ SysView sv;
   __shared__ SysState sst;
   __shared__ int pick;
@@ -291,9 +296,26 @@ __global__ void __launch_bounds__(kCTA) k_batch(BatchArgs a) {
     const int team = a.cta_team[cta];
     const TeamDesc td = a.teams[team];
     const int r = cta - td.cta_begin;
+    TeamBar* bar = a.bars + team;
     for (int j = td.sys_begin; j < td.sys_end; ++j) {
       load(a.team_sys[j]);
-      if (sst.stage != 3) run_system(sv, &sst, r, td.k, a.bars + team, a.err, a.budget);
+      if (sst.stage != 3) run_system(sv, &sst, r, td.k, bar, a.err, a.budget);
+      store(r == 0);
+    }
+    // Then the shared team queue: rank 0 draws the next system and publishes
+    // it through the team barrier; a second barrier keeps the next draw from
+    // overwriting `pick` before every CTA of the team has read it.
+    while (a.n_tqueue > 0) {
+      if (r == 0 && threadIdx.x == 0)
+        *((volatile int*)&bar->pick) = (int)atomicAdd(a.tqueue_head, 1u);
+      if (!team_sync(bar, td.k, r, a.err)) break;
+      if (threadIdx.x == 0) pick = *((volatile int*)&bar->pick);
+      __syncthreads();
+      const int q = pick;
+      if (!team_sync(bar, td.k, r, a.err)) break;
+      if (q >= a.n_tqueue) break;
+      load(a.tqueue[q]);
+      if (sst.stage != 3) run_system(sv, &sst, r, td.k, bar, a.err, a.budget);
       store(r == 0);
     }
   } else {
@@ -322,7 +344,7 @@ __global__ void k_gather_states(const SysView* views, int n, SysState* out) {
 // ---------------------------------------------------------------------------
 BatchRunner::~BatchRunner() {
   cudaFree(d_views_); cudaFree(d_teams_); cudaFree(d_cta_team_); cudaFree(d_team_sys_);
-  cudaFree(d_queue_); cudaFree(d_bars_); cudaFree(d_ctl_);
+  cudaFree(d_queue_); cudaFree(d_tqueue_); cudaFree(d_bars_); cudaFree(d_ctl_);
   if (h_err_) cudaFreeHost(h_err_);
   cudaFree(d_states_);
   if (ev0_) cudaEventDestroy(ev0_);
@@ -338,7 +360,7 @@ cudaError_t BatchRunner::init(cudaStream_t s) {
   NLGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, kCTA, 0));
   per_sm_ = std::max(1, per_sm);
   grid_ = n_sm_ * per_sm_;
-  NLGB_CUDA_TRY(cudaMalloc(&d_ctl_, 2 * sizeof(int)));
+  NLGB_CUDA_TRY(cudaMalloc(&d_ctl_, 3 * sizeof(int)));
   NLGB_CUDA_TRY(cudaMallocHost(&h_err_, sizeof(int)));
   *h_err_ = 0;
   NLGB_CUDA_TRY(cudaEventCreate(&ev0_));
@@ -355,56 +377,55 @@ static cudaError_t ensure(T*& p, size_t& cap, size_t n) {
   return cudaMalloc(&p, cap * sizeof(T));
 }
 
-void BatchRunner::plan(const std::vector<SysView>& views, const std::vector<long long>& work,
-                       int reserve_queue_ctas) {
-  // Large systems: more tiles than a CTA should carry per phase.
-  teams_.clear(); cta_team_.clear(); team_sys_.clear(); queue_.clear();
+// Schedule for one launch.  Small systems (fewer than kLargeTiles tiles) go to
+// the single-CTA queue, whose workers get a share of the grid proportional to
+// the small systems' work (at least one, at most one per system).  The large
+// ones, largest first, get teams sized by their share of the remaining CTAs
+// (at least 2, at most one CTA per 2 tiles) until the CTAs run out; the rest
+// wait in the team queue, from which every team draws (largest first) once
+// its own system is done -- list scheduling, so one mis-estimated system
+// does not leave the other teams idle.
+void BatchRunner::plan(const std::vector<SysView>& views, const std::vector<long long>& work) {
+  teams_.clear(); cta_team_.clear(); team_sys_.clear(); queue_.clear(); tqueue_.clear();
   const int n = (int)views.size();
   std::vector<int> order(n);
   std::iota(order.begin(), order.end(), 0);
-  std::sort(order.begin(), order.end(), [&](int a, int b) { return work[a] > work[b]; });
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work[a] > work[b]; });
   std::vector<int> large;
+  double w_large = 0.0, w_small = 0.0;
   for (int i : order) {
-    if (views[i].n_tiles >= kLargeTiles) large.push_back(i);
-    else queue_.push_back(i);
+    const double w = (double)std::max(1LL, work[i]);
+    if (views[i].n_tiles >= kLargeTiles) { large.push_back(i); w_large += w; }
+    else { queue_.push_back(i); w_small += w; }
   }
-  const int avail = std::max(0, grid_ - (queue_.empty() ? 0 : std::max(reserve_queue_ctas, 1)));
-  if (!large.empty() && avail > 0) {
-    // CTAs proportional to work, at least 2 and at most one per 2 tiles.
-    long long total = 0;
-    for (int i : large) total += std::max(1LL, work[i]);
-    std::vector<int> kk(large.size());
-    int used = 0;
-    for (size_t t = 0; t < large.size(); ++t) {
-      const int i = large[t];
-      long long want = (long long)((double)avail * (double)std::max(1LL, work[i]) / (double)total);
-      want = std::min<long long>(want, std::max(1, views[i].n_tiles / 2));
-      kk[t] = (int)std::min<long long>(kBarGroup * kBarMaxGroups, std::max(2LL, want));
-      used += kk[t];
-    }
-    // Too many CTAs requested (minimum of 2 each): trim the largest teams,
-    // then send what still does not fit to the queue.
-    while (used > avail) {
-      size_t big = std::max_element(kk.begin(), kk.end()) - kk.begin();
-      if (kk[big] <= 2) break;
-      kk[big] -= 1;
-      used -= 1;
-    }
-    int cta = 0;
-    for (size_t t = 0; t < large.size(); ++t) {
-      if (cta + kk[t] > avail) { queue_.push_back(large[t]); continue; }
-      TeamDesc td;
-      td.cta_begin = cta;
-      td.k = kk[t];
-      td.sys_begin = (int)team_sys_.size();
-      team_sys_.push_back(large[t]);
-      td.sys_end = (int)team_sys_.size();
-      for (int c = 0; c < td.k; ++c) cta_team_.push_back((int)teams_.size());
-      teams_.push_back(td);
-      cta += td.k;
-    }
-  } else {
-    for (int i : large) queue_.push_back(i);
+  if (large.empty()) return;
+  int reserve = 0;
+  if (!queue_.empty()) {
+    reserve = (int)std::ceil((double)grid_ * w_small / (w_small + w_large));
+    reserve = std::max(1, std::min(reserve, std::min((int)queue_.size(), grid_ / 2)));
+  }
+  const int avail = grid_ - reserve;
+  if (avail < 2) {   // no room for a team: everything goes to the queue workers
+    queue_.insert(queue_.begin(), large.begin(), large.end());
+    return;
+  }
+  const double per_cta = w_large / (double)avail;
+  int cta = 0;
+  for (int i : large) {
+    const double w = (double)std::max(1LL, work[i]);
+    const int cap = std::min(kBarGroup * kBarMaxGroups, std::max(2, views[i].n_tiles / 2));
+    int k = (int)std::min<double>((double)cap, std::max(2.0, std::floor(w / per_cta)));
+    if (cta + k > avail) k = avail - cta;     // the last team takes what is left
+    if (k < 2) { tqueue_.push_back(i); continue; }
+    TeamDesc td;
+    td.cta_begin = cta;
+    td.k = k;
+    td.sys_begin = (int)team_sys_.size();
+    team_sys_.push_back(i);
+    td.sys_end = (int)team_sys_.size();
+    for (int c = 0; c < k; ++c) cta_team_.push_back((int)teams_.size());
+    teams_.push_back(td);
+    cta += k;
   }
 }
 
@@ -418,12 +439,13 @@ cudaError_t BatchRunner::launch(const std::vector<SysView>& views, const std::ve
                                 long long budget) {
   pending_ = false;
   if (views.empty()) return cudaSuccess;
-  plan(views, work, std::max(n_sm_, (int)std::min<size_t>(views.size(), (size_t)grid_ / 2)));
+  plan(views, work);
   NLGB_CUDA_TRY(ensure(d_views_, cap_views_, views.size()));
   NLGB_CUDA_TRY(ensure(d_teams_, cap_teams_, teams_.size()));
   NLGB_CUDA_TRY(ensure(d_cta_team_, cap_cta_team_, cta_team_.size()));
   NLGB_CUDA_TRY(ensure(d_team_sys_, cap_team_sys_, team_sys_.size()));
   NLGB_CUDA_TRY(ensure(d_queue_, cap_queue_, queue_.size()));
+  NLGB_CUDA_TRY(ensure(d_tqueue_, cap_tqueue_, tqueue_.size()));
   NLGB_CUDA_TRY(ensure(d_bars_, cap_bars_, teams_.size()));
   cudaStream_t s = stream_;
   NLGB_CUDA_TRY(cudaMemcpyAsync(d_views_, views.data(), views.size() * sizeof(SysView), cudaMemcpyHostToDevice, s));
@@ -435,7 +457,9 @@ cudaError_t BatchRunner::launch(const std::vector<SysView>& views, const std::ve
   }
   if (!queue_.empty())
     NLGB_CUDA_TRY(cudaMemcpyAsync(d_queue_, queue_.data(), queue_.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-  NLGB_CUDA_TRY(cudaMemsetAsync(d_ctl_, 0, 2 * sizeof(int), s));
+  if (!tqueue_.empty())
+    NLGB_CUDA_TRY(cudaMemcpyAsync(d_tqueue_, tqueue_.data(), tqueue_.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+  NLGB_CUDA_TRY(cudaMemsetAsync(d_ctl_, 0, 3 * sizeof(int), s));
   BatchArgs a;
   std::memset(&a, 0, sizeof(a));
   a.views = d_views_;
@@ -443,11 +467,14 @@ cudaError_t BatchRunner::launch(const std::vector<SysView>& views, const std::ve
   a.cta_team = d_cta_team_;
   a.team_sys = d_team_sys_;
   a.queue = d_queue_;
+  a.tqueue = d_tqueue_;
   a.bars = d_bars_;
   a.err = d_ctl_;
   a.queue_head = reinterpret_cast<unsigned int*>(d_ctl_ + 1);
+  a.tqueue_head = reinterpret_cast<unsigned int*>(d_ctl_ + 2);
   a.team_ctas = (int)cta_team_.size();
   a.n_queue = (int)queue_.size();
+  a.n_tqueue = teams_.empty() ? 0 : (int)tqueue_.size();
   a.budget = budget;
   // Grid: every team CTA plus queue workers, never more than can be resident.
   const int workers = queue_.empty() ? 0 : std::min(grid_ - a.team_ctas, (int)queue_.size());

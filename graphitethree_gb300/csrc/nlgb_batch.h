@@ -8,8 +8,8 @@
 
 namespace nlgb {
 
-// Systems with at least this many tiles get a multi-CTA team; smaller ones
-// are popped from the queue by single CTAs.
+// Systems with at least this many tiles are run by multi-CTA teams; smaller
+// ones are popped from the queue by single CTAs.
 constexpr int kLargeTiles = 16;
 
 // Two-level team barrier: CTAs arrive on the counter of their group of 32,
@@ -21,6 +21,7 @@ struct TeamBar {
   unsigned int gen;
   unsigned int top;
   unsigned int grp[kBarMaxGroups];
+  int pick;       // team-queue entry drawn by the team's rank 0
 };
 
 struct TeamDesc {
@@ -36,11 +37,14 @@ struct BatchArgs {
   const int* cta_team;       // team of each team CTA
   const int* team_sys;       // system indices handled by teams, grouped by team
   const int* queue;          // system indices handled by queue workers
+  const int* tqueue;         // large systems drawn by any free team, largest first
   TeamBar* bars;
   int* err;                  // nonzero: a barrier timed out
   unsigned int* queue_head;
+  unsigned int* tqueue_head;
   int team_ctas;
   int n_queue;
+  int n_tqueue;
   long long budget;          // iterations per system in this launch (<= 0: no limit)
 };
 
@@ -85,7 +89,8 @@ class BatchRunner {
   BatchRunner& operator=(const BatchRunner&) = delete;
 
   cudaError_t init(cudaStream_t s);
-  // work[i]: relative cost estimate of system i (rows x expected iterations).
+  // work[i]: relative cost estimate of system i (bytes per iteration x
+  // expected iterations).
   // run() = launch() + finish().  Between the two the host may queue other
   // work (uploads of new requests) on other streams.
   cudaError_t run(const std::vector<SysView>& views, const std::vector<long long>& work,
@@ -99,19 +104,19 @@ class BatchRunner {
   int max_grid() const { return grid_; }
 
  private:
-  void plan(const std::vector<SysView>& views, const std::vector<long long>& work,
-            int reserve_queue_ctas);
+  void plan(const std::vector<SysView>& views, const std::vector<long long>& work);
 
   cudaStream_t stream_ = nullptr;
   int n_sm_ = 0, per_sm_ = 0, grid_ = 0;
   std::vector<TeamDesc> teams_;
-  std::vector<int> cta_team_, team_sys_, queue_;
+  std::vector<int> cta_team_, team_sys_, queue_, tqueue_;
   SysView* d_views_ = nullptr;
   TeamDesc* d_teams_ = nullptr;
-  int *d_cta_team_ = nullptr, *d_team_sys_ = nullptr, *d_queue_ = nullptr, *d_ctl_ = nullptr;
+  int *d_cta_team_ = nullptr, *d_team_sys_ = nullptr, *d_queue_ = nullptr, *d_tqueue_ = nullptr;
+  int* d_ctl_ = nullptr;           // error flag, queue head, team-queue head
   TeamBar* d_bars_ = nullptr;
   size_t cap_views_ = 0, cap_teams_ = 0, cap_cta_team_ = 0, cap_team_sys_ = 0, cap_queue_ = 0,
-         cap_bars_ = 0;
+         cap_tqueue_ = 0, cap_bars_ = 0;
   cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
   int* h_err_ = nullptr;           // pinned
   SysState* d_states_ = nullptr;

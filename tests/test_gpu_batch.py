@@ -78,3 +78,24 @@ def test_batch_edge_cases(gpu_ok):
     assert infos[1].status == "max_iter" and infos[1].iterations == 5
     xs, infos, _ = solver.batch_solve([], [])
     assert xs == [] and infos == []
+
+
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+def test_team_queue_more_large_systems_than_teams(gpu_ok, precision):
+    """More multi-tile systems than the grid has two-CTA teams for: the ones
+    left over are drawn from the shared team queue by whichever team finishes
+    first.  Every system still converges, bit-identical to its own solve."""
+    mats, bs = [], []
+    for c in range(400):
+        nx = 48 + (c % 5) * 8
+        fs = systems.fairing_system(nx, 48, seed=500 + c, n_rhs=1)
+        assert fs.n >= 2048                      # at least 16 tiles of 128 rows
+        mats.append(solver.Matrix(fs.rp, fs.ci, fs.va))
+        bs.append(fs.rhs[0])
+    xs, infos, secs = solver.batch_solve(mats, bs, precision=precision)
+    assert all(i.status == "converged" for i in infos)
+    for c in (0, 1, 250, 399):
+        x1, i1 = mats[c].solve(bs[c], precision=precision)
+        assert i1.iterations == infos[c].iterations and np.array_equal(xs[c], x1)
+    for M in mats:
+        M.close()
