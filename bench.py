@@ -66,7 +66,8 @@ def parse_args():
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-spmv", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--profile-case", choices=["spmv", "batch", "plain", "mixed"], default=None,
+    p.add_argument("--profile-case", choices=["spmv", "batch", "batch_small", "plain", "mixed", "plain_lscm",
+                                              "mixed_lscm"], default=None,
                    help="run one small case for an ncu capture and exit")
     p.add_argument("--workload", choices=["serving", "configs"], default="serving",
                    help="configs: measure the other benchmark configurations and exit")
@@ -136,6 +137,10 @@ def profile_case(which):
     spmv:  3 FP64 SpMVs on the 2048^2 cotangent Laplacian (k_spmv);
     batch: one persistent-kernel launch over 8 mid-size systems, 300
            iterations each (k_batch);
+    plain_lscm / mixed_lscm: 40 iterations on the 1.3M-unknown LSCM normal
+           equations (808^2 grid), graph path;
+    batch_small: one 4,604-unknown LSCM system in the persistent kernel,
+           1000 iterations (k_batch, latency-bound);
     plain: 20 FP64 PCG iterations on the 2048^2 Laplacian (graph kernels);
     mixed: 20 FP32/FP64 iterations on the same system."""
     import ctypes
@@ -156,6 +161,23 @@ def profile_case(which):
         else:
             x, info = A.solve(fs.rhs[0], max_iter=20, precision="double" if which == "plain" else "mixed")
             print(json.dumps({"case": which, "iterations": info.iterations, "ms": info.seconds * 1e3}))
+        return
+    if which in ("plain_lscm", "mixed_lscm"):
+        # 40 iterations on the LSCM normal equations of an 808 x 808 grid
+        # (1,305,724 unknowns): graph-captured single-system PCG
+        M, rhs, _ = solver.assemble(systems.lscm_system(808, 808, seed=1))
+        x, info = M.solve(rhs[0], max_iter=40, eps=1e-30,
+                          precision="double" if which == "plain_lscm" else "mixed")
+        print(json.dumps({"case": which, "iterations": info.iterations, "ms": info.seconds * 1e3,
+                          "n": M.n, "nnz": M.nnz, "tile_rows": M.tile_rows, "tpr": M.threads_per_row}))
+        return
+    if which == "batch_small":
+        # one small LSCM system (4,604 unknowns, 35 tiles) in the persistent
+        # kernel: a latency-bound team of 35 CTAs, 1000 FP64 iterations
+        M, rhs, _ = solver.assemble(systems.lscm_system(48, 48, seed=1))
+        xs, infos, ks = solver.batch_solve([M], [rhs[0]], max_iter=1000, eps=1e-30)
+        print(json.dumps({"case": which, "kernel_ms": ks * 1e3, "iterations": infos[0].iterations,
+                          "us_per_iteration": 1e3 * ks * 1e3 / max(1, infos[0].iterations)}))
         return
     mats, bs = [], []
     for s, side in enumerate((180, 150, 120, 90)):

@@ -158,8 +158,8 @@ int nlgb_matrix_set_layout(nlgb_matrix A, int tpr, int tile_rows) {
   if (!A) return fail(NLGB_E_INVALID, "nlgb_matrix_set_layout: null matrix");
   if (tpr != 0 && tpr != 1 && tpr != 2 && tpr != 4 && tpr != 8 && tpr != 16 && tpr != 32)
     return fail(NLGB_E_INVALID, "threads_per_row must be 0 or a power of two <= 32");
-  if (tile_rows != 0 && (tile_rows < 64 || (tile_rows & (tile_rows - 1)) != 0 || tile_rows > (1 << 20)))
-    return fail(NLGB_E_INVALID, "tile_rows must be a power of two in [64, 2^20]");
+  if (tile_rows != 0 && (tile_rows < 64 || tile_rows % 64 != 0 || tile_rows > (1 << 20)))
+    return fail(NLGB_E_INVALID, "tile_rows must be a multiple of 64 in [64, 2^20]");
   if (tpr) A->A.tpr = tpr;
   if (tile_rows) A->A.tile_rows = tile_rows;
   A->bound = false;   // the solver's graphs embed the layout

@@ -41,9 +41,28 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
 
 constexpr unsigned long long kBarrierTimeoutNs = 4000000000ULL;   // 4 s
 
+// Barriers this CTA has completed in the current launch (set to 0 at kernel
+// start; every CTA of a team passes the same sequence of barriers).
+__shared__ unsigned long long s_bar_epoch;
+
+__device__ __forceinline__ unsigned long long atom_add_acq_rel(unsigned long long* p, unsigned long long v) {
+  unsigned long long old;
+  asm volatile("atom.acq_rel.gpu.global.add.u64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+  return old;
+}
+
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
 // Team barrier.  k == 1: a CTA barrier.  Returns false (in every thread) if
 // the wait timed out or another CTA already flagged an error.  r: rank of
-// this CTA in the team.
+// this CTA in the team.  The __syncthreads before the arrival orders the
+// CTA's writes before thread 0's release; thread 0's acquire and the
+// __syncthreads after the wait order the other CTAs' writes before this
+// CTA's next reads (which go through L2: __ldcg).
 __device__ bool team_sync(TeamBar* bar, int k, int r, int* err) {
   if (k == 1) {
     __syncthreads();
@@ -53,35 +72,35 @@ __device__ bool team_sync(TeamBar* bar, int k, int r, int* err) {
   __syncthreads();
   if (threadIdx.x == 0) {
     ok = 1;
-    const unsigned int gen = *((volatile unsigned int*)&bar->gen);
-    __threadfence();
-    const int g = r / kBarGroup;
-    const int n_groups = (k + kBarGroup - 1) / kBarGroup;
-    const unsigned int g_size = (unsigned int)min(kBarGroup, k - g * kBarGroup);
-    bool last = false;
-    if (atomicAdd(&bar->grp[g], 1u) == g_size - 1u) {
-      bar->grp[g] = 0u;
-      __threadfence();
-      if (atomicAdd(&bar->top, 1u) == (unsigned int)n_groups - 1u) {
-        bar->top = 0u;
-        __threadfence();
-        atomicAdd(&bar->gen, 1u);
-        last = true;
-      }
+    const unsigned long long e = s_bar_epoch + 1;
+    s_bar_epoch = e;
+    unsigned long long target;
+    if (k <= kBarFlat) {
+      atom_add_acq_rel(&bar->top.count, 1ULL);
+      target = e * (unsigned long long)k;
+    } else {
+      const int g = r / kBarGroup;
+      const int n_groups = (k + kBarGroup - 1) / kBarGroup;
+      const unsigned long long g_size = (unsigned long long)min(kBarGroup, k - g * kBarGroup);
+      if (atom_add_acq_rel(&bar->grp[g].count, 1ULL) + 1ULL == e * g_size)
+        atom_add_acq_rel(&bar->top.count, 1ULL);
+      target = e * (unsigned long long)n_groups;
     }
-    if (!last) {
+    if (ld_acquire(&bar->top.count) < target) {
       const unsigned long long t0 = globaltimer_ns();
-      while (*((volatile unsigned int*)&bar->gen) == gen) {
-        if (*((volatile int*)err) != 0) { ok = 0; break; }
-        if (globaltimer_ns() - t0 > kBarrierTimeoutNs) {
-          atomicExch(err, 1);
-          ok = 0;
-          break;
+      unsigned int spins = 0;
+      while (ld_acquire(&bar->top.count) < target) {
+        if ((++spins & 31u) == 0u) {
+          if (*((volatile int*)err) != 0) { ok = 0; break; }
+          if (globaltimer_ns() - t0 > kBarrierTimeoutNs) {
+            atomicExch(err, 1);
+            ok = 0;
+            break;
+          }
         }
-        __nanosleep(32);
+        __nanosleep(8);
       }
     }
-    __threadfence();
   }
   __syncthreads();
   return ok != 0;
@@ -277,6 +296,8 @@ __global__ void __launch_bounds__(kCTA, 4) k_batch(BatchArgs a) {
   __shared__ SysState sst;
   __shared__ int pick;
   const int cta = blockIdx.x;
+  if (threadIdx.x == 0) s_bar_epoch = 0ULL;
+  __syncthreads();
   auto load = [&](int sys) {
     if (threadIdx.x == 0) {
       sv = a.views[sys];
@@ -307,9 +328,9 @@ __global__ void __launch_bounds__(kCTA, 4) k_batch(BatchArgs a) {
     // overwriting `pick` before every CTA of the team has read it.
     while (a.n_tqueue > 0) {
       if (r == 0 && threadIdx.x == 0)
-        *((volatile int*)&bar->pick) = (int)atomicAdd(a.tqueue_head, 1u);
+        *((volatile unsigned long long*)&bar->pick.count) = atomicAdd(a.tqueue_head, 1u);
       if (!team_sync(bar, td.k, r, a.err)) break;
-      if (threadIdx.x == 0) pick = *((volatile int*)&bar->pick);
+      if (threadIdx.x == 0) pick = (int)*((volatile unsigned long long*)&bar->pick.count);
       __syncthreads();
       const int q = pick;
       if (!team_sync(bar, td.k, r, a.err)) break;

@@ -12,16 +12,23 @@ namespace nlgb {
 // ones are popped from the queue by single CTAs.
 constexpr int kLargeTiles = 16;
 
-// Two-level team barrier: CTAs arrive on the counter of their group of 32,
-// the last of each group on the top counter, the last overall advances gen.
-// At most 32 atomics in a row on one address instead of one per CTA.
+// Team barrier on monotonic 64-bit arrival counters (never reset within a
+// launch): barrier number e of a team is complete when its counter reaches
+// e x (arrivals per barrier).  Teams of up to kBarFlat CTAs arrive on one
+// counter; larger teams arrive on the counter of their group of kBarGroup,
+// and the last of each group on the top counter, so at most kBarGroup
+// atomics in a row hit one address.  Each counter has its own 128-byte line.
+constexpr int kBarFlat = 64;
 constexpr int kBarGroup = 32;
-constexpr int kBarMaxGroups = 64;   // teams of up to 2048 CTAs
+constexpr int kBarMaxGroups = 32;   // teams of up to 1024 CTAs
+struct __align__(128) BarLine {
+  unsigned long long count;
+  unsigned long long pad_[15];
+};
 struct TeamBar {
-  unsigned int gen;
-  unsigned int top;
-  unsigned int grp[kBarMaxGroups];
-  int pick;       // team-queue entry drawn by the team's rank 0
+  BarLine top;
+  BarLine grp[kBarMaxGroups];
+  BarLine pick;   // .count: team-queue entry drawn by the team's rank 0
 };
 
 struct TeamDesc {

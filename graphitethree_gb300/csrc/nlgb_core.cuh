@@ -86,10 +86,16 @@ inline __host__ __device__ double algo_bytes(long long n, long long z, const Sys
   return b;
 }
 
+// Tiles per CTA in the vector phases of the graph solver: tiles of fewer
+// than 512 rows are grouped so that a CTA covers about 512 rows.
+inline __host__ __device__ int vec_tiles_for(int tile_rows) {
+  return tile_rows >= 512 ? 1 : 512 / tile_rows;
+}
+
 // Everything a tile procedure needs about one system.
 struct SysView {
   int n;                 // rows (== columns)
-  int tile_rows;         // rows per tile (multiple of 512)
+  int tile_rows;         // rows per tile (even; the autotuner uses multiples of 128)
   int n_tiles;
   int tpr;               // threads per row used by the SpMV (1..32)
   const int* rp;         // CRS row pointers (n+1)

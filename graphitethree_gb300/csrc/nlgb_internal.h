@@ -8,6 +8,8 @@
 
 namespace nlgb {
 
+struct SysState;
+
 // Thread-local error text reported by nlGetErrorString()/nlgb_last_error().
 void set_error(const std::string& msg);
 const char* last_error();
@@ -99,6 +101,7 @@ class PcgSolver {
   cudaError_t alloc(bool mixed);
   cudaError_t run_graph(bool mixed, const SolveParams& prm, long long max_iter, long long done,
                         int outer, float* ms);
+  cudaError_t run_eager(bool mixed, SysState* h);
   cudaError_t build_plain_graph();
   cudaError_t build_mixed_graph();
   void release();

@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -72,12 +73,13 @@ __global__ void __launch_bounds__(kCTA) k_spmv_pq(SysView s) {
   }
 }
 
-// Vector phases: each CTA handles kVecTiles consecutive tiles (the partial
-// of every tile is still computed and stored on its own, so the canonical
-// reduction is unchanged); fewer, fuller CTAs than one per 256-row tile.
-constexpr int kVecTiles = 4;
-__device__ __forceinline__ int vec_t0() { return blockIdx.x * kVecTiles; }
-__device__ __forceinline__ int vec_t1(const SysView& s) { return min(s.n_tiles, (int)(blockIdx.x + 1) * kVecTiles); }
+// Vector phases: each CTA handles vec_tiles_for(tile_rows) consecutive tiles
+// (the partial of every tile is still computed and stored on its own, so the
+// canonical reduction is unchanged): small tiles are grouped into fuller CTAs.
+__device__ __forceinline__ int vec_t0(const SysView& s) { return blockIdx.x * vec_tiles_for(s.tile_rows); }
+__device__ __forceinline__ int vec_t1(const SysView& s) {
+  return min(s.n_tiles, (int)(blockIdx.x + 1) * vec_tiles_for(s.tile_rows));
+}
 
 template <int K>
 __device__ __forceinline__ void store_parts(const SysView& s, int tile, const double (&v)[K], int slot) {
@@ -104,7 +106,7 @@ __device__ __forceinline__ bool elect_last(unsigned int* counter) {
 __global__ void __launch_bounds__(kCTA) k_update_xr(SysView s) {
   if (ld_status(s.st) != ST_RUNNING) return;
   const double alpha = __ldcg(&s.st->alpha);
-  for (int t = vec_t0(), t1 = vec_t1(s); t < t1; ++t) {
+  for (int t = vec_t0(s), t1 = vec_t1(s); t < t1; ++t) {
     double v[2];
     tile_update_xr(s, t, alpha, v);
     store_parts<2>(s, t, v, kSlotXR);
@@ -120,11 +122,12 @@ __global__ void __launch_bounds__(kCTA) k_update_xr(SysView s) {
 __global__ void __launch_bounds__(kCTA) k_update_p(SysView s) {
   if (ld_status(s.st) != ST_RUNNING) return;
   const double beta = __ldcg(&s.st->beta);
-  for (int t = vec_t0(), t1 = vec_t1(s); t < t1; ++t) tile_update_p(s, t, beta);
+  for (int t = vec_t0(s), t1 = vec_t1(s); t < t1; ++t) tile_update_p(s, t, beta);
 }
 
-// Termination guard of a while-node body (single thread).
-__global__ void k_guard(SysView s, cudaGraphConditionalHandle h, int need_mode) {
+// Termination guard of a while-node body (single thread).  use_handle == 0:
+// launched outside a graph (eager mode), the host reads the status instead.
+__global__ void k_guard(SysView s, cudaGraphConditionalHandle h, int need_mode, int use_handle) {
   SysState* st = s.st;
   st->guard += 1;
   bool stop = st->status != ST_RUNNING;
@@ -137,7 +140,7 @@ __global__ void k_guard(SysView s, cudaGraphConditionalHandle h, int need_mode) 
     stop = true;
   }
   if (!stop && need_mode >= 0 && st->mode != need_mode) stop = true;
-  if (stop) cudaGraphSetConditional(h, 0u);
+  if (stop && use_handle) cudaGraphSetConditional(h, 0u);
 }
 
 // ||b - A x||^2 of the final iterate; zeroes x when b == 0.
@@ -163,7 +166,7 @@ __global__ void __launch_bounds__(kCTA) k_final(SysView s) {
 // Reliable update, part 1: x += c, c = 0 (only when an update is due).
 __global__ void __launch_bounds__(kCTA) k_mx_apply(SysView s) {
   if (ld_status(s.st) != ST_RUNNING || ld_mode(s.st) != 0) return;
-  for (int t = vec_t0(), t1 = vec_t1(s); t < t1; ++t) tile_mx_apply(s, t);
+  for (int t = vec_t0(s), t1 = vec_t1(s); t < t1; ++t) tile_mx_apply(s, t);
 }
 
 // Reliable update, part 2: FP64 true residual, FP32 residual replaced.
@@ -193,11 +196,13 @@ __global__ void __launch_bounds__(kCTA) k_mx_spmv_pq(SysView s) {
 }
 
 // c += a p, r -= a q; the last CTA decides whether a reliable update is due
-// and sets the condition of the IF node that runs it.
-__global__ void __launch_bounds__(kCTA) k_mx_update_cr(SysView s, cudaGraphConditionalHandle h_upd) {
+// and sets the condition of the IF node that runs it (use_handle == 0: eager
+// mode, the update kernels are launched anyway and check the mode).
+__global__ void __launch_bounds__(kCTA) k_mx_update_cr(SysView s, cudaGraphConditionalHandle h_upd,
+                                                       int use_handle) {
   if (ld_status(s.st) != ST_RUNNING || ld_mode(s.st) != 1) return;
   const double alpha = __ldcg(&s.st->alpha);
-  for (int t = vec_t0(), t1 = vec_t1(s); t < t1; ++t) {
+  for (int t = vec_t0(s), t1 = vec_t1(s); t < t1; ++t) {
     double v[2];
     tile_mx_update_cr(s, t, alpha, v);
     store_parts<2>(s, t, v, kSlotXR);
@@ -209,7 +214,7 @@ __global__ void __launch_bounds__(kCTA) k_mx_update_cr(SysView s, cudaGraphCondi
     if (threadIdx.x == 0) {
       scalar_after_mx_cr(s.st, o[0], o[1]);
       const bool upd = s.st->status == ST_RUNNING && s.st->mode == 0;
-      cudaGraphSetConditional(h_upd, upd ? 1u : 0u);
+      if (use_handle) cudaGraphSetConditional(h_upd, upd ? 1u : 0u);
     }
   }
 }
@@ -217,7 +222,7 @@ __global__ void __launch_bounds__(kCTA) k_mx_update_cr(SysView s, cudaGraphCondi
 __global__ void __launch_bounds__(kCTA) k_mx_update_p(SysView s) {
   if (ld_status(s.st) != ST_RUNNING || ld_mode(s.st) != 1) return;
   const double beta = __ldcg(&s.st->beta);
-  for (int t = vec_t0(), t1 = vec_t1(s); t < t1; ++t) tile_mx_update_p(s, t, beta);
+  for (int t = vec_t0(s), t1 = vec_t1(s); t < t1; ++t) tile_mx_update_p(s, t, beta);
 }
 
 // ---------------------------------------------------------------------------
@@ -278,6 +283,18 @@ static int grid_for(long long n, int threads) {
   return (int)std::max(1LL, std::min(g, 152LL * 32));
 }
 
+// 256-thread phase CTAs resident on the device at once (eight per SM: the
+// phase kernels use at most 32 registers per thread).
+static long long resident_slots() {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+    cudaGetLastError();
+    sms = 152;
+  }
+  return 8LL * sms;
+}
+
 TuneChoice autotune(int n, long long nnz, int max_row, const int* hist33) {
   // Threads per row: the smallest power of two with at most ~8 nonzeros per
   // lane for the typical row (measured on GB300 with the 7-nonzero cotangent
@@ -298,14 +315,27 @@ TuneChoice autotune(int n, long long nnz, int max_row, const int* hist33) {
   const double typical = std::max(mean, 0.75 * double(p90 == 32 ? std::max(32, max_row) : p90));
   int tpr = 1;
   while (tpr < 32 && tpr * 8 < typical) tpr *= 2;
-  // Tile rows: small tiles keep many CTAs in flight (measured on GB300: the
-  // 4.2M-row Laplacian SpMV runs at 5.25 TB/s with 256-row tiles vs 5.0 with
-  // 1024 and 4.93 with 4096; the L2-resident 131k-row LSCM matrix is fastest
-  // at 128), but every scalar is a reduction over all tiles, done by one CTA
-  // per phase: ~10k tiles cost more than the SpMV itself on a 1.3M-row
-  // system.  So at most ~2k tiles: 128 rows up to 256k rows, then n / 2048.
+  // Tile rows.  Every phase kernel runs one CTA per tile (the vector phases
+  // one per tile group), eight 256-thread CTAs resident per SM.  A second,
+  // nearly empty wave of CTAs costs as much as a full one (measured on GB300
+  // with the 1.3M-row LSCM matrix: 1,276 tiles of 1,024 rows left the SMs
+  // idle 27 % of the SpMV), so the tile size minimises the rows of the
+  // busiest CTA slot, ceil(tiles / slots) x tile_rows, over multiples of 128
+  // rows with at most 4,096 tiles; among equal costs the fewest tiles (each
+  // scalar is a reduction over the tiles, so three waves of 384-row tiles
+  // are slower than one wave of 1,152).  Small systems keep 128-row tiles:
+  // one wave of CTAs as small as they go.
+  const long long slots = resident_slots();
   int tile = 128;
-  while (tile < 4096 && (long long)tile * 2048 < n) tile *= 2;
+  if ((long long)n > slots * 128) {
+    long long best_cost = -1;
+    for (int t = 128; t <= 16384; t += 128) {
+      const long long nt = ((long long)n + t - 1) / t;
+      if (nt > 4096) continue;
+      const long long cost = ((nt + slots - 1) / slots) * (long long)t;
+      if (best_cost < 0 || cost <= best_cost) { best_cost = cost; tile = t; }
+    }
+  }
   (void)acc;
   return TuneChoice{tpr, tile};
 }
@@ -403,18 +433,14 @@ static cudaError_t spmv_dispatch(const DeviceCRS& A, const V* va, const X* x, X*
   const int grid = (A.n + tile - 1) / tile;
   switch (A.tpr > 0 ? A.tpr : 4) {
     case 1: k_spmv<1, V, X><<<grid, kCTA, 0, s>>>(A.n, tile, A.rp, A.ci, va, x, y); break;
-    count_launches(1);
     case 2: k_spmv<2, V, X><<<grid, kCTA, 0, s>>>(A.n, tile, A.rp, A.ci, va, x, y); break;
-    count_launches(1);
     case 4: k_spmv<4, V, X><<<grid, kCTA, 0, s>>>(A.n, tile, A.rp, A.ci, va, x, y); break;
-    count_launches(1);
     case 8: k_spmv<8, V, X><<<grid, kCTA, 0, s>>>(A.n, tile, A.rp, A.ci, va, x, y); break;
-    count_launches(1);
     case 16: k_spmv<16, V, X><<<grid, kCTA, 0, s>>>(A.n, tile, A.rp, A.ci, va, x, y); break;
-    count_launches(1);
     default: k_spmv<32, V, X><<<grid, kCTA, 0, s>>>(A.n, tile, A.rp, A.ci, va, x, y); break;
-    count_launches(1);
   }
+  count_launches(1);
+
   return cudaGetLastError();
 }
 
@@ -569,13 +595,13 @@ cudaError_t PcgSolver::build_plain_graph() {
   for (int u = 0; u < kUnrollPlain; ++u) {
     cudaGraphNode_t n1, n2, n3;
     NLGB_CUDA_TRY(add_kernel(body, &n1, prev, ks.spmv, n_tiles_, kCTA, a1));
-    const int vg = (n_tiles_ + kVecTiles - 1) / kVecTiles;
+    const int vg = (n_tiles_ + vec_tiles_for(tile_rows_) - 1) / vec_tiles_for(tile_rows_);
     NLGB_CUDA_TRY(add_kernel(body, &n2, n1, (const void*)k_update_xr, vg, kCTA, a1));
     NLGB_CUDA_TRY(add_kernel(body, &n3, n2, (const void*)k_update_p, vg, kCTA, a1));
     prev = n3;
   }
-  int need_mode = -1;
-  void* ag[] = {&v, &h, &need_mode};
+  int need_mode = -1, use_handle = 1;
+  void* ag[] = {&v, &h, &need_mode, &use_handle};
   cudaGraphNode_t n_g;
   NLGB_CUDA_TRY(add_kernel(body, &n_g, prev, (const void*)k_guard, 1, 1, ag));
   NLGB_CUDA_TRY(add_kernel(g, &n_fin, n_loop, ks.fin, n_tiles_, kCTA, a1));
@@ -606,10 +632,11 @@ cudaError_t PcgSolver::build_mixed_graph() {
   for (int u = 0; u < kUnrollInner; ++u) {
     NLGB_CUDA_TRY(cudaGraphConditionalHandleCreate(&h_upd[u], body, 0u, cudaGraphCondAssignDefault));
     cudaGraphNode_t n1, n2, n3, n_if, n4, n5;
-    const int vg = (n_tiles_ + kVecTiles - 1) / kVecTiles;
+    const int vg = (n_tiles_ + vec_tiles_for(tile_rows_) - 1) / vec_tiles_for(tile_rows_);
     NLGB_CUDA_TRY(add_kernel(body, &n1, prev, (const void*)k_mx_update_p, vg, kCTA, a1));
     NLGB_CUDA_TRY(add_kernel(body, &n2, n1, ks.mx_spmv, n_tiles_, kCTA, a1));
-    void* acr[] = {&v, &h_upd[u]};
+    int use_handle = 1;
+    void* acr[] = {&v, &h_upd[u], &use_handle};
     NLGB_CUDA_TRY(add_kernel(body, &n3, n2, (const void*)k_mx_update_cr, vg, kCTA, acr));
     cudaGraph_t ubody;
     NLGB_CUDA_TRY(add_cond(body, &n_if, n3, h_upd[u], cudaGraphCondTypeIf, &ubody));
@@ -617,14 +644,68 @@ cudaError_t PcgSolver::build_mixed_graph() {
     NLGB_CUDA_TRY(add_kernel(ubody, &n5, n4, ks.mx_outer, n_tiles_, kCTA, a1));
     prev = n_if;
   }
-  int need_any = -1;
-  void* ag[] = {&v, &h_loop, &need_any};
+  int need_any = -1, use_handle = 1;
+  void* ag[] = {&v, &h_loop, &need_any, &use_handle};
   cudaGraphNode_t n_g;
   NLGB_CUDA_TRY(add_kernel(body, &n_g, prev, (const void*)k_guard, 1, 1, ag));
   NLGB_CUDA_TRY(add_kernel(g, &n_fin, n_loop, ks.fin, n_tiles_, kCTA, a1));
   cudaError_t e = cudaGraphInstantiate(&mixed_exec_, g, 0);
   cudaGraphDestroy(g);
   NLGB_CUDA_TRY(e);
+  return cudaSuccess;
+}
+
+// Eager mode (environment NLGB_EAGER_SOLVE=1): the same kernels as the
+// graphs, launched one by one from a host loop that reads the status after
+// every unrolled pass.  Slower (one host round trip per pass); it exists so
+// that profilers which do not descend into conditional graph nodes see
+// every kernel of an iteration.
+static bool eager_mode() {
+  static const bool on = [] {
+    const char* e = std::getenv("NLGB_EAGER_SOLVE");
+    return e != nullptr && e[0] == '1';
+  }();
+  return on;
+}
+
+cudaError_t PcgSolver::run_eager(bool mixed, SysState* h) {
+  SysView v = make_view(A_, tile_rows_, n_tiles_, b_, x_, r_, p_, q_, r32_, p32_, q32_, c32_,
+                        part_, st_, abort_flag_);
+  const KernelSet ks = kernels_for(tpr_);
+  const int vg = (n_tiles_ + vec_tiles_for(tile_rows_) - 1) / vec_tiles_for(tile_rows_);
+  const cudaGraphConditionalHandle none = 0;
+  const int need = -1, no_handle = 0;
+  long long launched = 0;
+  auto go = [&](const void* fn, int grid, int block, void** args) {
+    ++launched;
+    return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, 0, stream_);
+  };
+  void* a1[] = {&v};
+  void* ag[] = {&v, const_cast<cudaGraphConditionalHandle*>(&none), const_cast<int*>(&need),
+                const_cast<int*>(&no_handle)};
+  void* acr[] = {&v, const_cast<cudaGraphConditionalHandle*>(&none), const_cast<int*>(&no_handle)};
+  NLGB_CUDA_TRY(go(mixed ? ks.mx_outer : ks.init, n_tiles_, kCTA, a1));
+  while (true) {
+    for (int u = 0; u < (mixed ? kUnrollInner : kUnrollPlain); ++u) {
+      if (mixed) {
+        NLGB_CUDA_TRY(go((const void*)k_mx_update_p, vg, kCTA, a1));
+        NLGB_CUDA_TRY(go(ks.mx_spmv, n_tiles_, kCTA, a1));
+        NLGB_CUDA_TRY(go((const void*)k_mx_update_cr, vg, kCTA, acr));
+        NLGB_CUDA_TRY(go((const void*)k_mx_apply, vg, kCTA, a1));   // return unless an update is due
+        NLGB_CUDA_TRY(go(ks.mx_outer, n_tiles_, kCTA, a1));
+      } else {
+        NLGB_CUDA_TRY(go(ks.spmv, n_tiles_, kCTA, a1));
+        NLGB_CUDA_TRY(go((const void*)k_update_xr, vg, kCTA, a1));
+        NLGB_CUDA_TRY(go((const void*)k_update_p, vg, kCTA, a1));
+      }
+    }
+    NLGB_CUDA_TRY(go((const void*)k_guard, 1, 1, ag));
+    NLGB_CUDA_TRY(cudaMemcpyAsync(h, st_, sizeof(SysState), cudaMemcpyDeviceToHost, stream_));
+    NLGB_CUDA_TRY(cudaStreamSynchronize(stream_));
+    if (h->status != ST_RUNNING) break;
+  }
+  NLGB_CUDA_TRY(go(ks.fin, n_tiles_, kCTA, a1));
+  count_launches(launched);
   return cudaSuccess;
 }
 
@@ -660,11 +741,16 @@ cudaError_t PcgSolver::run_graph(bool mixed, const SolveParams& prm, long long m
     NLGB_CUDA_TRY(cudaMemsetAsync(p32_, 0, (size_t)n_ * sizeof(float), stream_));
   }
   NLGB_CUDA_TRY(cudaEventRecord(ev0_, stream_));
-  NLGB_CUDA_TRY(cudaGraphLaunch(mixed ? mixed_exec_ : plain_exec_, stream_));
+  if (eager_mode()) {
+    NLGB_CUDA_TRY(run_eager(mixed, h));
+  } else {
+    NLGB_CUDA_TRY(cudaGraphLaunch(mixed ? mixed_exec_ : plain_exec_, stream_));
+  }
   NLGB_CUDA_TRY(cudaEventRecord(ev1_, stream_));
   NLGB_CUDA_TRY(cudaMemcpyAsync(h, st_, sizeof(SysState), cudaMemcpyDeviceToHost, stream_));
   NLGB_CUDA_TRY(cudaStreamSynchronize(stream_));
   NLGB_CUDA_TRY(cudaEventElapsedTime(ms, ev0_, ev1_));
+  if (eager_mode()) return cudaSuccess;   // run_eager counted its launches
   ++graph_launches_;
   // Kernel nodes executed: every while-body pass runs all of its kernels
   // (3 per unrolled iteration + the guard); the mixed graph adds 2 kernels

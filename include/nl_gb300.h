@@ -66,7 +66,7 @@ void        nlgb_matrix_destroy(nlgb_matrix A);
 int         nlgb_matrix_info(nlgb_matrix A, int* n_rows, long long* nnz, int* threads_per_row,
                              int* tile_rows);
 /* Override the autotuner (threads_per_row in {1,2,4,8,16,32}, tile_rows a
- * power of two in [64, 2^20]; 0 keeps the current value). */
+ * multiple of 64 in [64, 2^20]; 0 keeps the current value). */
 int         nlgb_matrix_set_layout(nlgb_matrix A, int threads_per_row, int tile_rows);
 /* Copy the CRS arrays back to host buffers of size n+1 / nnz / nnz. */
 int         nlgb_matrix_download(nlgb_matrix A, int* rp, int* ci, double* va);
