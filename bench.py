@@ -8,7 +8,9 @@ fairing (3 right-hand sides) with probability 1/2 each, vertex counts
 log-uniform in [1e3, 1e6], square-ish grid patches with the seeded bump
 model, Poisson arrivals at `--rate` per second -- submitted through the C ABI
 (nlgb_server_submit_rows / _crs with host buffers) to the continuous-batching
-server (HBM budget 150 GB, mixed precision with FP64 fallback) and drained.
+server (HBM budget 150 GB, precision AUTO: mixed FP32/FP64 with FP64
+fallback for square systems, FP64 for least-squares normal equations) and
+drained.
 Every step re-submits the same sample from scratch (assembly, upload, solve,
 download: nothing is cached).
 
@@ -24,8 +26,11 @@ Reported:
               request from its iteration counts) vs the measured HBM peak;
   spmv_fp64   the FP64 CRS SpMV on the 2048^2 cotangent Laplacian (4.2M
               rows, 29.3M nonzeros) vs the measured HBM peak;
-  cpu_baseline  the CPU oracle (C, OpenMP, FP64 Jacobi-PCG on host cores)
-              on a bounded prefix of the same sample.
+  cpu_baseline  the CPU oracle (C, OpenMP, FP64 Jacobi-PCG on all host
+              cores) on the same sample: every request assembled and timed;
+              systems over 250k unknowns timed on 200 iterations and scaled
+              to the oracle's own iteration count for them (committed
+              fixture oracle/serving_sample_iterations.json).
 `--impl reference` runs only the CPU reference arm (the oracle port: the
 reference's own OpenNL source is not in the checkout) and prints its line.
 """
@@ -62,12 +67,11 @@ def parse_args():
     p.add_argument("--rate", type=float, default=1000.0)
     p.add_argument("--eps", type=float, default=1e-10)
     p.add_argument("--budget-gb", type=float, default=150.0)
-    p.add_argument("--cpu-seconds", type=float, default=20.0)
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-spmv", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--profile-case", choices=["spmv", "batch", "batch_small", "plain", "mixed", "plain_lscm",
-                                              "mixed_lscm"], default=None,
+    p.add_argument("--profile-case", choices=["spmv", "batch", "batch_small", "batch_lscm", "plain", "mixed",
+                                              "plain_lscm", "mixed_lscm"], default=None,
                    help="run one small case for an ncu capture and exit")
     p.add_argument("--workload", choices=["serving", "configs"], default="serving",
                    help="configs: measure the other benchmark configurations and exit")
@@ -139,6 +143,8 @@ def profile_case(which):
            iterations each (k_batch);
     plain_lscm / mixed_lscm: 40 iterations on the 1.3M-unknown LSCM normal
            equations (808^2 grid), graph path;
+    batch_lscm: the 1.3M-unknown LSCM system alone in the persistent kernel,
+           200 FP64 iterations;
     batch_small: one 4,604-unknown LSCM system in the persistent kernel,
            1000 iterations (k_batch, latency-bound);
     plain: 20 FP64 PCG iterations on the 2048^2 Laplacian (graph kernels);
@@ -170,6 +176,14 @@ def profile_case(which):
                           precision="double" if which == "plain_lscm" else "mixed")
         print(json.dumps({"case": which, "iterations": info.iterations, "ms": info.seconds * 1e3,
                           "n": M.n, "nnz": M.nnz, "tile_rows": M.tile_rows, "tpr": M.threads_per_row}))
+        return
+    if which == "batch_lscm":
+        # the 1.3M-unknown LSCM system alone in the persistent kernel, 200
+        # FP64 iterations (one team over the whole grid)
+        M, rhs, _ = solver.assemble(systems.lscm_system(808, 808, seed=1))
+        xs, infos, ks = solver.batch_solve([M], [rhs[0]], max_iter=200, eps=1e-30)
+        print(json.dumps({"case": which, "kernel_ms": ks * 1e3, "iterations": infos[0].iterations,
+                          "us_per_iteration": 1e3 * ks * 1e3 / max(1, infos[0].iterations)}))
         return
     if which == "batch_small":
         # one small LSCM system (4,604 unknowns, 35 tiles) in the persistent
@@ -204,14 +218,7 @@ def measured_peak():
 
 def build_sample(R, seed, rate):
     from graphitethree_gb300 import systems
-    reqs = systems.request_stream(R, seed, rate, 1_000, 1_000_000)
-    objs = []
-    for r in reqs:
-        if r.kind == "lscm":
-            objs.append(("rows", systems.lscm_system(r.nx, r.ny, r.seed)))
-        else:
-            objs.append(("square", systems.fairing_system(r.nx, r.ny, r.seed, lam=1e-2, n_rhs=3)))
-    return reqs, objs
+    return systems.serving_sample(R, seed, rate, 1_000, 1_000_000)
 
 
 def io_bytes(objs):
@@ -317,44 +324,81 @@ def spmv_roofline(peak):
     return out
 
 
-def cpu_arm(objs, reqs, budget_s, eps):
-    """Oracle FP64 Jacobi-PCG (C, OpenMP on all host cores) on a bounded
-    prefix of the sample, in arrival order."""
+CPU_FULL_LIMIT = 250_000   # unknowns: systems up to this size are solved to completion
+CPU_PROBE_ITERS = 200       # timed iterations of a larger system
+
+
+def sample_iterations_fixture(args):
+    """Per-system iteration counts of the oracle's PCG on this exact sample
+    (oracle/make_sample_iterations.py), or None for another sample."""
+    path = ROOT / "oracle" / "serving_sample_iterations.json"
+    try:
+        fx = json.loads(path.read_text())
+    except (OSError, ValueError):
+        return None
+    if (fx.get("requests"), fx.get("seed"), fx.get("rate"), fx.get("eps")) != \
+            (args.requests, args.seed, args.rate, args.eps):
+        return None
+    return {r["request"]: r for r in fx["systems"]}
+
+
+def cpu_arm(objs, args):
+    """The oracle (C, OpenMP on all host cores): row assembly + FP64
+    Jacobi-PCG for every request of the sample, in arrival order.  Systems up
+    to CPU_FULL_LIMIT unknowns are solved to completion; a larger one runs
+    CPU_PROBE_ITERS timed iterations and its solve time is that per-iteration
+    time x the iteration count the same oracle needs to converge on it
+    (committed fixture).  Without the fixture the larger requests are left
+    out and the sample says so."""
     from oracle import oracle
     threads = oracle.max_threads()
-    t_total = 0.0
-    done = 0
-    sizes = []
-    for (kind, o) in objs:
-        # a single large LSCM request takes minutes on the host: the bounded
-        # sample keeps the requests up to 250k unknowns, in arrival order
-        unknowns = o.n_vars if kind == "rows" else o.n
-        if unknowns > 250_000:
-            continue
+    fx = sample_iterations_fixture(args)
+    total, done, full, scaled, skipped = 0.0, 0, [], [], []
+    for i, (kind, o) in enumerate(objs):
         t0 = time.perf_counter()
         rp, ci, va, rhs = oracle.assemble_rowstream(o if kind == "rows" else o.to_rows())
-        for s in range(rhs.shape[0]):
-            oracle.pcg(rp, ci, va, rhs[s], eps=eps, nthreads=threads)
-        t_total += time.perf_counter() - t0
+        t_req = time.perf_counter() - t0
+        n = int(rp.shape[0] - 1)
+        if n <= CPU_FULL_LIMIT:
+            t0 = time.perf_counter()
+            for s in range(rhs.shape[0]):
+                oracle.pcg(rp, ci, va, rhs[s], eps=args.eps, nthreads=threads)
+            t_req += time.perf_counter() - t0
+            full.append(n)
+        elif fx is not None and i in fx and fx[i]["unknowns"] == n:
+            for s in range(rhs.shape[0]):
+                t0 = time.perf_counter()
+                _, _, it, _ = oracle.pcg(rp, ci, va, rhs[s], eps=1e-300, max_iter=CPU_PROBE_ITERS,
+                                         nthreads=threads)
+                per_iter = (time.perf_counter() - t0) / max(1, it)
+                t_req += per_iter * fx[i]["iterations"][s]
+            scaled.append((n, fx[i]["iterations"]))
+        else:
+            skipped.append(n)
+            continue
+        total += t_req
         done += 1
-        sizes.append(int(rp.shape[0] - 1))
-        if t_total >= budget_s:
-            break
-    return {"value": done / t_total if t_total > 0 else 0.0, "unit": "solves/s", "cores": threads,
-            "kind": "port",
-            "sample": f"{done} of the {len(objs)} sampled requests (those with <= 250k "
-                      f"unknowns, in arrival order; systems solved: {sizes}), CPU assembly + "
-                      f"FP64 Jacobi-PCG to 1e-10, {t_total:.1f} s"}
+    desc = (f"all {len(objs)} requests of the sample: CPU assembly + FP64 Jacobi-PCG to "
+            f"{args.eps:g}; systems solved to completion: {full}")
+    if scaled:
+        desc += (f"; larger systems (unknowns, iterations to converge): {scaled} -- "
+                 f"{CPU_PROBE_ITERS} iterations timed, scaled to the oracle's own iteration "
+                 f"count (oracle/serving_sample_iterations.json)")
+    if skipped:
+        desc += f"; left out (no iteration-count fixture for this sample): {skipped}"
+    desc += f"; {total:.1f} s of host time"
+    return {"value": done / total if total > 0 else 0.0, "unit": "solves/s", "cores": threads,
+            "kind": "port", "sample": desc}
 
 
 def run_reference(args):
     reqs, objs = build_sample(args.requests, args.seed, args.rate)
-    # bounded: each step solves a prefix of the sample within ~cpu_seconds / steps
+    # each step: the whole sample on the host cores (large systems timed on a
+    # bounded number of iterations, see cpu_arm)
     vals = []
-    per_step = max(2.0, args.cpu_seconds / max(1, args.steps + args.warmup))
     res = None
     for i in range(args.warmup + args.steps):
-        r = cpu_arm(objs, reqs, per_step, args.eps)
+        r = cpu_arm(objs, args)
         if i >= args.warmup:
             vals.append(r["value"])
             res = r
@@ -374,7 +418,9 @@ def config(args):
                         f"(3 RHS) 50/50, vertices log-uniform [1e3,1e6], Poisson arrivals "
                         f"{args.rate:g}/s, seed {args.seed}",
             "requests": args.requests, "rate_per_s": args.rate, "rel_residual": args.eps,
-            "hbm_budget_gb": args.budget_gb, "precision": "mixed FP32/FP64 with FP64 fallback",
+            "hbm_budget_gb": args.budget_gb,
+            "precision": "auto: mixed FP32/FP64 (with FP64 fallback) for the square fairing "
+                         "systems, FP64 for the least-squares LSCM normal equations",
             "l2": "inputs larger than L2 for the large requests; every step re-uploads and "
                   "re-assembles (no cached data)"}
 
@@ -412,7 +458,7 @@ def main():
     R = len(objs)
 
     for _ in range(args.warmup):
-        serve(objs, reqs, "mixed", "batched", args.eps, budget)
+        serve(objs, reqs, "auto", "batched", args.eps, budget)
     if dist is not None:
         dist.barrier()
     clocks = ClockSampler()
@@ -421,7 +467,7 @@ def main():
     steps = []
     t_wall0 = time.perf_counter()
     for _ in range(args.steps):
-        st, results = serve(objs, reqs, "mixed", "batched", args.eps, budget)
+        st, results = serve(objs, reqs, "auto", "batched", args.eps, budget)
         steps.append((st, results))
     t_wall = time.perf_counter() - t_wall0
     launches = L.nlgb_kernel_launches() - launches0
@@ -457,7 +503,7 @@ def main():
     spmv = None if args.no_spmv else spmv_roofline(peak)
     cpu = None
     if not args.no_cpu and rank == 0:
-        cpu = cpu_arm(objs, reqs, args.cpu_seconds, args.eps)
+        cpu = cpu_arm(objs, args)
 
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,

@@ -261,6 +261,13 @@ void ij_to_rows(Context* c) {
 }
 
 // Upload the row stream and assemble the system on the GPU.
+// NL_GB300_PRECISION_AUTO: FP64 for least-squares (normal-equation) systems,
+// mixed for square ones.
+int effective_precision(const Context* c) {
+  if (c->precision != NL_GB300_PRECISION_AUTO) return c->precision;
+  return c->least_squares ? NL_GB300_PRECISION_DOUBLE : NL_GB300_PRECISION_MIXED;
+}
+
 bool assemble(Context* c) {
   std::string why;
   if (!device_ready(&why)) { nl_error(NL_DEVICE_ERROR, "nlSolve: " + why); return false; }
@@ -317,7 +324,7 @@ bool assemble(Context* c) {
                                    : assemble_square(R, c->A, c->d_rhs, s);
   if (e != cudaSuccess) return fail("assembly");
   if (c->tpr_override > 0) { c->A.tpr = c->tpr_override; }
-  e = crs_prepare(c->A, c->precision == NL_GB300_PRECISION_MIXED, s);
+  e = crs_prepare(c->A, effective_precision(c) == NL_GB300_PRECISION_MIXED, s);
   if (c->tpr_override > 0) c->A.tpr = c->tpr_override;
   if (e != cudaSuccess) return fail("matrix preparation");
   if (cudaStreamSynchronize(s) != cudaSuccess) { set_error(cudaGetErrorString(cudaGetLastError())); return fail("assembly"); }
@@ -399,7 +406,8 @@ void nlSolverParameteri(NLenum pname, NLint param) {
           param != (NLint)NL_PRECOND_SSOR) { nl_error(NL_INVALID_ENUM, "unknown NL_PRECONDITIONER"); return; }
       c->precond = (NLenum)param; invalidate_device(c); break;
     case NL_GB300_PRECISION:
-      if (param != NL_GB300_PRECISION_DOUBLE && param != NL_GB300_PRECISION_MIXED) {
+      if (param != NL_GB300_PRECISION_DOUBLE && param != NL_GB300_PRECISION_MIXED &&
+          param != NL_GB300_PRECISION_AUTO) {
         nl_error(NL_INVALID_ENUM, "unknown NL_GB300_PRECISION"); return;
       }
       c->precision = param; invalidate_device(c); break;
@@ -734,7 +742,7 @@ NLboolean nlSolve(void) {
   SolveParams prm;
   prm.eps = c->threshold;
   prm.max_iter = c->max_iterations >= 0 ? c->max_iterations : 5LL * nf;
-  prm.precision = c->precision;
+  prm.precision = effective_precision(c);
   prm.inner_eps = c->inner_threshold;
   prm.max_outer = c->max_refinement;
   bool ok = true;

@@ -239,8 +239,11 @@ int nlgb_solve(nlgb_matrix A, const double* b, double* x, const nlgb_params* prm
   nlgb_params p;
   nlgb_default_params(&p);
   if (prm) p = *prm;
-  if (p.precision != NL_GB300_PRECISION_DOUBLE && p.precision != NL_GB300_PRECISION_MIXED)
+  if (p.precision != NL_GB300_PRECISION_DOUBLE && p.precision != NL_GB300_PRECISION_MIXED &&
+      p.precision != NL_GB300_PRECISION_AUTO)
     return fail(NLGB_E_INVALID, "nlgb_solve: unknown precision");
+  // a matrix given directly is square: AUTO means mixed
+  if (p.precision == NL_GB300_PRECISION_AUTO) p.precision = NL_GB300_PRECISION_MIXED;
   if (!(p.eps >= 0.0) || !(p.inner_eps > 0.0 && p.inner_eps < 1.0) || p.max_outer < 1)
     return fail(NLGB_E_INVALID, "nlgb_solve: bad tolerances");
   cudaStream_t s = A->stream;
@@ -283,8 +286,11 @@ int nlgb_batch_solve(int n_sys, const nlgb_matrix* A, const double* const* b, do
   nlgb_params p;
   nlgb_default_params(&p);
   if (prm) p = *prm;
-  if (p.precision != NL_GB300_PRECISION_DOUBLE && p.precision != NL_GB300_PRECISION_MIXED)
+  if (p.precision != NL_GB300_PRECISION_DOUBLE && p.precision != NL_GB300_PRECISION_MIXED &&
+      p.precision != NL_GB300_PRECISION_AUTO)
     return fail(NLGB_E_INVALID, "nlgb_batch_solve: unknown precision");
+  // a matrix given directly is square: AUTO means mixed
+  if (p.precision == NL_GB300_PRECISION_AUTO) p.precision = NL_GB300_PRECISION_MIXED;
   if (n_sys == 0) return NLGB_OK;
   if (!ensure_ready()) return NLGB_E_DEVICE;
   const bool mixed = p.precision == NL_GB300_PRECISION_MIXED;

@@ -63,7 +63,7 @@ __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long lon
 // CTA's writes before thread 0's release; thread 0's acquire and the
 // __syncthreads after the wait order the other CTAs' writes before this
 // CTA's next reads (which go through L2: __ldcg).
-__device__ bool team_sync(TeamBar* bar, int k, int r, int* err) {
+__device__ __noinline__ bool team_sync(TeamBar* bar, int k, int r, int* err) {
   if (k == 1) {
     __syncthreads();
     return true;
@@ -137,6 +137,91 @@ __device__ void get_sums(const SysView& s, int slot, double (&o)[K]) {
   if (threadIdx.x == 0) { stmt; } \
   __syncthreads();
 
+// Phase procedures: the tile loop of one phase for this CTA's tiles (t = r,
+// r + k, ...), partials stored for the canonical reduction.  Kept out of line
+// so that each is register-allocated on its own: inlined into the one
+// persistent kernel (six threads-per-row variants of each) they forced the
+// kernel to spill inside the SpMV loops.  NLGB_HOT_PHASE marks the three
+// phases of the FP64 iteration.
+#ifndef NLGB_HOT_PHASE
+#define NLGB_HOT_PHASE __noinline__
+#endif
+__device__ __noinline__ void ph_residual(const SysView& s, int r, int k) {
+  for (int t = r; t < s.n_tiles; t += k) {
+    double v[3];
+    NLGB_TPR_SWITCH(tile_residual<T, true>(s, t, v));
+    put_parts(s, t, kSlotInit, v, 3);
+  }
+}
+__device__ __noinline__ void ph_mx_outer(const SysView& s, int r, int k) {
+  for (int t = r; t < s.n_tiles; t += k) {
+    double v[4];
+    NLGB_TPR_SWITCH(tile_mx_outer<T, true>(s, t, v));
+    put_parts(s, t, kSlotInit, v, 4);
+  }
+}
+__device__ NLGB_HOT_PHASE void ph_spmv_pq(const SysView& s, int r, int k) {
+  for (int t = r; t < s.n_tiles; t += k) {
+    double v[1];
+    NLGB_TPR_SWITCH(v[0] = tile_spmv_pq<T, true>(s, t));
+    put_parts(s, t, kSlotPQ, v, 1);
+  }
+}
+__device__ NLGB_HOT_PHASE void ph_update_xr(const SysView& s, int r, int k, double alpha) {
+  for (int t = r; t < s.n_tiles; t += k) {
+    double v[2];
+    tile_update_xr(s, t, alpha, v);
+    put_parts(s, t, kSlotXR, v, 2);
+  }
+}
+__device__ NLGB_HOT_PHASE void ph_update_p(const SysView& s, int r, int k, double beta) {
+  for (int t = r; t < s.n_tiles; t += k) tile_update_p(s, t, beta);
+}
+__device__ __noinline__ void ph_mx_update_p(const SysView& s, int r, int k, double beta) {
+  for (int t = r; t < s.n_tiles; t += k) tile_mx_update_p(s, t, beta);
+}
+__device__ __noinline__ void ph_mx_spmv_pq(const SysView& s, int r, int k) {
+  for (int t = r; t < s.n_tiles; t += k) {
+    double v[1];
+    NLGB_TPR_SWITCH(v[0] = tile_mx_spmv_pq<T, true>(s, t));
+    put_parts(s, t, kSlotPQ, v, 1);
+  }
+}
+__device__ __noinline__ void ph_mx_update_cr(const SysView& s, int r, int k, double alpha) {
+  for (int t = r; t < s.n_tiles; t += k) {
+    double v[2];
+    tile_mx_update_cr(s, t, alpha, v);
+    put_parts(s, t, kSlotXR, v, 2);
+  }
+}
+__device__ __noinline__ void ph_mx_apply(const SysView& s, int r, int k) {
+  for (int t = r; t < s.n_tiles; t += k) tile_mx_apply(s, t);
+}
+__device__ __noinline__ void ph_final(const SysView& s, int r, int k, bool zero_rhs) {
+  for (int t = r; t < s.n_tiles; t += k) {
+    double v[1] = {0.0};
+    if (zero_rhs) {
+      tile_zero_x(s, t);
+    } else {
+      NLGB_TPR_SWITCH(v[0] = tile_true_rr<T, true>(s, t));
+    }
+    put_parts(s, t, kSlotFinal, v, 1);
+  }
+}
+
+// Canonical sums of K consecutive partial slots (out of line, as above).
+struct Sums4 { double v[4]; };
+__device__ __noinline__ Sums4 sums_of(const SysView& s, int slot, int K) {
+  Sums4 o = {{0.0, 0.0, 0.0, 0.0}};
+  switch (K) {
+    case 1: { double a[1]; get_sums<1>(s, slot, a); o.v[0] = a[0]; } break;
+    case 2: { double a[2]; get_sums<2>(s, slot, a); o.v[0] = a[0]; o.v[1] = a[1]; } break;
+    case 3: { double a[3]; get_sums<3>(s, slot, a); for (int i = 0; i < 3; ++i) o.v[i] = a[i]; } break;
+    default: { double a[4]; get_sums<4>(s, slot, a); for (int i = 0; i < 4; ++i) o.v[i] = a[i]; } break;
+  }
+  return o;
+}
+
 // One system, run by a team (rank r of k CTAs) for at most `budget`
 // iterations.  st: the CTA's shared-memory copy of the system state.
 __device__ void run_system_once(const SysView& s, SysState* st, int r, int k, TeamBar* bar, int* err,
@@ -145,108 +230,67 @@ __device__ void run_system_once(const SysView& s, SysState* st, int r, int k, Te
   long long done_iters = 0;
   if (st->stage == 0) {
     if (!mixed) {
-      for (int t = r; t < s.n_tiles; t += k) {
-        double v[3];
-        NLGB_TPR_SWITCH(tile_residual<T, true>(s, t, v));
-        put_parts(s, t, kSlotInit, v, 3);
-      }
+      ph_residual(s, r, k);
       if (!team_sync(bar, k, r, err)) { NLGB_SCALAR(st->status = ST_DEVICE_ERR; st->stage = 3); return; }
-      double o[3];
-      get_sums<3>(s, kSlotInit, o);
-      NLGB_SCALAR(scalar_after_init(st, o[0], o[1], o[2]); st->stage = st->status == ST_RUNNING ? 1 : 2);
+      const Sums4 o = sums_of(s, kSlotInit, 3);
+      NLGB_SCALAR(scalar_after_init(st, o.v[0], o.v[1], o.v[2]); st->stage = st->status == ST_RUNNING ? 1 : 2);
     } else {
       // initial FP64 residual (first "reliable update"; c = 0, p = 0)
-      for (int t = r; t < s.n_tiles; t += k) {
-        double v[4];
-        NLGB_TPR_SWITCH(tile_mx_outer<T, true>(s, t, v));
-        put_parts(s, t, kSlotInit, v, 4);
-      }
+      ph_mx_outer(s, r, k);
       if (!team_sync(bar, k, r, err)) { NLGB_SCALAR(st->status = ST_DEVICE_ERR; st->stage = 3); return; }
-      double o[4];
-      get_sums<4>(s, kSlotInit, o);
-      NLGB_SCALAR(st->mode = 0; scalar_after_outer(st, o[0], o[1], o[2], o[3]);
+      const Sums4 o = sums_of(s, kSlotInit, 4);
+      NLGB_SCALAR(st->mode = 0; scalar_after_outer(st, o.v[0], o.v[1], o.v[2], o.v[3]);
                   st->stage = st->status == ST_RUNNING ? 1 : 2);
     }
   }
   while (st->stage == 1 && (budget <= 0 || done_iters < budget)) {
     if (!mixed) {
       // q = A p, p.q
-      for (int t = r; t < s.n_tiles; t += k) {
-        double v[1];
-        NLGB_TPR_SWITCH(v[0] = tile_spmv_pq<T, true>(s, t));
-        put_parts(s, t, kSlotPQ, v, 1);
-      }
+      ph_spmv_pq(s, r, k);
       if (!team_sync(bar, k, r, err)) break;
       {
-        double o[1];
-        get_sums<1>(s, kSlotPQ, o);
-        NLGB_SCALAR(scalar_after_pq(st, o[0]));
+        const Sums4 o = sums_of(s, kSlotPQ, 1);
+        NLGB_SCALAR(scalar_after_pq(st, o.v[0]));
       }
       if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
-      const double alpha = st->alpha;
-      for (int t = r; t < s.n_tiles; t += k) {
-        double v[2];
-        tile_update_xr(s, t, alpha, v);
-        put_parts(s, t, kSlotXR, v, 2);
-      }
+      ph_update_xr(s, r, k, st->alpha);
       if (!team_sync(bar, k, r, err)) break;
       {
-        double o[2];
-        get_sums<2>(s, kSlotXR, o);
-        NLGB_SCALAR(scalar_after_xr(st, o[0], o[1]));
+        const Sums4 o = sums_of(s, kSlotXR, 2);
+        NLGB_SCALAR(scalar_after_xr(st, o.v[0], o.v[1]));
       }
       ++done_iters;
       if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
-      const double beta = st->beta;
-      for (int t = r; t < s.n_tiles; t += k) tile_update_p(s, t, beta);
+      ph_update_p(s, r, k, st->beta);
       if (!team_sync(bar, k, r, err)) break;
     } else {
       // FP32 PCG iteration with FP64 reliable updates; same phase order as
       // the graph solver: p update, SpMV + p.q, c/r update, [update].
-      {
-        const double beta = st->beta;
-        for (int t = r; t < s.n_tiles; t += k) tile_mx_update_p(s, t, beta);
-        if (!team_sync(bar, k, r, err)) break;
-      }
-      for (int t = r; t < s.n_tiles; t += k) {
-        double v[1];
-        NLGB_TPR_SWITCH(v[0] = tile_mx_spmv_pq<T, true>(s, t));
-        put_parts(s, t, kSlotPQ, v, 1);
-      }
+      ph_mx_update_p(s, r, k, st->beta);
+      if (!team_sync(bar, k, r, err)) break;
+      ph_mx_spmv_pq(s, r, k);
       if (!team_sync(bar, k, r, err)) break;
       {
-        double o[1];
-        get_sums<1>(s, kSlotPQ, o);
-        NLGB_SCALAR(scalar_after_pq(st, o[0]));
+        const Sums4 o = sums_of(s, kSlotPQ, 1);
+        NLGB_SCALAR(scalar_after_pq(st, o.v[0]));
       }
       if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
-      const double alpha = st->alpha;
-      for (int t = r; t < s.n_tiles; t += k) {
-        double v[2];
-        tile_mx_update_cr(s, t, alpha, v);
-        put_parts(s, t, kSlotXR, v, 2);
-      }
+      ph_mx_update_cr(s, r, k, st->alpha);
       if (!team_sync(bar, k, r, err)) break;
       {
-        double o[2];
-        get_sums<2>(s, kSlotXR, o);
-        NLGB_SCALAR(scalar_after_mx_cr(st, o[0], o[1]));
+        const Sums4 o = sums_of(s, kSlotXR, 2);
+        NLGB_SCALAR(scalar_after_mx_cr(st, o.v[0], o.v[1]));
       }
       ++done_iters;
       if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
       if (st->mode == 0) {
         // reliable update: x += c, r = b - A x in FP64, FP32 residual replaced
-        for (int t = r; t < s.n_tiles; t += k) tile_mx_apply(s, t);
+        ph_mx_apply(s, r, k);
         if (!team_sync(bar, k, r, err)) break;
-        for (int t = r; t < s.n_tiles; t += k) {
-          double v[4];
-          NLGB_TPR_SWITCH(tile_mx_outer<T, true>(s, t, v));
-          put_parts(s, t, kSlotInit, v, 4);
-        }
+        ph_mx_outer(s, r, k);
         if (!team_sync(bar, k, r, err)) break;
-        double o[4];
-        get_sums<4>(s, kSlotInit, o);
-        NLGB_SCALAR(scalar_after_outer(st, o[0], o[1], o[2], o[3]);
+        const Sums4 o = sums_of(s, kSlotInit, 4);
+        NLGB_SCALAR(scalar_after_outer(st, o.v[0], o.v[1], o.v[2], o.v[3]);
                     // FP32 cannot track this system: continue it in FP64
                     // from the current x (same rule as the graph solver).
                     if (st->status == ST_STAGNATION && !st->fell_back) {
@@ -264,19 +308,10 @@ __device__ void run_system_once(const SysView& s, SysState* st, int r, int k, Te
   }
   if (st->stage == 2) {
     // final true residual (FP64) of the returned x; x = 0 when b == 0
-    for (int t = r; t < s.n_tiles; t += k) {
-      double v[1] = {0.0};
-      if (st->zero_rhs) {
-        tile_zero_x(s, t);
-      } else {
-        NLGB_TPR_SWITCH(v[0] = tile_true_rr<T, true>(s, t));
-      }
-      put_parts(s, t, kSlotFinal, v, 1);
-    }
+    ph_final(s, r, k, st->zero_rhs != 0);
     if (!team_sync(bar, k, r, err)) { NLGB_SCALAR(st->status = ST_DEVICE_ERR; st->stage = 3); return; }
-    double o[1];
-    get_sums<1>(s, kSlotFinal, o);
-    NLGB_SCALAR(st->rr_true = o[0]; st->stage = 3);
+    const Sums4 o = sums_of(s, kSlotFinal, 1);
+    NLGB_SCALAR(st->rr_true = o.v[0]; st->stage = 3);
   }
 }
 
@@ -402,7 +437,7 @@ static cudaError_t ensure(T*& p, size_t& cap, size_t n) {
 // the single-CTA queue, whose workers get a share of the grid proportional to
 // the small systems' work (at least one, at most one per system).  The large
 // ones, largest first, get teams sized by their share of the remaining CTAs
-// (at least 2, at most one CTA per 2 tiles) until the CTAs run out; the rest
+// (at least 2, at most one CTA per tile) until the CTAs run out; the rest
 // wait in the team queue, from which every team draws (largest first) once
 // its own system is done -- list scheduling, so one mis-estimated system
 // does not leave the other teams idle.
@@ -434,10 +469,15 @@ void BatchRunner::plan(const std::vector<SysView>& views, const std::vector<long
   int cta = 0;
   for (int i : large) {
     const double w = (double)std::max(1LL, work[i]);
-    const int cap = std::min(kBarGroup * kBarMaxGroups, std::max(2, views[i].n_tiles / 2));
+    const int cap = std::min(kBarGroup * kBarMaxGroups, std::max(2, views[i].n_tiles));
     int k = (int)std::min<double>((double)cap, std::max(2.0, std::floor(w / per_cta)));
     if (cta + k > avail) k = avail - cta;     // the last team takes what is left
     if (k < 2) { tqueue_.push_back(i); continue; }
+    // Balanced: the fewest CTAs with the same tiles on the busiest CTA (1,023
+    // tiles on 604 CTAs are 2 on the busiest, as on 512; the other 92 CTAs
+    // would only add barrier and reduction traffic).
+    const int per = (views[i].n_tiles + k - 1) / k;
+    k = std::max(2, (views[i].n_tiles + per - 1) / per);
     TeamDesc td;
     td.cta_begin = cta;
     td.k = k;

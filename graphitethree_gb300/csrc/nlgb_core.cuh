@@ -178,7 +178,9 @@ __device__ __forceinline__ A subwarp_sum(A v) {
 // Row dot product a_row . x with T threads per row.  All 32 lanes of the warp
 // must call it (the shuffles use the full mask); `valid` masks the loads.
 // kCoh: gather x through L2 only (needed when x was written earlier in the
-// same kernel by another CTA, i.e. in the persistent batched kernel).
+// same kernel by another CTA, i.e. in the persistent batched kernel; the
+// read-only path may return stale data there.  L1-cached gathers after the
+// team barrier's acquire measured the same on GB300.)
 // ---------------------------------------------------------------------------
 template <int T, typename VT, typename XT, typename A, bool kCoh = false>
 __device__ __forceinline__ A row_dot(const int* __restrict__ rp, const int* __restrict__ ci,

@@ -128,13 +128,22 @@ struct nlgb_server_s {
 
 namespace {
 
-bool mixed_of(const nlgb_server_s* S) { return S->cfg.precision == NL_GB300_PRECISION_MIXED; }
+// Precision of one request: NL_GB300_PRECISION_AUTO runs square systems in
+// mixed precision and least-squares row submissions (normal equations,
+// kappa(A^T A) = kappa(A)^2, too ill-conditioned for FP32 values on meshes)
+// in FP64 from the start, instead of spending an FP32 phase before the
+// fallback.
+bool req_mixed(const nlgb_server_s* S, const Req& r) {
+  if (S->cfg.precision == NL_GB300_PRECISION_MIXED) return true;
+  if (S->cfg.precision == NL_GB300_PRECISION_AUTO) return !(r.kind == 1 && r.least_squares);
+  return false;
+}
 
-SolveParams params_of(const nlgb_server_s* S) {
+SolveParams params_of(const nlgb_server_s* S, bool mixed) {
   SolveParams p;
   p.eps = S->cfg.eps;
   p.max_iter = S->cfg.max_iter;
-  p.precision = S->cfg.precision;
+  p.precision = mixed ? NL_GB300_PRECISION_MIXED : NL_GB300_PRECISION_DOUBLE;
   p.inner_eps = S->cfg.inner_eps;
   p.max_outer = 100000;
   return p;
@@ -142,7 +151,7 @@ SolveParams params_of(const nlgb_server_s* S) {
 
 // Upload / assemble a request on stream `s` and start its systems.
 bool admit(nlgb_server_s* S, Req* r, cudaStream_t s) {
-  const bool mixed = mixed_of(S);
+  const bool mixed = req_mixed(S, *r);
   cudaError_t e = cudaSuccess;
   if (r->kind == 0) {
     e = crs_upload(r->A, r->n, r->n, r->rp.data(), r->ci.data(), r->va.data(), s);
@@ -181,7 +190,7 @@ bool admit(nlgb_server_s* S, Req* r, cudaStream_t s) {
     S->used = S->used - std::min(S->used, r->bytes) + actual;
     r->bytes = actual;
     r->slots.resize((size_t)r->n_rhs);
-    const SolveParams prm = params_of(S);
+    const SolveParams prm = params_of(S, mixed);
     for (int k = 0; k < r->n_rhs && e == cudaSuccess; ++k) {
       e = r->slots[k].alloc(&r->A, mixed, s);
       if (e != cudaSuccess) break;
@@ -304,7 +313,6 @@ void worker_batched(nlgb_server_s* S) {
     S->fatal = last_error();
     fail_all_waiting(S, "server could not start on the GPU");
   }
-  const bool mixed = mixed_of(S);
   std::vector<SysState> states;
   std::vector<std::pair<Req*, int>> owner;   // system index -> (request, rhs)
   int active_systems = 0;
@@ -412,14 +420,13 @@ void worker_batched(nlgb_server_s* S) {
 void worker_serial(nlgb_server_s* S) {
   cudaStream_t s = nullptr;
   cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
-  const SolveParams prm = params_of(S);
   while (true) {
     if (!intake(S, true)) break;
     if (S->aborting) { fail_all_waiting(S, "server aborted"); continue; }
     if (S->pending.empty()) continue;
     Req* r = S->pending.front();
     S->pending.erase(S->pending.begin());
-    r->bytes = estimate_bytes(*r, mixed_of(S));
+    r->bytes = estimate_bytes(*r, req_mixed(S, *r));
     S->used += r->bytes;
     {
       std::lock_guard<std::mutex> lk(S->mu);
@@ -428,6 +435,7 @@ void worker_serial(nlgb_server_s* S) {
     // Reuse the admission upload/assembly, then solve each right-hand side
     // with the graph-captured single-system solver.
     bool ok = admit(S, r, s);
+    const SolveParams prm = params_of(S, req_mixed(S, *r));
     if (ok) {
       PcgSolver pcg;
       ok = pcg.bind(&r->A, s) == cudaSuccess;
@@ -507,7 +515,8 @@ nlgb_server nlgb_server_create(const nlgb_server_config* cfg) {
   if (cfg) S->cfg = *cfg;
   if (S->cfg.epoch_iters <= 0) S->cfg.epoch_iters = 256;
   if (S->cfg.max_systems <= 0) S->cfg.max_systems = 8192;
-  if (S->cfg.precision != NL_GB300_PRECISION_MIXED && S->cfg.precision != NL_GB300_PRECISION_DOUBLE) {
+  if (S->cfg.precision != NL_GB300_PRECISION_MIXED && S->cfg.precision != NL_GB300_PRECISION_DOUBLE &&
+      S->cfg.precision != NL_GB300_PRECISION_AUTO) {
     set_error("nlgb_server_create: unknown precision");
     delete S;
     return nullptr;
@@ -550,7 +559,7 @@ long long nlgb_server_submit_crs(nlgb_server S, int n, const int* rp, const int*
   if (x0) r->x0.assign(x0, x0 + (size_t)n * n_rhs);
   r->x_out = x_out;
   r->arrival = arrival_s;
-  r->bytes = estimate_bytes(*r, mixed_of(S));
+  r->bytes = estimate_bytes(*r, req_mixed(S, *r));
   return enqueue(S, std::move(r));
 }
 
@@ -591,7 +600,7 @@ long long nlgb_server_submit_rows(nlgb_server S, int least_squares, long long n_
   if (x0) r->x0.assign(x0, x0 + (size_t)n_free * n_rhs);
   r->x_out = x_out;
   r->arrival = arrival_s;
-  r->bytes = estimate_bytes(*r, mixed_of(S));
+  r->bytes = estimate_bytes(*r, req_mixed(S, *r));
   return enqueue(S, std::move(r));
 }
 

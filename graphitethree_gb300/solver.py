@@ -21,7 +21,7 @@ from .systems import RowStream
 
 K = _lib.header_constants()
 PRECISION = {"double": K["NL_GB300_PRECISION_DOUBLE"], "fp64": K["NL_GB300_PRECISION_DOUBLE"],
-             "mixed": K["NL_GB300_PRECISION_MIXED"]}
+             "mixed": K["NL_GB300_PRECISION_MIXED"], "auto": K["NL_GB300_PRECISION_AUTO"]}
 STATUS = {K[n]: n.replace("NL_GB300_STATUS_", "").lower() for n in K if n.startswith("NL_GB300_STATUS_")}
 
 

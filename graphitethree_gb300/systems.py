@@ -263,3 +263,18 @@ def request_stream(n_requests: int, seed: int, rate: float, vmin: int = 1_000,
         out.append(Request(rid=k, kind="lscm" if kinds[k] == 0 else "fairing", nx=side, ny=side,
                            seed=int(rng.integers(0, 2**31 - 1)), arrival=float(t[k])))
     return out
+
+
+def serving_sample(n_requests: int, seed: int, rate: float, vmin: int = 1_000,
+                   vmax: int = 1_000_000):
+    """The requests of request_stream() with their systems: ("rows", RowStream)
+    for LSCM (least-squares rows, one right-hand side) and ("square",
+    SquareSystem) for fairing (L + 1e-2 I, three right-hand sides)."""
+    reqs = request_stream(n_requests, seed, rate, vmin, vmax)
+    objs = []
+    for r in reqs:
+        if r.kind == "lscm":
+            objs.append(("rows", lscm_system(r.nx, r.ny, r.seed)))
+        else:
+            objs.append(("square", fairing_system(r.nx, r.ny, r.seed, lam=1e-2, n_rhs=3)))
+    return reqs, objs

@@ -31,7 +31,8 @@ typedef struct nlgb_matrix_s* nlgb_matrix;
 typedef struct {
     double    eps;            /* stop when ||b-Ax|| <= eps ||b||           */
     long long max_iter;       /* < 0: 5 n                                  */
-    int       precision;      /* NL_GB300_PRECISION_DOUBLE / _MIXED        */
+    int       precision;      /* NL_GB300_PRECISION_DOUBLE / _MIXED (_AUTO
+                                 = _MIXED for a matrix given directly)    */
     double    inner_eps;      /* mixed: reliable-update factor (0.1)       */
     int       max_outer;      /* mixed: cap on reliable updates (100000)   */
 } nlgb_params;
@@ -149,7 +150,9 @@ typedef struct nlgb_server_s* nlgb_server;
 typedef struct {
     size_t    hbm_budget_bytes;  /* admission limit (default 150e9)            */
     int       mode;              /* NLGB_SERVER_BATCHED / NLGB_SERVER_SERIAL    */
-    int       precision;         /* NL_GB300_PRECISION_MIXED (default) / _DOUBLE */
+    int       precision;         /* NL_GB300_PRECISION_MIXED (default) / _DOUBLE /
+                                    _AUTO: FP64 for least-squares row
+                                    submissions, mixed for the others     */
     double    eps;               /* relative residual (default 1e-10)          */
     long long max_iter;          /* < 0: 5 n per system                         */
     double    inner_eps;         /* mixed reliable-update factor (0.1)         */

@@ -73,23 +73,25 @@ def max_threads() -> int:
 
 def dedupe_rows(row_ptr, var, val):
     """Merge repeated variables of a row into their first occurrence (the
-    nlCoefficient semantics of include/nl.h)."""
+    nlCoefficient semantics of include/nl.h).  Vectorised: the entries that
+    survive keep their first-occurrence order within each row, and the
+    repeats of a variable are added left to right (bincount accumulates in
+    index order), exactly as a sequential pass over the row would."""
     row_ptr = np.asarray(row_ptr, np.int64)
-    out_rp = [0]
-    out_var, out_val = [], []
-    for r in range(row_ptr.shape[0] - 1):
-        seen = {}
-        for k in range(row_ptr[r], row_ptr[r + 1]):
-            v = int(var[k])
-            if v in seen:
-                out_val[seen[v]] += float(val[k])
-            else:
-                seen[v] = len(out_var)
-                out_var.append(v)
-                out_val.append(float(val[k]))
-        out_rp.append(len(out_var))
-    return (np.asarray(out_rp, np.int64), np.asarray(out_var, np.int32),
-            np.asarray(out_val, np.float64))
+    var = np.asarray(var, np.int64)
+    val = np.asarray(val, np.float64)
+    n_rows = row_ptr.shape[0] - 1
+    if var.size == 0:
+        return (np.zeros(n_rows + 1, np.int64), np.zeros(0, np.int32), np.zeros(0, np.float64))
+    row = np.repeat(np.arange(n_rows, dtype=np.int64), np.diff(row_ptr))
+    key = row * (int(var.max()) + 1) + var
+    _, first, inv = np.unique(key, return_index=True, return_inverse=True)
+    sums = np.bincount(inv.ravel(), weights=val, minlength=first.shape[0])
+    order = np.argsort(first, kind="stable")
+    keep = first[order]
+    out_rp = np.zeros(n_rows + 1, np.int64)
+    np.cumsum(np.bincount(row[keep], minlength=n_rows), out=out_rp[1:])
+    return out_rp, var[keep].astype(np.int32), sums[order]
 
 
 def assemble(least_squares: bool, row_ptr, col, val, rhs, weight, n_free: int, n_vars: int,

@@ -38,6 +38,11 @@ def test_parameters_roundtrip(ctx):
     assert nl.nlGetIntegerv(nl.NL_MAX_ITERATIONS) == 123
     assert nl.nlGetIntegerv(nl.NL_GB300_PRECISION) == nl.NL_GB300_PRECISION_MIXED
     assert nl.nlGetError() == nl.NL_NO_ERROR
+    nl.nlSolverParameteri(nl.NL_GB300_PRECISION, nl.NL_GB300_PRECISION_AUTO)
+    assert nl.nlGetIntegerv(nl.NL_GB300_PRECISION) == nl.NL_GB300_PRECISION_AUTO
+    nl.nlSolverParameteri(nl.NL_GB300_PRECISION, 7)
+    assert nl.nlGetError() == nl.NL_INVALID_ENUM
+    assert nl.nlGetIntegerv(nl.NL_GB300_PRECISION) == nl.NL_GB300_PRECISION_AUTO
 
 
 def test_bad_parameters_are_rejected(ctx):
