@@ -11,6 +11,10 @@ namespace nlgb {
 // Systems with at least this many tiles are run by multi-CTA teams; smaller
 // ones are popped from the queue by single CTAs.
 constexpr int kLargeTiles = 16;
+// A system alone in the server from this many tiles on is continued on the
+// graph executor (measured on GB300: from ~500 tiles the graph path is faster
+// per iteration than a single-system persistent launch).
+constexpr int kGraphMinTiles = 384;
 
 // Team barrier on monotonic 64-bit arrival counters (never reset within a
 // launch): barrier number e of a team is complete when its counter reaches
@@ -81,6 +85,28 @@ struct SystemSlot {
   // b, x0: host or device vectors of n doubles (x0 may be null: zero start).
   cudaError_t start(const double* b, const double* x0, const SolveParams& prm, cudaStream_t s);
   void release(cudaStream_t s);
+};
+
+// Resumable FP64 PCG continuation, as CUDA graph chunks, of a system whose
+// buffers and device state belong to a SystemSlot (see nlgb_solver.cu).
+class ViewGraph {
+ public:
+  ViewGraph() = default;
+  ~ViewGraph();
+  ViewGraph(const ViewGraph&) = delete;
+  ViewGraph& operator=(const ViewGraph&) = delete;
+  // Queue a chunk of at most `iters` iterations (whole passes of 4) of the
+  // system on stream s; finish() waits for it and stores its time in *ms.
+  cudaError_t run(const SysView& v, long long iters, cudaStream_t s, float* ms);
+  cudaError_t finish(long long iters_before, long long iters_after);
+
+ private:
+  cudaError_t build(const SysView& v);
+  SysView view_{};
+  cudaGraphExec_t exec_ = nullptr;
+  cudaEvent_t e0_ = nullptr, e1_ = nullptr;
+  float* ms_ = nullptr;
+  bool pending_ = false;
 };
 
 // Launches the persistent kernel over a set of resident systems.  Each

@@ -67,6 +67,7 @@ struct __align__(16) SysState {
   int fell_back;               // mixed system continued in FP64 (FP32 could not track it)
   int pad_;
   long long iter_at_fallback;  // FP32 iterations done before the FP64 fallback
+  long long iter_stop;         // > 0: a graph chunk pauses (status unchanged) at this iteration
 };
 
 // Algorithmic HBM bytes of one solve (n rows, z nonzeros), from its final

@@ -66,6 +66,8 @@ struct Req {
   double* d_rhs = nullptr;      // assembled right-hand sides (row streams)
   std::vector<SystemSlot> slots;
   std::vector<int> sys_done;
+  std::vector<int> sys_stage;   // SysState::stage after the last epoch
+  std::vector<long long> sys_iter;
   std::vector<nlgb_result> res;
   double t_done = 0.0;
   int status = NL_GB300_STATUS_NONE;
@@ -211,6 +213,8 @@ bool admit(nlgb_server_s* S, Req* r, cudaStream_t s) {
     return false;
   }
   r->sys_done.assign((size_t)r->n_rhs, 0);
+  r->sys_stage.assign((size_t)r->n_rhs, 0);
+  r->sys_iter.assign((size_t)r->n_rhs, 0);
   r->res.assign((size_t)r->n_rhs, nlgb_result{});
   return true;
 }
@@ -316,6 +320,7 @@ void worker_batched(nlgb_server_s* S) {
   std::vector<SysState> states;
   std::vector<std::pair<Req*, int>> owner;   // system index -> (request, rhs)
   int active_systems = 0;
+  ViewGraph solo;
   auto admit_pending = [&]() {
     // first fit in arrival order
     for (size_t i = 0; i < S->pending.size();) {
@@ -358,16 +363,41 @@ void worker_batched(nlgb_server_s* S) {
         owner.push_back({r, k});
       }
     BatchLaunchStats bst;
-    cudaError_t e = runner.launch(views, work, S->aborting ? 1 : S->cfg.epoch_iters);
-    if (e == cudaSuccess) {
-      // overlap: admit what arrived meanwhile while the epoch runs
-      intake(S, false);
-      admit_pending();
-      e = runner.finish(&bst);
+    // A lone large FP64 system (everything else finished) continues on the
+    // graph executor, which is faster per iteration than the persistent
+    // kernel once one system fills the GPU (same iterates, see ViewGraph).
+    bool graph_epoch = false;
+    if (views.size() == 1 && !S->aborting) {
+      Req* r = owner[0].first;
+      const int k = owner[0].second;
+      graph_epoch = !req_mixed(S, *r) && views[0].n_tiles >= kGraphMinTiles && r->sys_stage[k] == 1;
     }
-    if (e == cudaSuccess) {
-      states.resize(views.size());
-      e = runner.gather_states(states.data(), (int)views.size());
+    cudaError_t e = cudaSuccess;
+    if (graph_epoch) {
+      float gms = 0.f;
+      const long long before = owner[0].first->sys_iter[owner[0].second];
+      e = solo.run(views[0], S->cfg.epoch_iters, sc, &gms);
+      if (e == cudaSuccess) {
+        intake(S, false);
+        admit_pending();
+        states.resize(1);
+        e = cudaMemcpyAsync(states.data(), views[0].st, sizeof(SysState), cudaMemcpyDeviceToHost, sc);
+      }
+      if (e == cudaSuccess) e = cudaStreamSynchronize(sc);
+      if (e == cudaSuccess) e = solo.finish(before, states[0].iter);
+      bst.ms = gms;
+    } else {
+      e = runner.launch(views, work, S->aborting ? 1 : S->cfg.epoch_iters);
+      if (e == cudaSuccess) {
+        // overlap: admit what arrived meanwhile while the epoch runs
+        intake(S, false);
+        admit_pending();
+        e = runner.finish(&bst);
+      }
+      if (e == cudaSuccess) {
+        states.resize(views.size());
+        e = runner.gather_states(states.data(), (int)views.size());
+      }
     }
     if (e != cudaSuccess) {
       S->fatal = last_error();
@@ -381,6 +411,8 @@ void worker_batched(nlgb_server_s* S) {
     for (size_t i = 0; i < views.size(); ++i) {
       Req* r = owner[i].first;
       const int k = owner[i].second;
+      r->sys_stage[k] = states[i].stage;
+      r->sys_iter[k] = states[i].iter;
       if (states[i].stage == 3 || S->aborting) {
         SysState h = states[i];
         if (h.stage != 3) h.status = ST_ABORTED;

@@ -10,6 +10,7 @@
 // scalar during the solve: the loop is a CUDA-graph while-node whose
 // condition is cleared from the device.  A guard kernel counts body passes
 // and clears the condition after a hard cap, so the loop always ends.
+#include "nlgb_batch.h"
 #include "nlgb_core.cuh"
 #include "nlgb_internal.h"
 
@@ -140,7 +141,22 @@ __global__ void k_guard(SysView s, cudaGraphConditionalHandle h, int need_mode, 
     stop = true;
   }
   if (!stop && need_mode >= 0 && st->mode != need_mode) stop = true;
+  // pause of a resumable chunk: the system stays ST_RUNNING
+  if (!stop && st->iter_stop > 0 && st->iter >= st->iter_stop) stop = true;
   if (stop && use_handle) cudaGraphSetConditional(h, 0u);
+}
+
+// Before a resumable chunk of at most `iters` iterations: pause point and a
+// matching cap on while-body passes.
+__global__ void k_chunk_start(SysState* st, long long iters, int unroll) {
+  st->iter_stop = st->iter + iters;
+  st->guard_cap = st->guard + iters / unroll + 4;
+}
+
+// After a chunk: a system that stopped (converged or failed) is done; its
+// true residual was computed by the final kernel of the graph.
+__global__ void k_chunk_end(SysState* st) {
+  if (st->status != ST_RUNNING) st->stage = 3;
 }
 
 // ||b - A x||^2 of the final iterate; zeroes x when b == 0.
@@ -652,6 +668,84 @@ cudaError_t PcgSolver::build_mixed_graph() {
   cudaError_t e = cudaGraphInstantiate(&mixed_exec_, g, 0);
   cudaGraphDestroy(g);
   NLGB_CUDA_TRY(e);
+  return cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------
+// ViewGraph: resumable FP64 PCG continuation of a system whose buffers and
+// state live elsewhere (a SystemSlot of the persistent solver).  Same kernels
+// and order as the plain graph, without the initial residual:
+//   chunk start -> while { (q = A p, p.q ; x, r ; p) x 4 ; guard } -> final
+//   residual -> chunk end.
+// The iterates are those of the persistent kernel (same tile procedures and
+// canonical reductions), so a system may switch between the two executors
+// at any iteration boundary (the graph pauses on whole passes of 4).
+// ---------------------------------------------------------------------------
+ViewGraph::~ViewGraph() {
+  if (exec_) cudaGraphExecDestroy(exec_);
+  if (e0_) cudaEventDestroy(e0_);
+  if (e1_) cudaEventDestroy(e1_);
+}
+
+cudaError_t ViewGraph::build(const SysView& v) {
+  if (exec_) cudaGraphExecDestroy(exec_);
+  exec_ = nullptr;
+  if (!e0_) NLGB_CUDA_TRY(cudaEventCreate(&e0_));
+  if (!e1_) NLGB_CUDA_TRY(cudaEventCreate(&e1_));
+  view_ = v;
+  const KernelSet ks = kernels_for(v.tpr);
+  cudaGraph_t g;
+  NLGB_CUDA_TRY(cudaGraphCreate(&g, 0));
+  cudaGraphConditionalHandle h;
+  NLGB_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault));
+  void* a1[] = {&view_};
+  cudaGraphNode_t n_loop, n_fin, prev = nullptr;
+  cudaGraph_t body;
+  NLGB_CUDA_TRY(add_while(g, &n_loop, nullptr, h, &body));
+  const int vg = (v.n_tiles + vec_tiles_for(v.tile_rows) - 1) / vec_tiles_for(v.tile_rows);
+  for (int u = 0; u < kUnrollPlain; ++u) {
+    cudaGraphNode_t n1, n2, n3;
+    NLGB_CUDA_TRY(add_kernel(body, &n1, prev, ks.spmv, v.n_tiles, kCTA, a1));
+    NLGB_CUDA_TRY(add_kernel(body, &n2, n1, (const void*)k_update_xr, vg, kCTA, a1));
+    NLGB_CUDA_TRY(add_kernel(body, &n3, n2, (const void*)k_update_p, vg, kCTA, a1));
+    prev = n3;
+  }
+  int need_mode = -1, use_handle = 1;
+  void* ag[] = {&view_, &h, &need_mode, &use_handle};
+  cudaGraphNode_t n_g, n_end;
+  NLGB_CUDA_TRY(add_kernel(body, &n_g, prev, (const void*)k_guard, 1, 1, ag));
+  NLGB_CUDA_TRY(add_kernel(g, &n_fin, n_loop, ks.fin, v.n_tiles, kCTA, a1));
+  SysState* st = v.st;
+  void* ae[] = {&st};
+  NLGB_CUDA_TRY(add_kernel(g, &n_end, n_fin, (const void*)k_chunk_end, 1, 1, ae));
+  cudaError_t e = cudaGraphInstantiate(&exec_, g, 0);
+  cudaGraphDestroy(g);
+  NLGB_CUDA_TRY(e);
+  return cudaSuccess;
+}
+
+cudaError_t ViewGraph::run(const SysView& v, long long iters, cudaStream_t s, float* ms) {
+  if (!exec_ || v.st != view_.st || v.x != view_.x || v.n_tiles != view_.n_tiles || v.tpr != view_.tpr)
+    NLGB_CUDA_TRY(build(v));
+  NLGB_CUDA_TRY(cudaEventRecord(e0_, s));
+  k_chunk_start<<<1, 1, 0, s>>>(v.st, std::max(1LL, iters), kUnrollPlain);
+  NLGB_CUDA_TRY(cudaGetLastError());
+  NLGB_CUDA_TRY(cudaGraphLaunch(exec_, s));
+  NLGB_CUDA_TRY(cudaEventRecord(e1_, s));
+  pending_ = true;
+  ms_ = ms;
+  return cudaSuccess;
+}
+
+cudaError_t ViewGraph::finish(long long iters_before, long long iters_after) {
+  if (!pending_) return cudaSuccess;
+  pending_ = false;
+  NLGB_CUDA_TRY(cudaEventSynchronize(e1_));
+  if (ms_) NLGB_CUDA_TRY(cudaEventElapsedTime(ms_, e0_, e1_));
+  // kernels executed: chunk start/end, final residual, and per while-body
+  // pass 3 kernels per unrolled iteration + the guard
+  const long long passes = (std::max(0LL, iters_after - iters_before) + kUnrollPlain - 1) / kUnrollPlain;
+  count_launches(3 + std::max(1LL, passes) * (3LL * kUnrollPlain + 1));
   return cudaSuccess;
 }
 

@@ -135,3 +135,45 @@ def test_auto_precision_least_squares_in_fp64(gpu_ok):
     assert np.array_equal(xa1, xd1) and ia1[0].iterations == id1[0].iterations
     assert all(i.status == "converged" and i.refinement_steps >= 1 for i in ia2)
     assert np.array_equal(xa2, xm2)
+
+
+def test_lone_large_system_continues_on_graph(gpu_ok):
+    """A large FP64 system alone in the server runs its first epoch in the
+    persistent kernel, then continues in CUDA-graph chunks: the result is the
+    same as the graph solver's and the persistent kernel's, bit for bit."""
+    fs = systems.fairing_system(420, 400, seed=21, n_rhs=1)
+    A = solver.Matrix(fs.rp, fs.ci, fs.va)
+    assert A.n // A.tile_rows >= 384
+    x1, i1 = A.solve(fs.rhs[0])
+    xs, infos, _ = solver.batch_solve([A], [fs.rhs[0]])
+    srv = solver.Server(precision="double", epoch_iters=32)
+    t = srv.submit_square(fs)
+    x, infs, _ = srv.wait(t)
+    st = srv.stats()
+    srv.close()
+    assert infs[0].status == "converged" and st["epochs"] >= 3
+    assert infs[0].iterations == i1.iterations == infos[0].iterations
+    assert np.array_equal(x[0], x1) and np.array_equal(x[0], xs[0])
+
+
+def test_switch_back_from_graph_when_requests_arrive(gpu_ok):
+    """A large least-squares system runs alone (graph chunks) until a small
+    request arrives; both then share persistent-kernel epochs.  Each result
+    equals its solve alone."""
+    big = systems.lscm_system(200, 190, seed=31)
+    small = systems.fairing_system(40, 37, seed=32)
+    alone = []
+    for kind, obj in (("rows", big), ("square", small)):
+        srv = solver.Server(precision="auto", epoch_iters=64)
+        x, infs, _ = srv.wait(_submit(srv, kind, obj))
+        alone.append((x.copy(), [i.iterations for i in infs]))
+        srv.close()
+    srv = solver.Server(precision="auto", epoch_iters=64)
+    t1 = _submit(srv, "rows", big, arrival=0.0)
+    t2 = _submit(srv, "square", small, arrival=0.05)
+    for t, (xa, ia) in zip((t1, t2), alone):
+        x, infs, _ = srv.wait(t)
+        assert all(i.status == "converged" for i in infs)
+        assert [i.iterations for i in infs] == ia
+        assert np.array_equal(x, xa)
+    srv.close()
