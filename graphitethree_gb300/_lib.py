@@ -72,7 +72,9 @@ class NlgbServerStats(C.Structure):
                 ("p99_latency_s", C.c_double), ("mean_latency_s", C.c_double),
                 ("max_latency_s", C.c_double), ("solves_per_s", C.c_double), ("wall_s", C.c_double),
                 ("kernel_s", C.c_double), ("epochs", C.c_longlong), ("iterations", C.c_longlong),
-                ("algo_bytes", C.c_double), ("peak_bytes", C.c_size_t), ("budget_bytes", C.c_size_t)]
+                ("algo_bytes", C.c_double), ("peak_bytes", C.c_size_t), ("budget_bytes", C.c_size_t),
+                ("graph_s", C.c_double), ("graph_algo_bytes", C.c_double),
+                ("graph_epochs", C.c_longlong)]
 
 
 _SIGS = {

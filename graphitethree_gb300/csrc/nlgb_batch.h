@@ -102,11 +102,13 @@ class ViewGraph {
 
  private:
   cudaError_t build(const SysView& v);
+  cudaError_t run_eager(cudaStream_t s, long long iters);
   SysView view_{};
   cudaGraphExec_t exec_ = nullptr;
   cudaEvent_t e0_ = nullptr, e1_ = nullptr;
   float* ms_ = nullptr;
   bool pending_ = false;
+  bool eager_counted_ = false;
 };
 
 // Launches the persistent kernel over a set of resident systems.  Each

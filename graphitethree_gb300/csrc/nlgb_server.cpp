@@ -386,6 +386,14 @@ void worker_batched(nlgb_server_s* S) {
       if (e == cudaSuccess) e = cudaStreamSynchronize(sc);
       if (e == cudaSuccess) e = solo.finish(before, states[0].iter);
       bst.ms = gms;
+      if (e == cudaSuccess) {
+        const Req* r = owner[0].first;
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->st.graph_s += gms * 1e-3;
+        S->st.graph_epochs += 1;
+        S->st.graph_algo_bytes +=
+            double(states[0].iter - before) * (12.0 * double(r->A.nnz) + 108.0 * double(r->A.n));
+      }
     } else {
       e = runner.launch(views, work, S->aborting ? 1 : S->cfg.epoch_iters);
       if (e == cudaSuccess) {

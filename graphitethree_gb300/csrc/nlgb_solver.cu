@@ -671,6 +671,8 @@ cudaError_t PcgSolver::build_mixed_graph() {
   return cudaSuccess;
 }
 
+static bool eager_mode();
+
 // ---------------------------------------------------------------------------
 // ViewGraph: resumable FP64 PCG continuation of a system whose buffers and
 // state live elsewhere (a SystemSlot of the persistent solver).  Same kernels
@@ -730,10 +732,46 @@ cudaError_t ViewGraph::run(const SysView& v, long long iters, cudaStream_t s, fl
   NLGB_CUDA_TRY(cudaEventRecord(e0_, s));
   k_chunk_start<<<1, 1, 0, s>>>(v.st, std::max(1LL, iters), kUnrollPlain);
   NLGB_CUDA_TRY(cudaGetLastError());
-  NLGB_CUDA_TRY(cudaGraphLaunch(exec_, s));
+  if (eager_mode()) {
+    NLGB_CUDA_TRY(run_eager(s, iters));
+  } else {
+    NLGB_CUDA_TRY(cudaGraphLaunch(exec_, s));
+  }
   NLGB_CUDA_TRY(cudaEventRecord(e1_, s));
   pending_ = true;
   ms_ = ms;
+  return cudaSuccess;
+}
+
+// Eager mode: the chunk's kernels launched one by one (profiling only).
+cudaError_t ViewGraph::run_eager(cudaStream_t s, long long iters) {
+  const KernelSet ks = kernels_for(view_.tpr);
+  const int vg = (view_.n_tiles + vec_tiles_for(view_.tile_rows) - 1) / vec_tiles_for(view_.tile_rows);
+  const cudaGraphConditionalHandle none = 0;
+  const int need = -1, no_handle = 0;
+  void* a1[] = {&view_};
+  void* ag[] = {&view_, const_cast<cudaGraphConditionalHandle*>(&none), const_cast<int*>(&need),
+                const_cast<int*>(&no_handle)};
+  SysState* st = view_.st;
+  void* ae[] = {&st};
+  int status = ST_RUNNING;
+  long long launched = 0;
+  for (long long pass = 0; pass * kUnrollPlain < std::max(1LL, iters) && status == ST_RUNNING; ++pass) {
+    for (int u = 0; u < kUnrollPlain; ++u) {
+      NLGB_CUDA_TRY(cudaLaunchKernel(ks.spmv, dim3(view_.n_tiles), dim3(kCTA), a1, 0, s));
+      NLGB_CUDA_TRY(cudaLaunchKernel((const void*)k_update_xr, dim3(vg), dim3(kCTA), a1, 0, s));
+      NLGB_CUDA_TRY(cudaLaunchKernel((const void*)k_update_p, dim3(vg), dim3(kCTA), a1, 0, s));
+      launched += 3;
+    }
+    NLGB_CUDA_TRY(cudaLaunchKernel((const void*)k_guard, dim3(1), dim3(1), ag, 0, s));
+    ++launched;
+    NLGB_CUDA_TRY(cudaMemcpyAsync(&status, &st->status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    NLGB_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  NLGB_CUDA_TRY(cudaLaunchKernel(ks.fin, dim3(view_.n_tiles), dim3(kCTA), a1, 0, s));
+  NLGB_CUDA_TRY(cudaLaunchKernel((const void*)k_chunk_end, dim3(1), dim3(1), ae, 0, s));
+  count_launches(launched + 2);
+  eager_counted_ = true;
   return cudaSuccess;
 }
 
@@ -744,6 +782,11 @@ cudaError_t ViewGraph::finish(long long iters_before, long long iters_after) {
   if (ms_) NLGB_CUDA_TRY(cudaEventElapsedTime(ms_, e0_, e1_));
   // kernels executed: chunk start/end, final residual, and per while-body
   // pass 3 kernels per unrolled iteration + the guard
+  if (eager_counted_) {   // run_eager counted its launches (plus the chunk start)
+    eager_counted_ = false;
+    count_launches(1);
+    return cudaSuccess;
+  }
   const long long passes = (std::max(0LL, iters_after - iters_before) + kUnrollPlain - 1) / kUnrollPlain;
   count_launches(3 + std::max(1LL, passes) * (3LL * kUnrollPlain + 1));
   return cudaSuccess;

@@ -171,6 +171,11 @@ typedef struct {
     double    algo_bytes;        /* algorithmic HBM bytes over all systems     */
     size_t    peak_bytes;        /* peak admitted device footprint             */
     size_t    budget_bytes;
+    double    graph_s;           /* part of kernel_s spent in graph chunks (a
+                                    lone large FP64 system continued on the
+                                    single-system graph executor)            */
+    double    graph_algo_bytes;  /* part of algo_bytes: iterations run there   */
+    long long graph_epochs;      /* part of epochs run as graph chunks         */
 } nlgb_server_stats;
 
 void        nlgb_server_default_config(nlgb_server_config* cfg);

@@ -29,6 +29,11 @@ for name, A, b in (("lscm", M, rhs[0]), ("fair", F, fs.rhs[0])):
     for prec in ("double", "mixed"):
         x, info = A.solve(b, precision=prec)
         out[f"{name}_{prec}"] = {"x": x.tolist(), "it": info.iterations, "status": info.status}
+big = systems.fairing_system(420, 400, seed=21, n_rhs=1)
+srv = solver.Server(precision="double", epoch_iters=32)
+xb, ib, _ = srv.wait(srv.submit_square(big))
+srv.close()
+out["server_graph_chunks"] = {"x": xb[0].tolist(), "it": ib[0].iterations, "status": ib[0].status}
 np.save(sys.argv[2], np.array([json.dumps(out)]))
 """
 
@@ -49,3 +54,11 @@ def test_eager_mode_bit_identical(gpu_ok, tmp_path):
             assert e["status"] == info.status == "converged"
             assert e["it"] == info.iterations
             assert np.array_equal(np.array(e["x"]), x)
+    # the server's lone-large-system graph chunks, eager vs graph
+    big = systems.fairing_system(420, 400, seed=21, n_rhs=1)
+    srv = solver.Server(precision="double", epoch_iters=32)
+    xb, ib, _ = srv.wait(srv.submit_square(big))
+    srv.close()
+    e = eager["server_graph_chunks"]
+    assert e["status"] == ib[0].status == "converged" and e["it"] == ib[0].iterations
+    assert np.array_equal(np.array(e["x"]), xb[0])
