@@ -131,6 +131,25 @@ def measure_configs():
         serial += M.solve(b)[1].seconds
     c3["serial_plain_s"] = serial
     out["config3_charts_reduced"] = c3
+    progress("mesh builders")
+    V1, F1 = meshes.height_field(256, 256, seed=1)
+    V2, F2 = meshes.height_field(2048, 2048, seed=2)
+    solver.build_lscm(V1, F1)                       # warm-up (context, kernels)
+    t0 = time.perf_counter()
+    rs1 = systems.lscm_rows(V1, F1)
+    host_lscm = time.perf_counter() - t0
+    _, _, asm1 = solver.assemble(rs1)
+    gl_best = min(solver.build_lscm(V1, F1)[2] for _ in range(3))
+    t0 = time.perf_counter()
+    systems.cotan_laplacian(V2, F2, 1e-2)
+    host_fair = time.perf_counter() - t0
+    gf_best = min(solver.build_fairing(V2, F2, 1e-2)[1] for _ in range(3))
+    out["mesh_builders"] = {
+        "lscm_256": {"gpu_build_s": gl_best, "host_rows_s": host_lscm, "gpu_assembly_of_host_rows_s": asm1,
+                     "triangles": int(F1.shape[0])},
+        "fairing_2048": {"gpu_build_s": gf_best, "host_crs_s": host_fair, "triangles": int(F2.shape[0])},
+        "note": "gpu_build_s: nlgb_build_* on the host clock, mesh upload + rows + assembly; host: numpy "
+                "builders of graphitethree_gb300.systems (single thread)"}
     progress("config 5")
     f5 = systems.fairing_system(1024, 1024, seed=5, lam=1e-4, n_rhs=1, stretch_bands=16, rhs_normal=True)
     A5 = solver.Matrix(f5.rp, f5.ci, f5.va)

@@ -151,6 +151,10 @@ _SIGS = {
                                    C.POINTER(NlgbResult), f64p]),
     "nlgb_assemble": (C.c_int, [C.c_int, C.c_longlong, i64p, i32p, f64p, f64p, f64p, C.c_int,
                                 C.c_int, f64p, C.c_int, C.POINTER(C.c_void_p), f64p, f64p]),
+    "nlgb_build_lscm": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.POINTER(C.c_void_p), C.c_void_p, f64p]),
+    "nlgb_build_fairing": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_double,
+                                     C.POINTER(C.c_void_p), f64p]),
     "nlgb_server_default_config": (None, [C.POINTER(NlgbServerConfig)]),
     "nlgb_server_create": (C.c_void_p, [C.POINTER(NlgbServerConfig)]),
     "nlgb_server_reset_clock": (None, [C.c_void_p]),

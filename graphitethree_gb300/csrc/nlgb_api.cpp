@@ -397,4 +397,59 @@ int nlgb_assemble(int least_squares, long long n_rows, const long long* row_ptr,
   return NLGB_OK;
 }
 
+int nlgb_build_lscm(int n_verts, const double* xyz, int n_tris, const int* tris, const int* pins,
+                    const double* pin_uv, nlgb_matrix* A_out, double* rhs_out, double* seconds) {
+  if (!A_out) return fail(NLGB_E_INVALID, "nlgb_build_lscm: bad arguments");
+  *A_out = nullptr;
+  if (n_verts < 3 || n_tris < 0 || !xyz || (n_tris > 0 && !tris))
+    return fail(NLGB_E_INVALID, "nlgb_build_lscm: bad arguments");
+  const int pv[2] = {pins ? pins[0] : 0, pins ? pins[1] : n_verts - 1};
+  const double uv[4] = {pin_uv ? pin_uv[0] : 0.0, pin_uv ? pin_uv[1] : 0.0,
+                        pin_uv ? pin_uv[2] : 1.0, pin_uv ? pin_uv[3] : 1.0};
+  if (pv[0] < 0 || pv[0] >= n_verts || pv[1] < 0 || pv[1] >= n_verts || pv[0] == pv[1])
+    return fail(NLGB_E_INVALID, "nlgb_build_lscm: the two pins must be distinct vertices");
+  if (!ensure_ready()) return NLGB_E_DEVICE;
+  nlgb_matrix M = new nlgb_matrix_s();
+  if (matrix_stream(M) != cudaSuccess) { delete M; return NLGB_E_DEVICE; }
+  cudaStream_t s = M->stream;
+  const int n_free = 2 * n_verts - 4;
+  double* drhs = nullptr;
+  if (cudaMalloc(&drhs, sizeof(double) * (size_t)std::max(1, n_free)) != cudaSuccess) { delete M; return NLGB_E_DEVICE; }
+  const auto t0 = std::chrono::steady_clock::now();
+  bool bad = false;
+  cudaError_t e = build_lscm_system(n_verts, xyz, n_tris, tris, pv, uv, M->A, drhs, s, &bad);
+  if (e == cudaSuccess && !bad) e = crs_prepare(M->A, false, s);
+  if (e == cudaSuccess && !bad) e = cudaStreamSynchronize(s);
+  if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (e == cudaSuccess && !bad && rhs_out)
+    e = cudaMemcpy(rhs_out, drhs, sizeof(double) * (size_t)n_free, cudaMemcpyDefault);
+  cudaFree(drhs);
+  if (bad) { delete M; return fail(NLGB_E_INVALID, "nlgb_build_lscm: triangle index out of range"); }
+  if (e != cudaSuccess) { delete M; return fail(NLGB_E_DEVICE, cudaGetErrorString(e)); }
+  *A_out = M;
+  return NLGB_OK;
+}
+
+int nlgb_build_fairing(int n_verts, const double* xyz, int n_tris, const int* tris, double lambda,
+                       nlgb_matrix* A_out, double* seconds) {
+  if (!A_out) return fail(NLGB_E_INVALID, "nlgb_build_fairing: bad arguments");
+  *A_out = nullptr;
+  if (n_verts < 1 || n_tris < 0 || !xyz || (n_tris > 0 && !tris) || !(lambda >= 0.0))
+    return fail(NLGB_E_INVALID, "nlgb_build_fairing: bad arguments");
+  if (!ensure_ready()) return NLGB_E_DEVICE;
+  nlgb_matrix M = new nlgb_matrix_s();
+  if (matrix_stream(M) != cudaSuccess) { delete M; return NLGB_E_DEVICE; }
+  cudaStream_t s = M->stream;
+  const auto t0 = std::chrono::steady_clock::now();
+  bool bad = false;
+  cudaError_t e = build_fairing_system(n_verts, xyz, n_tris, tris, lambda, M->A, s, &bad);
+  if (e == cudaSuccess && !bad) e = crs_prepare(M->A, false, s);
+  if (e == cudaSuccess && !bad) e = cudaStreamSynchronize(s);
+  if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (bad) { delete M; return fail(NLGB_E_INVALID, "nlgb_build_fairing: triangle index out of range"); }
+  if (e != cudaSuccess) { delete M; return fail(NLGB_E_DEVICE, cudaGetErrorString(e)); }
+  *A_out = M;
+  return NLGB_OK;
+}
+
 }  // extern "C"

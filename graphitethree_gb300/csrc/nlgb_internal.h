@@ -148,6 +148,16 @@ cudaError_t assemble_normal_equations(const LSRowsDevice& rows, DeviceCRS& out,
 cudaError_t assemble_square(const LSRowsDevice& rows, DeviceCRS& out, double* rhs_out,
                             cudaStream_t s);
 
+// Mesh system builders (nlgb_build.cu).  Vertices xyz (n_verts x 3) and
+// triangles (n_tris x 3) may be host or device arrays; *bad_input is set
+// (and nothing built) when a triangle index is out of range.
+cudaError_t build_lscm_system(int n_verts, const double* xyz, int n_tris, const int* tris,
+                              const int pins[2], const double pin_uv[4], DeviceCRS& out,
+                              double* rhs_out /* 2 n_verts - 4, device */, cudaStream_t s,
+                              bool* bad_input);
+cudaError_t build_fairing_system(int n_verts, const double* xyz, int n_tris, const int* tris,
+                                 double lambda, DeviceCRS& out, cudaStream_t s, bool* bad_input);
+
 // Device BLAS-1 (FP64).
 cudaError_t dev_dot(const double* x, const double* y, long long n, double* out_host, cudaStream_t s);
 cudaError_t dev_axpy(long long n, double a, const double* x, double* y, cudaStream_t s);

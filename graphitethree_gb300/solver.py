@@ -287,6 +287,38 @@ def assemble(rs: RowStream):
     return Matrix(None, None, None, _handle=h.value), out[:, :n_free], secs.value
 
 
+def build_lscm(V, F, pins=None, pin_uv=None):
+    """LSCM system of a triangle mesh built on the GPU (nlgb_build_lscm):
+    returns (Matrix over the 2 nv - 4 free variables, rhs, seconds)."""
+    L = _lib.load()
+    V = np.ascontiguousarray(V, np.float64)
+    F = np.ascontiguousarray(F, np.int32)
+    nv = V.shape[0]
+    pins_a = None if pins is None else np.ascontiguousarray(pins, np.int32)
+    uv_a = None if pin_uv is None else np.ascontiguousarray(pin_uv, np.float64).reshape(4)
+    rhs = np.empty(max(1, 2 * nv - 4), np.float64)
+    h = ctypes.c_void_p()
+    secs = ctypes.c_double()
+    _check(L.nlgb_build_lscm(nv, V.ctypes.data, F.shape[0], F.ctypes.data if F.size else None,
+                             None if pins_a is None else pins_a.ctypes.data,
+                             None if uv_a is None else uv_a.ctypes.data, ctypes.byref(h),
+                             rhs.ctypes.data, ctypes.byref(secs)), "nlgb_build_lscm")
+    return Matrix(None, None, None, _handle=h.value), rhs[: 2 * nv - 4], secs.value
+
+
+def build_fairing(V, F, lam: float):
+    """Cotangent Laplacian + lam I of a triangle mesh built on the GPU
+    (nlgb_build_fairing): returns (Matrix, seconds)."""
+    L = _lib.load()
+    V = np.ascontiguousarray(V, np.float64)
+    F = np.ascontiguousarray(F, np.int32)
+    h = ctypes.c_void_p()
+    secs = ctypes.c_double()
+    _check(L.nlgb_build_fairing(V.shape[0], V.ctypes.data, F.shape[0], F.ctypes.data if F.size else None,
+                                float(lam), ctypes.byref(h), ctypes.byref(secs)), "nlgb_build_fairing")
+    return Matrix(None, None, None, _handle=h.value), secs.value
+
+
 def solve_opennl(rs: RowStream, precision: str = "double", eps: float = 1e-10,
                  max_iter: int | None = None, per_call: bool = False):
     """Run the OpenNL context sequence on a row stream; returns (values

@@ -69,6 +69,26 @@ int         nlgb_matrix_info(nlgb_matrix A, int* n_rows, long long* nnz, int* th
 /* Override the autotuner (threads_per_row in {1,2,4,8,16,32}, tile_rows a
  * multiple of 64 in [64, 2^20]; 0 keeps the current value). */
 int         nlgb_matrix_set_layout(nlgb_matrix A, int threads_per_row, int tile_rows);
+/* Mesh system builders on the GPU.  Replace the host-side row emission of
+ * Graphite's mesh_compute_LSCM and mesh_smooth commands (reference:
+ * src/lib/OGF/mesh/commands/mesh_grob_surface_commands.cpp:759 and :703,
+ * whose builders emit rows through nlBegin(NL_ROW)/nlCoefficient): one GPU
+ * thread per triangle writes the rows, then the normal-equation assembly of
+ * nlgb_assemble builds the system.  xyz: n_verts x 3 doubles, tris:
+ * n_tris x 3 vertex indices (host or device arrays).
+ *
+ * LSCM: variables u_k = 2k, v_k = 2k + 1; the two pinned vertices (pins, or
+ * NULL for 0 and n_verts - 1) are locked at pin_uv = (u0, v0, u1, v1) (NULL:
+ * (0, 0) and (1, 1)); the matrix is over the 2 n_verts - 4 free variables and
+ * rhs_out (host or device, may be NULL) receives the right-hand side.
+ * Fairing: the cotangent Laplacian + lambda I (L_ij = -(cot a + cot b) / 2).
+ * An out-of-range triangle index returns NLGB_E_INVALID.  *seconds: build
+ * time on the host clock (may be NULL). */
+int         nlgb_build_lscm(int n_verts, const double* xyz, int n_tris, const int* tris,
+                            const int* pins, const double* pin_uv, nlgb_matrix* A_out,
+                            double* rhs_out, double* seconds);
+int         nlgb_build_fairing(int n_verts, const double* xyz, int n_tris, const int* tris,
+                               double lambda, nlgb_matrix* A_out, double* seconds);
 /* Copy the CRS arrays back to host buffers of size n+1 / nnz / nnz. */
 int         nlgb_matrix_download(nlgb_matrix A, int* rp, int* ci, double* va);
 /* Jacobi inverse diagonal (host buffer of n doubles). */
