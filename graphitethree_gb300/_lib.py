@@ -155,6 +155,9 @@ _SIGS = {
                                   C.POINTER(C.c_void_p), C.c_void_p, f64p]),
     "nlgb_build_fairing": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_double,
                                      C.POINTER(C.c_void_p), f64p]),
+    "nlgb_server_submit_mesh": (C.c_longlong, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int,
+                                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int,
+                                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]),
     "nlgb_server_default_config": (None, [C.POINTER(NlgbServerConfig)]),
     "nlgb_server_create": (C.c_void_p, [C.POINTER(NlgbServerConfig)]),
     "nlgb_server_reset_clock": (None, [C.c_void_p]),

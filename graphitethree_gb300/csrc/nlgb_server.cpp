@@ -44,7 +44,7 @@ enum ReqState { R_FUTURE, R_PENDING, R_ACTIVE, R_DONE, R_FAILED };
 
 struct Req {
   long long id = 0;
-  int kind = 0;                 // 0: CRS, 1: row stream
+  int kind = 0;                 // 0: CRS, 1: row stream, 2: mesh (built on the GPU)
   int least_squares = 1;
   int n = 0;                    // unknowns per system
   int n_rhs = 1;
@@ -57,6 +57,14 @@ struct Req {
   std::vector<double> val, rhs, weight, xl;
   int n_vars = 0;
   bool has_weight = false, has_rhs = false, has_xl = false;
+  // mesh requests
+  int mesh_kind = 0;            // NLGB_MESH_LSCM / NLGB_MESH_FAIRING
+  int n_verts = 0, n_tris = 0;
+  std::vector<double> xyz;
+  std::vector<int> tris;
+  int pins[2] = {0, 0};
+  double pin_uv[4] = {0.0, 0.0, 1.0, 1.0};
+  double lambda = 0.0;
   double* x_out = nullptr;
   double arrival = 0.0;
   // runtime
@@ -88,6 +96,14 @@ size_t estimate_bytes(const Req& r, bool mixed) {
   size_t nnz = 0, upload = 0;
   if (r.kind == 0) {
     nnz = (size_t)r.rp[r.n];
+  } else if (r.kind == 2) {
+    // LSCM normal matrix ~14 nonzeros per row, Laplacian ~7; the device row
+    // stream of the build (12 B per coefficient + weights) is counted too
+    const bool lscm = r.mesh_kind == NLGB_MESH_LSCM;
+    nnz = (size_t)r.n * (lscm ? 16 : 8);
+    const size_t coefs = lscm ? 12 * (size_t)r.n_tris : 6 * (size_t)r.n_tris + (size_t)r.n_verts;
+    upload = (size_t)r.n_verts * 24 + (size_t)r.n_tris * 12 + coefs * 12 + coefs * 8 +
+             (size_t)r.n * 8 * r.n_rhs;
   } else {
     // normal-matrix nonzeros: about half the row-merge candidates
     double cand = 0.0;
@@ -137,7 +153,8 @@ namespace {
 // fallback.
 bool req_mixed(const nlgb_server_s* S, const Req& r) {
   if (S->cfg.precision == NL_GB300_PRECISION_MIXED) return true;
-  if (S->cfg.precision == NL_GB300_PRECISION_AUTO) return !(r.kind == 1 && r.least_squares);
+  if (S->cfg.precision == NL_GB300_PRECISION_AUTO)
+    return !((r.kind == 1 && r.least_squares) || (r.kind == 2 && r.mesh_kind == NLGB_MESH_LSCM));
   return false;
 }
 
@@ -157,6 +174,25 @@ bool admit(nlgb_server_s* S, Req* r, cudaStream_t s) {
   cudaError_t e = cudaSuccess;
   if (r->kind == 0) {
     e = crs_upload(r->A, r->n, r->n, r->rp.data(), r->ci.data(), r->va.data(), s);
+  } else if (r->kind == 2) {
+    // build the system from the mesh on the GPU (right-hand sides: LSCM's
+    // from the pins, fairing's given by the caller)
+    bool bad = false;
+    e = cudaMalloc(&r->d_rhs, sizeof(double) * std::max<size_t>(1, (size_t)r->n_rhs * r->n));
+    if (e == cudaSuccess && r->mesh_kind == NLGB_MESH_LSCM) {
+      e = build_lscm_system(r->n_verts, r->xyz.data(), r->n_tris, r->tris.data(), r->pins, r->pin_uv,
+                            r->A, r->d_rhs, s, &bad);
+    } else if (e == cudaSuccess) {
+      e = build_fairing_system(r->n_verts, r->xyz.data(), r->n_tris, r->tris.data(), r->lambda, r->A, s,
+                               &bad);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(r->d_rhs, r->b.data(), sizeof(double) * (size_t)r->n_rhs * r->n,
+                            cudaMemcpyHostToDevice, s);
+    }
+    if (e == cudaSuccess && bad) {
+      set_error("nlgb_server_submit_mesh: triangle index out of range");
+      e = cudaErrorInvalidValue;
+    }
   } else {
     long long* drp = nullptr; int* dcol = nullptr;
     double *dval = nullptr, *drhs = nullptr, *dw = nullptr, *dxl = nullptr;
@@ -208,6 +244,7 @@ bool admit(nlgb_server_s* S, Req* r, cudaStream_t s) {
   std::vector<long long>().swap(r->row_ptr); std::vector<int>().swap(r->col);
   std::vector<double>().swap(r->val); std::vector<double>().swap(r->rhs);
   std::vector<double>().swap(r->weight); std::vector<double>().swap(r->xl);
+  std::vector<double>().swap(r->xyz); std::vector<int>().swap(r->tris);
   if (e != cudaSuccess) {
     r->error = std::string("admission failed: ") + last_error();
     return false;
@@ -597,6 +634,51 @@ long long nlgb_server_submit_crs(nlgb_server S, int n, const int* rp, const int*
   r->va.assign(va, va + nnz);
   r->b.assign(b, b + (size_t)n * n_rhs);
   if (x0) r->x0.assign(x0, x0 + (size_t)n * n_rhs);
+  r->x_out = x_out;
+  r->arrival = arrival_s;
+  r->bytes = estimate_bytes(*r, req_mixed(S, *r));
+  return enqueue(S, std::move(r));
+}
+
+long long nlgb_server_submit_mesh(nlgb_server S, int mesh_kind, int n_verts, const double* xyz,
+                                  int n_tris, const int* tris, const int* pins, const double* pin_uv,
+                                  double lambda, int n_rhs, const double* b, const double* x0,
+                                  double* x_out, double arrival_s) {
+  const bool lscm = mesh_kind == NLGB_MESH_LSCM;
+  if (!S || (mesh_kind != NLGB_MESH_LSCM && mesh_kind != NLGB_MESH_FAIRING) || n_verts < 3 ||
+      n_tris < 0 || !xyz || (n_tris > 0 && !tris) || !x_out || n_rhs < 1 || (lscm && n_rhs != 1) ||
+      (!lscm && (!b || !(lambda >= 0.0)))) {
+    set_error("nlgb_server_submit_mesh: bad arguments");
+    return NLGB_E_INVALID;
+  }
+  for (long long k = 0; k < 3LL * n_tris; ++k)
+    if (tris[k] < 0 || tris[k] >= n_verts) {
+      set_error("nlgb_server_submit_mesh: triangle index out of range");
+      return NLGB_E_INVALID;
+    }
+  auto r = std::make_unique<Req>();
+  r->kind = 2;
+  r->mesh_kind = mesh_kind;
+  r->least_squares = lscm ? 1 : 0;
+  r->n_verts = n_verts;
+  r->n_tris = n_tris;
+  r->xyz.assign(xyz, xyz + 3 * (size_t)n_verts);
+  r->tris.assign(tris, tris + 3 * (size_t)n_tris);
+  if (lscm) {
+    r->pins[0] = pins ? pins[0] : 0;
+    r->pins[1] = pins ? pins[1] : n_verts - 1;
+    if (pin_uv) std::memcpy(r->pin_uv, pin_uv, sizeof(r->pin_uv));
+    if (r->pins[0] < 0 || r->pins[0] >= n_verts || r->pins[1] < 0 || r->pins[1] >= n_verts ||
+        r->pins[0] == r->pins[1]) {
+      set_error("nlgb_server_submit_mesh: the two pins must be distinct vertices");
+      return NLGB_E_INVALID;
+    }
+  }
+  r->lambda = lambda;
+  r->n = lscm ? 2 * n_verts - 4 : n_verts;
+  r->n_rhs = n_rhs;
+  if (!lscm) r->b.assign(b, b + (size_t)n_rhs * r->n);
+  if (x0) r->x0.assign(x0, x0 + (size_t)n_rhs * r->n);
   r->x_out = x_out;
   r->arrival = arrival_s;
   r->bytes = estimate_bytes(*r, req_mixed(S, *r));

@@ -230,6 +230,32 @@ class Server:
         self._out[t] = out
         return t
 
+    def submit_mesh(self, kind: str, V, F, b=None, lam: float = 1e-2, pins=None, pin_uv=None,
+                    arrival: float = -1.0) -> int:
+        """A triangle mesh whose system the server builds on the GPU:
+        kind "lscm" (b must be None) or "fairing" (b: (n_rhs, nv))."""
+        L = _lib.load()
+        K = _lib.header_constants()
+        V = np.ascontiguousarray(V, np.float64)
+        F = np.ascontiguousarray(F, np.int32)
+        nv = V.shape[0]
+        lscm = kind == "lscm"
+        n = 2 * nv - 4 if lscm else nv
+        bb = None if b is None else np.ascontiguousarray(np.atleast_2d(b), np.float64)
+        k = 1 if lscm else bb.shape[0]
+        out = np.empty((k, n), np.float64)
+        pins_a = None if pins is None else np.ascontiguousarray(pins, np.int32)
+        uv_a = None if pin_uv is None else np.ascontiguousarray(pin_uv, np.float64).reshape(4)
+        t = L.nlgb_server_submit_mesh(
+            self._h, K["NLGB_MESH_LSCM"] if lscm else K["NLGB_MESH_FAIRING"], nv, V.ctypes.data,
+            F.shape[0], F.ctypes.data if F.size else None,
+            None if pins_a is None else pins_a.ctypes.data, None if uv_a is None else uv_a.ctypes.data,
+            float(lam), k, None if bb is None else bb.ctypes.data, None, out.ctypes.data, float(arrival))
+        if t < 0:
+            raise SolverError(f"submit failed ({t}): {_lib.last_error()}")
+        self._out[t] = out
+        return t
+
     def wait(self, ticket: int):
         """Returns (solutions (n_rhs, n), [SolveInfo], latency_s)."""
         out = self._out[ticket]

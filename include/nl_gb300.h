@@ -220,6 +220,21 @@ long long   nlgb_server_submit_rows(nlgb_server srv, int least_squares, long lon
                                     const double* rhs, const double* weight, int n_free,
                                     int n_vars, const double* xl, int n_rhs, const double* x0,
                                     double* x_out, double arrival_s);
+/* A triangle mesh whose system the server builds on the GPU at admission
+ * (nlgb_build_lscm / nlgb_build_fairing).  NLGB_MESH_LSCM: one system over
+ * the 2 n_verts - 4 free variables (pins / pin_uv as in nlgb_build_lscm,
+ * NULL for the defaults), n_rhs must be 1 and b NULL.  NLGB_MESH_FAIRING:
+ * L + lambda I over n_verts variables, b holds n_rhs * n_verts right-hand
+ * sides.  x0 (may be NULL) and x_out hold n_rhs * n values.  Reference: the
+ * solve of mesh_compute_LSCM / mesh_smooth
+ * (src/lib/OGF/mesh/commands/mesh_grob_surface_commands.cpp:759, :703). */
+#define NLGB_MESH_LSCM    0
+#define NLGB_MESH_FAIRING 1
+long long   nlgb_server_submit_mesh(nlgb_server srv, int mesh_kind, int n_verts, const double* xyz,
+                                    int n_tris, const int* tris, const int* pins,
+                                    const double* pin_uv, double lambda, int n_rhs,
+                                    const double* b, const double* x0, double* x_out,
+                                    double arrival_s);
 /* Block until the ticket completes; res: n_rhs entries (may be NULL). */
 int         nlgb_server_wait(nlgb_server srv, long long ticket, nlgb_result* res,
                              double* latency_s);

@@ -114,3 +114,37 @@ def test_builders_reject_bad_input(gpu_ok):
         solver.build_fairing(V, bad, 1e-2)
     with pytest.raises(solver.SolverError):
         solver.build_lscm(V, F, pins=(4, 4))
+
+
+@pytest.mark.parametrize("precision", ["auto", "mixed"])
+def test_server_mesh_requests(gpu_ok, precision):
+    """Mesh submissions: the server builds the systems on the GPU at
+    admission; the results equal the builder + single-system solve, bit for
+    bit (same matrix bits, same iterates), LSCM in FP64 under AUTO."""
+    V1, F1 = meshes.height_field(36, 30, seed=11)
+    V2, F2 = meshes.height_field(44, 40, seed=12)
+    fs = systems.fairing_system(44, 40, seed=12, n_rhs=2)
+    srv = solver.Server(precision=precision, epoch_iters=64)
+    t1 = srv.submit_mesh("lscm", V1, F1)
+    t2 = srv.submit_mesh("fairing", V2, F2, b=fs.rhs, lam=1e-2)
+    x1, i1, _ = srv.wait(t1)
+    x2, i2, _ = srv.wait(t2)
+    srv.close()
+    M1, rhs1, _ = solver.build_lscm(V1, F1)
+    M2, _ = solver.build_fairing(V2, F2, 1e-2)
+    p1 = "double" if precision == "auto" else "mixed"
+    xs1, is1 = M1.solve(rhs1, precision=p1)
+    assert i1[0].status == "converged" and np.array_equal(x1[0], xs1)
+    if precision == "auto":
+        assert i1[0].refinement_steps == 0
+    for k in range(2):
+        xs2, is2 = M2.solve(fs.rhs[k], precision="mixed")
+        assert i2[k].status == "converged" and np.array_equal(x2[k], xs2)
+    with pytest.raises(solver.SolverError):
+        srv2 = solver.Server(precision=precision)
+        bad = F1.copy()
+        bad[0, 0] = -1
+        try:
+            srv2.submit_mesh("lscm", V1, bad)
+        finally:
+            srv2.close()
