@@ -81,19 +81,35 @@ def nlMatrixCompress(M: int) -> int:
     return h.value
 
 
-def nlMultMatrixVector(M: int, x: np.ndarray, y: np.ndarray) -> None:
-    x = np.ascontiguousarray(x, np.float64)
-    assert y.dtype == np.float64 and y.flags.c_contiguous
-    _L().nlMultMatrixVector(M, x.ctypes.data_as(_lib.f64p), y.ctypes.data_as(_lib.f64p))
+def _vec_ptr(a, writable: bool):
+    """Pointer to an FP64 vector: a numpy array (host) or any CUDA array
+    exposing __cuda_array_interface__ (device; passed to the library as is,
+    no staging).  Returns (pointer, keep-alive object)."""
+    cai = getattr(a, "__cuda_array_interface__", None)
+    if cai is not None:
+        if cai["typestr"] != "<f8" or len(cai["shape"]) != 1 or cai.get("strides") not in (None, (8,)):
+            raise ValueError("device vectors must be contiguous 1-D float64")
+        return ctypes.cast(ctypes.c_void_p(cai["data"][0]), _lib.f64p), a
+    if writable:
+        assert a.dtype == np.float64 and a.flags.c_contiguous
+        return a.ctypes.data_as(_lib.f64p), a
+    h = np.ascontiguousarray(a, np.float64)
+    return h.ctypes.data_as(_lib.f64p), h
 
 
-def nlSolveSystemIterative(blas, M, P, b: np.ndarray, x: np.ndarray, solver: int, eps: float,
+def nlMultMatrixVector(M: int, x, y) -> None:
+    """y = M x; x and y are host (numpy) or device (CUDA array) vectors."""
+    px, kx = _vec_ptr(x, False)
+    py, ky = _vec_ptr(y, True)
+    _L().nlMultMatrixVector(M, px, py)
+
+
+def nlSolveSystemIterative(blas, M, P, b, x, solver: int, eps: float,
                            max_iter: int, inner_iter: int = 5) -> int:
-    b = np.ascontiguousarray(b, np.float64)
-    assert x.dtype == np.float64 and x.flags.c_contiguous
-    return _L().nlSolveSystemIterative(blas, M, P, b.ctypes.data_as(_lib.f64p),
-                                       x.ctypes.data_as(_lib.f64p), solver, eps, max_iter,
-                                       inner_iter)
+    """b and x are host (numpy) or device (CUDA array) vectors."""
+    pb, kb = _vec_ptr(b, False)
+    px, kx = _vec_ptr(x, True)
+    return _L().nlSolveSystemIterative(blas, M, P, pb, px, solver, eps, max_iter, inner_iter)
 
 
 # ---- bulk helpers (nl_gb300.h) -------------------------------------------

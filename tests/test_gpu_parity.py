@@ -275,6 +275,38 @@ def test_scripting_matrix_api(gpu_ok, oracle_mod):
     nl.nlDeleteMatrix(M)
 
 
+def test_scripting_matrix_api_device_vectors(gpu_ok):
+    """The same scripting calls with device-resident vectors
+    (graphitethree_gb300.nlvector.Vector, __cuda_array_interface__): no
+    staging, results identical to the host-vector calls."""
+    pytest.importorskip("torch")
+    from graphitethree_gb300.nlvector import Vector
+    fs = systems.fairing_system(30, 27, seed=10)
+    M = nl.nlSparseMatrixNew(fs.n, fs.n, nl.NL_MATRIX_STORE_ROWS)
+    for i in range(fs.n):
+        for k in range(fs.rp[i], fs.rp[i + 1]):
+            nl.nlSparseMatrixAdd(M, i, int(fs.ci[k]), float(fs.va[k]))
+    M = nl.nlMatrixCompress(M)
+    x = np.random.default_rng(1).normal(size=fs.n)
+    y_host = np.zeros(fs.n)
+    nl.nlMultMatrixVector(M, x, y_host)
+    xd, yd = Vector(x), Vector(fs.n)
+    nl.nlMultMatrixVector(M, xd, yd)
+    assert np.array_equal(yd.numpy(), y_host)
+    P = nl.nlNewJacobiPreconditioner(M)
+    sol_host = np.zeros(fs.n)
+    it_h = nl.nlSolveSystemIterative(nl.nlHostBlas(), M, P, fs.rhs[0], sol_host, nl.NL_CG, 1e-10,
+                                     5 * fs.n, 5)
+    bd, sd = Vector(fs.rhs[0]), Vector(fs.n)
+    it_d = nl.nlSolveSystemIterative(nl.nlHostBlas(), M, P, bd, sd, nl.NL_CG, 1e-10, 5 * fs.n, 5)
+    assert it_d == it_h and np.array_equal(sd.numpy(), sol_host)
+    with pytest.raises(ValueError):
+        import torch
+        nl.nlMultMatrixVector(M, torch.zeros(fs.n, dtype=torch.float32, device="cuda"), yd)
+    nl.nlDeleteMatrix(P)
+    nl.nlDeleteMatrix(M)
+
+
 def test_blas_table(gpu_ok):
     import ctypes
     from graphitethree_gb300 import _lib
