@@ -104,6 +104,7 @@ struct Context {
   bool least_squares = false;
   NLenum solver = NL_SOLVER_DEFAULT;
   NLenum precond = NL_PRECOND_JACOBI;
+  int inner_iterations = 5;     // GMRES restart length (NL_INNER_ITERATIONS)
   double threshold = 1e-10;
   long long max_iterations = -1;
   int nb_systems = 1;
@@ -400,7 +401,10 @@ void nlSolverParameteri(NLenum pname, NLint param) {
       if (param < 0) { nl_error(NL_INVALID_VALUE, "NL_MAX_ITERATIONS must be >= 0"); return; }
       c->max_iterations = param; break;
     case NL_SYMMETRIC: c->symmetric = param != 0; break;
-    case NL_INNER_ITERATIONS: break;   // restart length of GMRES: unused by CG
+    case NL_INNER_ITERATIONS:          // restart length of GMRES
+      if (param < 1) { nl_error(NL_INVALID_VALUE, "NL_INNER_ITERATIONS must be >= 1"); return; }
+      c->inner_iterations = param;
+      break;
     case NL_PRECONDITIONER:
       if (param != (NLint)NL_PRECOND_JACOBI && param != (NLint)NL_PRECOND_NONE &&
           param != (NLint)NL_PRECOND_SSOR) { nl_error(NL_INVALID_ENUM, "unknown NL_PRECONDITIONER"); return; }
@@ -429,6 +433,7 @@ void nlGetIntegerv(NLenum pname, NLint* params) {
   if (!c || !params) return;
   switch (pname) {
     case NL_SOLVER: *params = (NLint)c->solver; break;
+    case NL_INNER_ITERATIONS: *params = (NLint)c->inner_iterations; break;
     case NL_NB_VARIABLES: *params = (NLint)c->nb_variables; break;
     case NL_NB_SYSTEMS: *params = c->nb_systems; break;
     case NL_LEAST_SQUARES: *params = c->least_squares; break;
@@ -702,6 +707,66 @@ void nlRowScaling(NLdouble value) {
   c->cur_scale = value;
 }
 
+// NL_BICGSTAB / NL_GMRES: general (non-symmetric) square systems, FP64,
+// Jacobi or no right preconditioning (nlgb_krylov.cu).
+static NLboolean solve_krylov(Context* c) {
+  const int nf = c->n_free();
+  const int k = c->nb_systems;
+  cudaStream_t s = api_stream();
+  double* ones = nullptr;
+  const double* dinv = c->A.dinv;
+  if (c->precond == NL_PRECOND_NONE) {
+    std::vector<double> h((size_t)std::max(1, nf), 1.0);
+    if (cudaMalloc(&ones, sizeof(double) * h.size()) != cudaSuccess ||
+        cudaMemcpy(ones, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaFree(ones);
+      nl_error(NL_DEVICE_ERROR, "nlSolve: device allocation failed");
+      c->status = NL_GB300_STATUS_DEVICE_ERR;
+      return NL_FALSE;
+    }
+    dinv = ones;
+  }
+  const int method = c->solver == NL_BICGSTAB ? KRYLOV_BICGSTAB : KRYLOV_GMRES;
+  const long long max_iter = c->max_iterations >= 0 ? c->max_iterations : 5LL * nf;
+  bool ok = true;
+  long long iters = 0;
+  double err = 0.0, terr = 0.0;
+  int worst = NL_GB300_STATUS_CONVERGED;
+  const auto t0 = std::chrono::steady_clock::now();
+  std::vector<double> xf((size_t)std::max(1, nf));
+  for (int sys = 0; sys < k; ++sys) {
+    for (int f = 0; f < nf; ++f) xf[f] = c->values[(size_t)sys * c->nb_variables + c->free_vars[f]];
+    KrylovResult kr;
+    cudaError_t e = cudaMemcpyAsync(c->d_x, xf.data(), sizeof(double) * nf, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = krylov_solve(c->A, dinv, c->d_rhs + (size_t)sys * nf, c->d_x, method, c->threshold, max_iter,
+                       c->inner_iterations, s, &kr);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(xf.data(), c->d_x, sizeof(double) * nf, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      cudaFree(ones);
+      nl_error(NL_DEVICE_ERROR, std::string("nlSolve: ") + cudaGetErrorString(e));
+      c->status = NL_GB300_STATUS_DEVICE_ERR;
+      return NL_FALSE;
+    }
+    for (int f = 0; f < nf; ++f) c->values[(size_t)sys * c->nb_variables + c->free_vars[f]] = xf[f];
+    iters += kr.iterations;
+    err = std::max(err, kr.rel_residual);
+    terr = std::max(terr, kr.true_rel_residual);
+    if (kr.status != NL_GB300_STATUS_CONVERGED) { ok = false; worst = kr.status; }
+  }
+  cudaFree(ones);
+  c->used_iterations = iters;
+  c->error = err;
+  c->true_error = terr;
+  c->elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  c->refinement_steps = 0;
+  c->status = worst;
+  c->gflops = 0.0;
+  c->state = S_SOLVED;
+  return ok ? NL_TRUE : NL_FALSE;
+}
+
 NLboolean nlSolve(void) {
   Context* c = ctx_or_error("nlSolve");
   if (!c) return NL_FALSE;
@@ -710,11 +775,6 @@ NLboolean nlSolve(void) {
     return NL_FALSE;
   }
   c->status = NL_GB300_STATUS_NONE;
-  if (c->solver != NL_CG && c->solver != NL_SOLVER_DEFAULT) {
-    nl_error(NL_INVALID_OPERATION, "nlSolve: only NL_CG (Jacobi-preconditioned) is built for the GPU");
-    c->status = NL_GB300_STATUS_BAD_INPUT;
-    return NL_FALSE;
-  }
   if (c->precond == NL_PRECOND_SSOR) {
     nl_error(NL_INVALID_OPERATION, "nlSolve: NL_PRECOND_SSOR is not built; use NL_PRECOND_JACOBI");
     c->status = NL_GB300_STATUS_BAD_INPUT;
@@ -724,6 +784,7 @@ NLboolean nlSolve(void) {
   const int nf = c->n_free();
   const int k = c->nb_systems;
   cudaStream_t s = api_stream();
+  if (c->solver == NL_BICGSTAB || c->solver == NL_GMRES) return solve_krylov(c);
   if (!c->pcg_bound) {
     if (c->precond == NL_PRECOND_NONE) {
       // Identity preconditioner: CG on the same matrix with D^-1 = 1.

@@ -252,14 +252,14 @@ NLMatrix nlMatrixFactorize(NLMatrix, NLenum) {
 }
 
 NLuint nlSolveSystemIterative(NLBlas_t, NLMatrix M, NLMatrix P, const double* b, double* x,
-                              NLenum solver, double eps, NLuint max_iter, NLuint) {
+                              NLenum solver, double eps, NLuint max_iter, NLuint inner_iter) {
   LibMatrix* L = (LibMatrix*)M;
   if (!L || (L->kind != K_DYNAMIC && L->kind != K_CRS) || L->pub.m != L->pub.n) {
     report("nlSolveSystemIterative: needs a square sparse matrix");
     return 0;
   }
-  if (solver != NL_CG && solver != NL_SOLVER_DEFAULT) {
-    report("nlSolveSystemIterative: only NL_CG is built for the GPU path");
+  if (solver != NL_CG && solver != NL_SOLVER_DEFAULT && solver != NL_BICGSTAB && solver != NL_GMRES) {
+    report("nlSolveSystemIterative: unknown solver");
     return 0;
   }
   LibMatrix* PL = (LibMatrix*)P;
@@ -288,6 +288,18 @@ NLuint nlSolveSystemIterative(NLBlas_t, NLMatrix M, NLMatrix P, const double* b,
   }
   Staged sb, sx;
   if (!sb.in(b, n, s) || !sx.in(x, n, s)) { report("nlSolveSystemIterative: staging failed"); return 0; }
+  if (solver == NL_BICGSTAB || solver == NL_GMRES) {
+    // general square systems; inner_iter is GMRES's restart length
+    KrylovResult kr;
+    if (krylov_solve(*L->dev, view.dinv, sb.d, sx.d, solver == NL_BICGSTAB ? KRYLOV_BICGSTAB : KRYLOV_GMRES,
+                     eps, max_iter, std::max<NLuint>(1, inner_iter), s, &kr) != cudaSuccess) {
+      report(last_error());
+      return 0;
+    }
+    sx.out(x, n, s);
+    cudaStreamSynchronize(s);
+    return (NLuint)kr.iterations;
+  }
   PcgSolver pcg;
   SolveParams prm;
   prm.eps = eps;

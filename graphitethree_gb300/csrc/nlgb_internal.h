@@ -158,6 +158,20 @@ cudaError_t build_lscm_system(int n_verts, const double* xyz, int n_tris, const 
 cudaError_t build_fairing_system(int n_verts, const double* xyz, int n_tris, const int* tris,
                                  double lambda, DeviceCRS& out, cudaStream_t s, bool* bad_input);
 
+// Krylov solvers for general square systems (nlgb_krylov.cu): BiCGSTAB and
+// restarted GMRES(restart), FP64, right preconditioning by dinv (Jacobi; all
+// ones for none).  b, x: device vectors of A.n (x: initial guess, replaced).
+enum { KRYLOV_BICGSTAB = 1, KRYLOV_GMRES = 2 };
+struct KrylovResult {
+  int status = 0;                 // ST_* (nlgb_core.cuh)
+  long long iterations = 0;       // BiCGSTAB iterations / GMRES inner steps
+  double rel_residual = 0.0;      // recursive (BiCGSTAB) / restart-time true (GMRES)
+  double true_rel_residual = 0.0; // ||b - A x|| / ||b|| of the returned x
+};
+cudaError_t krylov_solve(const DeviceCRS& A, const double* dinv, const double* b, double* x,
+                         int method, double eps, long long max_iter, int restart, cudaStream_t s,
+                         KrylovResult* res);
+
 // Device BLAS-1 (FP64).
 cudaError_t dev_dot(const double* x, const double* y, long long n, double* out_host, cudaStream_t s);
 cudaError_t dev_axpy(long long n, double a, const double* x, double* y, cudaStream_t s);

@@ -346,7 +346,8 @@ def build_fairing(V, F, lam: float):
 
 
 def solve_opennl(rs: RowStream, precision: str = "double", eps: float = 1e-10,
-                 max_iter: int | None = None, per_call: bool = False):
+                 max_iter: int | None = None, per_call: bool = False, solver: str = "cg",
+                 inner_iterations: int | None = None, preconditioner: str = "jacobi"):
     """Run the OpenNL context sequence on a row stream; returns (values
     (n_systems, n_vars), info dict).  per_call=True feeds rows through
     nlBegin(NL_ROW)/nlCoefficient/nlEnd(NL_ROW) one call at a time (slow in
@@ -357,8 +358,12 @@ def solve_opennl(rs: RowStream, precision: str = "double", eps: float = 1e-10,
         nl.nlSolverParameteri(nl.NL_NB_VARIABLES, rs.n_vars)
         nl.nlSolverParameteri(nl.NL_NB_SYSTEMS, rs.n_systems)
         nl.nlSolverParameteri(nl.NL_LEAST_SQUARES, nl.NL_TRUE if rs.least_squares else nl.NL_FALSE)
-        nl.nlSolverParameteri(nl.NL_SOLVER, nl.NL_CG)
-        nl.nlSolverParameteri(nl.NL_PRECONDITIONER, nl.NL_PRECOND_JACOBI)
+        nl.nlSolverParameteri(nl.NL_SOLVER, {"cg": nl.NL_CG, "bicgstab": nl.NL_BICGSTAB,
+                                             "gmres": nl.NL_GMRES}[solver])
+        nl.nlSolverParameteri(nl.NL_PRECONDITIONER, {"jacobi": nl.NL_PRECOND_JACOBI,
+                                                     "none": nl.NL_PRECOND_NONE}[preconditioner])
+        if inner_iterations is not None:
+            nl.nlSolverParameteri(nl.NL_INNER_ITERATIONS, int(inner_iterations))
         nl.nlSolverParameterd(nl.NL_THRESHOLD, eps)
         if max_iter is not None:
             nl.nlSolverParameteri(nl.NL_MAX_ITERATIONS, int(max_iter))

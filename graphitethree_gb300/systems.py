@@ -216,6 +216,35 @@ def lscm_system(nx: int, ny: int, seed: int, flat: bool = False) -> RowStream:
 
 
 # ---------------------------------------------------------------------------
+# Non-symmetric test system (BiCGSTAB / GMRES)
+# ---------------------------------------------------------------------------
+def convection_diffusion(nx: int, ny: int, seed: int, wind=(40.0, 25.0), reaction: float = 2e4,
+                         n_rhs: int = 1) -> SquareSystem:
+    """-lap u + w . grad u + c u on the unit square, Dirichlet boundary,
+    first-order upwind differences on an nx x ny interior grid, c(x) seeded
+    uniform in [0, reaction]: a non-symmetric M-matrix with a varying
+    diagonal (the structure of a linearised transport step).  Right-hand
+    sides N(0, 1), seeded."""
+    hx, hy = 1.0 / (nx + 1), 1.0 / (ny + 1)
+    wx, wy = wind
+    n = nx * ny
+    I, J, W = [], [], []
+    k = np.arange(n)
+    i, j = k % nx, k // nx
+    rng = np.random.default_rng(seed)
+    diag = 2.0 / hx**2 + 2.0 / hy**2 + abs(wx) / hx + abs(wy) / hy + rng.uniform(0.0, reaction, n)
+    I.append(k); J.append(k); W.append(diag)
+    for di, dj, c in ((-1, 0, -1.0 / hx**2 - max(wx, 0.0) / hx), (1, 0, -1.0 / hx**2 + min(wx, 0.0) / hx),
+                      (0, -1, -1.0 / hy**2 - max(wy, 0.0) / hy), (0, 1, -1.0 / hy**2 + min(wy, 0.0) / hy)):
+        ok = (i + di >= 0) & (i + di < nx) & (j + dj >= 0) & (j + dj < ny)
+        I.append(k[ok]); J.append((k + di + dj * nx)[ok]); W.append(np.full(int(ok.sum()), c))
+    rp, ci, va = csr_from_coo(n, np.concatenate(I), np.concatenate(J), np.concatenate(W))
+    rhs = rng.standard_normal((n_rhs, n))
+    return SquareSystem(n=n, rp=rp, ci=ci, va=va, rhs=rhs,
+                        meta={"kind": "convection-diffusion", "nx": nx, "ny": ny, "seed": seed})
+
+
+# ---------------------------------------------------------------------------
 # WarpDrive voxel interpolation fixture (least squares, locked data voxels)
 # ---------------------------------------------------------------------------
 def voxel_rows(nu: int, nv: int, nw: int, seed: int, locked_fraction: float = 0.3) -> RowStream:

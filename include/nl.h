@@ -113,8 +113,8 @@ typedef void*          NLContext;
 /* ---- solvers / preconditioners ---- */
 #define NL_SOLVER_DEFAULT 0x000
 #define NL_CG             0x200
-#define NL_BICGSTAB       0x201  /* accepted by name, rejected by nlSolve */
-#define NL_GMRES          0x202  /* accepted by name, rejected by nlSolve */
+#define NL_BICGSTAB       0x201  /* general square systems, FP64 */
+#define NL_GMRES          0x202  /* restarted every NL_INNER_ITERATIONS steps, FP64 */
 
 #define NL_PRECOND_NONE    0x000
 #define NL_PRECOND_JACOBI  0x300
@@ -254,8 +254,10 @@ void     nlBlasResetStats(NLBlas_t blas);
 
 /* Iterative solve of M x = b (matrix.cpp:390-393).  M: CRS, dynamic or
  * device matrix; P: NULL or a Jacobi preconditioner; b, x: host or device
- * vectors of size M->n (x is the initial guess).  Only NL_CG (and
- * NL_SOLVER_DEFAULT) is supported; returns the number of iterations used. */
+ * vectors of size M->n (x is the initial guess).  solver: NL_CG /
+ * NL_SOLVER_DEFAULT (Jacobi-PCG), NL_BICGSTAB or NL_GMRES (restart length
+ * inner_iter; both FP64, right-preconditioned by P); returns the number of
+ * iterations used. */
 NLuint nlSolveSystemIterative(NLBlas_t blas, NLMatrix M, NLMatrix P,
                               const double* b, double* x, NLenum solver,
                               double eps, NLuint max_iter, NLuint inner_iter);

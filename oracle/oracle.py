@@ -167,6 +167,131 @@ def direct_solve(rp, ci, va, b):
     return spla.spsolve(A, np.asarray(b, np.float64))
 
 
+def _csr(rp, ci, va):
+    import scipy.sparse as sp
+    n = len(rp) - 1
+    return sp.csr_matrix((np.asarray(va, np.float64), np.asarray(ci), np.asarray(rp)), shape=(n, n))
+
+
+def bicgstab(rp, ci, va, b, x0=None, eps: float = 1e-10, max_iter: int | None = None,
+             jacobi: bool = True):
+    """Right-preconditioned BiCGSTAB (van der Vorst 1992), M^-1 = D^-1 (or
+    the identity): the algorithm of graphitethree_gb300/csrc/nlgb_krylov.cu,
+    restated in numpy.  Stops when ||r|| <= eps ||b|| (recursive r).
+    Returns (x, status, iterations) with status 1 converged, 2 max_iter,
+    3 breakdown."""
+    A = _csr(rp, ci, va)
+    n = A.shape[0]
+    b = np.asarray(b, np.float64)
+    d = A.diagonal()
+    dinv = np.where(d != 0, 1.0 / np.where(d != 0, d, 1.0), 1.0) if jacobi else np.ones(n)
+    x = np.zeros(n) if x0 is None else np.array(x0, np.float64, copy=True)
+    max_iter = 5 * n if max_iter is None else max_iter
+    r = b - A @ x
+    rh = r.copy()
+    bb = b @ b
+    if bb == 0.0:
+        return np.zeros(n), 1, 0
+    rho, alpha, omega = r @ r, 1.0, 1.0
+    beta = rho
+    p = np.zeros(n)
+    v = np.zeros(n)
+    if r @ r <= eps * eps * bb:
+        return x, 1, 0
+    it = 0
+    while True:
+        p = r + beta * (p - omega * v)
+        y = dinv * p
+        v = A @ y
+        rv = rh @ v
+        if rv == 0.0 or not np.isfinite(rv):
+            return x, 3, it
+        alpha = rho / rv
+        s = r - alpha * v
+        z = dinv * s
+        t = A @ z
+        tt = t @ t
+        omega = (t @ s) / tt if tt > 0 else 0.0
+        x = x + alpha * y + omega * z
+        r = s - omega * t
+        it += 1
+        rr = r @ r
+        if rr <= eps * eps * bb:
+            return x, 1, it
+        if it >= max_iter:
+            return x, 2, it
+        rho_new = rh @ r
+        if rho_new == 0.0 or omega == 0.0:
+            return x, 3, it
+        beta = (rho_new / rho) * (alpha / omega)
+        rho = rho_new
+
+
+def gmres(rp, ci, va, b, x0=None, eps: float = 1e-10, restart: int = 30,
+          max_iter: int | None = None, jacobi: bool = True):
+    """Restarted right-preconditioned GMRES(m) (Saad & Schultz 1986) with
+    modified Gram-Schmidt and Givens rotations, M^-1 = D^-1 (or the
+    identity): the algorithm of nlgb_krylov.cu in numpy.  Convergence is
+    decided on the true residual at the start of a cycle; a cycle ends early
+    when its residual estimate reaches eps.  Returns (x, status, inner
+    steps)."""
+    A = _csr(rp, ci, va)
+    n = A.shape[0]
+    b = np.asarray(b, np.float64)
+    d = A.diagonal()
+    dinv = np.where(d != 0, 1.0 / np.where(d != 0, d, 1.0), 1.0) if jacobi else np.ones(n)
+    x = np.zeros(n) if x0 is None else np.array(x0, np.float64, copy=True)
+    max_iter = 5 * n if max_iter is None else max_iter
+    bb = b @ b
+    if bb == 0.0:
+        return np.zeros(n), 1, 0
+    m = restart
+    it = 0
+    while True:
+        r = b - A @ x
+        rr = r @ r
+        if rr <= eps * eps * bb:
+            return x, 1, it
+        if it >= max_iter:
+            return x, 2, it
+        beta = np.sqrt(rr)
+        V = np.zeros((m + 1, n))
+        H = np.zeros((m + 1, m))
+        cs, sn = np.zeros(m), np.zeros(m)
+        g = np.zeros(m + 1)
+        g[0] = beta
+        V[0] = r / beta
+        k = 0
+        for j in range(m):
+            w = A @ (dinv * V[j])
+            for i in range(j + 1):
+                H[i, j] = w @ V[i]
+                w = w - H[i, j] * V[i]
+            hn = np.sqrt(w @ w)
+            H[j + 1, j] = hn
+            for i in range(j):
+                a_, b_ = H[i, j], H[i + 1, j]
+                H[i, j] = cs[i] * a_ + sn[i] * b_
+                H[i + 1, j] = -sn[i] * a_ + cs[i] * b_
+            den = np.hypot(H[j, j], H[j + 1, j])
+            if not den > 0:
+                return x, 3, it
+            cs[j], sn[j] = H[j, j] / den, H[j + 1, j] / den
+            H[j, j], H[j + 1, j] = den, 0.0
+            g[j + 1] = -sn[j] * g[j]
+            g[j] = cs[j] * g[j]
+            it += 1
+            k = j + 1
+            if hn > 0:
+                V[j + 1] = w / hn
+            if g[j + 1] ** 2 <= eps * eps * bb or it >= max_iter or not hn > 0:
+                break
+        y = np.zeros(k)
+        for i in range(k - 1, -1, -1):
+            y[i] = (g[i] - H[i, i + 1:k] @ y[i + 1:k]) / H[i, i]
+        x = x + dinv * (V[:k].T @ y)
+
+
 def dense_normal_equations(rs):
     """Independent numpy restatement of the least-squares normal equations
     (dense; small systems only)."""

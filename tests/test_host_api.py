@@ -103,15 +103,27 @@ def test_variables_and_locks(ctx):
     assert nl.nlGetError() == nl.NL_INVALID_VALUE
 
 
-def test_unsupported_solvers_fail_loudly(ctx):
+def test_unsupported_preconditioner_fails_loudly(ctx):
+    """SSOR is not built: nlSolve refuses it (no silent substitution)."""
     nl.nlSolverParameteri(nl.NL_NB_VARIABLES, 1)
-    nl.nlSolverParameteri(nl.NL_SOLVER, nl.NL_BICGSTAB)
+    nl.nlSolverParameteri(nl.NL_PRECONDITIONER, nl.NL_PRECOND_SSOR)
     nl.nlBegin(nl.NL_SYSTEM); nl.nlBegin(nl.NL_MATRIX)
     nl.nlBegin(nl.NL_ROW); nl.nlCoefficient(0, 1.0); nl.nlRightHandSide(1.0); nl.nlEnd(nl.NL_ROW)
     nl.nlEnd(nl.NL_MATRIX); nl.nlEnd(nl.NL_SYSTEM)
     assert nl.nlSolve() == 0
-    assert "NL_CG" in nl.nlGetErrorString()
+    assert "SSOR" in nl.nlGetErrorString()
     assert nl.nlGetIntegerv(nl.NL_GB300_STATUS) == nl.NL_GB300_STATUS_BAD_INPUT
+
+
+def test_krylov_solver_parameters(ctx):
+    for solver in (nl.NL_CG, nl.NL_BICGSTAB, nl.NL_GMRES):
+        nl.nlSolverParameteri(nl.NL_SOLVER, solver)
+        assert nl.nlGetIntegerv(nl.NL_SOLVER) == solver
+    nl.nlSolverParameteri(nl.NL_INNER_ITERATIONS, 12)
+    assert nl.nlGetIntegerv(nl.NL_INNER_ITERATIONS) == 12
+    nl.nlSolverParameteri(nl.NL_INNER_ITERATIONS, 0)      # a restart length must be >= 1
+    assert nl.nlGetError() == nl.NL_INVALID_VALUE
+    assert nl.nlGetIntegerv(nl.NL_INNER_ITERATIONS) == 12
 
 
 def test_solve_without_gpu_reports_device_error(nllib, ctx):

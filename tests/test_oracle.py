@@ -112,3 +112,24 @@ def test_generators_are_seeded():
     A = sp.csr_matrix((a.va, a.ci, a.rp), shape=(a.n, a.n))
     assert abs(A - A.T).max() < 1e-14
     assert np.allclose(A @ np.ones(a.n), 1e-2)
+
+
+def test_oracle_bicgstab_gmres_pinned_to_direct_solve(oracle_mod):
+    """The numpy restatements of BiCGSTAB and GMRES(m) (checkers of the GPU
+    Krylov solvers) converge on a non-symmetric convection-diffusion system
+    to the SuperLU solution."""
+    from graphitethree_gb300 import systems
+    cd = systems.convection_diffusion(30, 24, seed=3)
+    xd = oracle_mod.direct_solve(cd.rp, cd.ci, cd.va, cd.rhs[0])
+    for jac in (True, False):
+        x, st, it = oracle_mod.bicgstab(cd.rp, cd.ci, cd.va, cd.rhs[0], eps=1e-12, jacobi=jac)
+        assert st == 1 and it > 5
+        assert np.linalg.norm(x - xd) <= 1e-9 * np.linalg.norm(xd)
+        for m in (5, 30):
+            x, st, it = oracle_mod.gmres(cd.rp, cd.ci, cd.va, cd.rhs[0], eps=1e-12, restart=m, jacobi=jac)
+            assert st == 1 and it > 5
+            assert np.linalg.norm(x - xd) <= 1e-9 * np.linalg.norm(xd)
+    x, st, it = oracle_mod.bicgstab(cd.rp, cd.ci, cd.va, np.zeros(cd.n))
+    assert st == 1 and it == 0 and not x.any()
+    x, st, it = oracle_mod.gmres(cd.rp, cd.ci, cd.va, cd.rhs[0], eps=1e-14, restart=5, max_iter=7)
+    assert st == 2 and it == 7                    # stops inside the second cycle
