@@ -150,6 +150,22 @@ def measure_configs():
         "fairing_2048": {"gpu_build_s": gf_best, "host_crs_s": host_fair, "triangles": int(F2.shape[0])},
         "note": "gpu_build_s: nlgb_build_* on the host clock, mesh upload + rows + assembly; host: numpy "
                 "builders of graphitethree_gb300.systems (single thread)"}
+    progress("krylov (non-symmetric)")
+    cd = systems.convection_diffusion(1024, 1024, seed=8)
+    Ak = solver.Matrix(cd.rp, cd.ci, cd.va)
+    kr = {"system": "upwind convection-diffusion 1024^2 (1,048,576 unknowns, non-symmetric)", "nnz": Ak.nnz}
+    for method in ("bicgstab", "gmres"):
+        Ak.solve_krylov(cd.rhs[0], method=method, eps=1e-10, max_iter=20)          # warm-up
+        x, inf = Ak.solve_krylov(cd.rhs[0], method=method, eps=1e-10, restart=30)
+        kr[method] = {"status": inf.status, "iterations": inf.iterations, "ms": inf.seconds * 1e3,
+                      "us_per_iteration": 1e6 * inf.seconds / max(1, inf.iterations),
+                      "true_rel_residual": inf.true_rel_residual}
+    # BiCGSTAB algorithmic bytes per iteration: two SpMVs (12 nnz + 28 n
+    # each) and the three vector passes (p, y: 48 n; s, z: 40 n; x, r: 64 n)
+    b_it = 2 * (12 * Ak.nnz + 28 * Ak.n) + 152 * Ak.n
+    kr["bicgstab"]["algo_GBs"] = b_it / (kr["bicgstab"]["us_per_iteration"] * 1e-6) / 1e9
+    out["krylov"] = kr
+    Ak.close()
     progress("config 5")
     f5 = systems.fairing_system(1024, 1024, seed=5, lam=1e-4, n_rhs=1, stretch_bands=16, rhs_normal=True)
     A5 = solver.Matrix(f5.rp, f5.ci, f5.va)

@@ -151,6 +151,8 @@ _SIGS = {
                                    C.POINTER(NlgbResult), f64p]),
     "nlgb_assemble": (C.c_int, [C.c_int, C.c_longlong, i64p, i32p, f64p, f64p, f64p, C.c_int,
                                 C.c_int, f64p, C.c_int, C.POINTER(C.c_void_p), f64p, f64p]),
+    "nlgb_solve_krylov": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double,
+                                    C.c_longlong, C.c_int, C.c_int, C.POINTER(NlgbResult)]),
     "nlgb_build_lscm": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.POINTER(C.c_void_p), C.c_void_p, f64p]),
     "nlgb_build_fairing": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_double,

@@ -397,6 +397,50 @@ int nlgb_assemble(int least_squares, long long n_rows, const long long* row_ptr,
   return NLGB_OK;
 }
 
+int nlgb_solve_krylov(nlgb_matrix A, const double* b, double* x, int method, double eps,
+                      long long max_iter, int restart, int jacobi, nlgb_result* res) {
+  if (!A || !b || !x) return fail(NLGB_E_INVALID, "nlgb_solve_krylov: bad arguments");
+  if (A->A.n != A->A.m) return fail(NLGB_E_INVALID, "nlgb_solve_krylov: matrix is not square");
+  if (method != NLGB_KRYLOV_BICGSTAB && method != NLGB_KRYLOV_GMRES)
+    return fail(NLGB_E_INVALID, "nlgb_solve_krylov: unknown method");
+  if (!(eps >= 0.0) || restart < 1) return fail(NLGB_E_INVALID, "nlgb_solve_krylov: bad parameters");
+  cudaStream_t s = A->stream;
+  const size_t n = (size_t)A->A.n;
+  Stage sb, sx;
+  if (sb.in(b, n, s, true) != cudaSuccess || sx.in(x, n, s, true) != cudaSuccess) return NLGB_E_DEVICE;
+  double* ones = nullptr;
+  const double* dinv = A->A.dinv;
+  if (!jacobi) {
+    std::vector<double> h(std::max<size_t>(1, n), 1.0);
+    if (cudaMalloc(&ones, sizeof(double) * h.size()) != cudaSuccess ||
+        cudaMemcpy(ones, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaFree(ones);
+      return fail(NLGB_E_DEVICE, "nlgb_solve_krylov: allocation failed");
+    }
+    dinv = ones;
+  }
+  cudaEventRecord(A->e0, s);
+  KrylovResult kr;
+  const cudaError_t e = krylov_solve(A->A, dinv, sb.d, sx.d,
+                                     method == NLGB_KRYLOV_BICGSTAB ? KRYLOV_BICGSTAB : KRYLOV_GMRES, eps,
+                                     max_iter >= 0 ? max_iter : 5LL * (long long)n, restart, s, &kr);
+  cudaEventRecord(A->e1, s);
+  cudaFree(ones);
+  if (e != cudaSuccess) return fail(NLGB_E_DEVICE, cudaGetErrorString(e));
+  if (sx.out(x, n, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) return NLGB_E_DEVICE;
+  if (res) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, A->e0, A->e1);
+    std::memset(res, 0, sizeof(*res));
+    res->status = kr.status;
+    res->iterations = kr.iterations;
+    res->rel_residual = kr.rel_residual;
+    res->true_rel_residual = kr.true_rel_residual;
+    res->seconds = ms * 1e-3;
+  }
+  return NLGB_OK;
+}
+
 int nlgb_build_lscm(int n_verts, const double* xyz, int n_tris, const int* tris, const int* pins,
                     const double* pin_uv, nlgb_matrix* A_out, double* rhs_out, double* seconds) {
   if (!A_out) return fail(NLGB_E_INVALID, "nlgb_build_lscm: bad arguments");

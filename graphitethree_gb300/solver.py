@@ -127,6 +127,20 @@ class Matrix:
         return x, SolveInfo(STATUS.get(r.status, str(r.status)), r.iterations, r.refinement_steps,
                             r.rel_residual, r.true_rel_residual, r.seconds, r.algo_bytes)
 
+    def solve_krylov(self, b, method: str = "bicgstab", x0=None, eps: float = 1e-10,
+                     max_iter: int = -1, restart: int = 30, jacobi: bool = True):
+        """General (non-symmetric) systems: BiCGSTAB or GMRES(restart), FP64.
+        Returns (x, SolveInfo)."""
+        K = _lib.header_constants()
+        b = np.ascontiguousarray(b, np.float64)
+        x = np.zeros(self.n) if x0 is None else np.array(x0, np.float64, copy=True)
+        r = _lib.NlgbResult()
+        code = K["NLGB_KRYLOV_BICGSTAB"] if method == "bicgstab" else K["NLGB_KRYLOV_GMRES"]
+        _check(_lib.load().nlgb_solve_krylov(self._h, b.ctypes.data, x.ctypes.data, code, eps, max_iter,
+                                             restart, int(jacobi), ctypes.byref(r)), "nlgb_solve_krylov")
+        return x, SolveInfo(STATUS.get(r.status, str(r.status)), r.iterations, 0, r.rel_residual,
+                            r.true_rel_residual, r.seconds, 0.0)
+
     def solve_device(self, b_ptr: int, x_ptr: int, eps: float = 1e-10, max_iter: int = -1,
                      precision: str = "double", inner_eps: float = 0.1, max_outer: int = 100000):
         """Solve with device pointers (e.g. torch tensors' data_ptr())."""

@@ -69,6 +69,17 @@ int         nlgb_matrix_info(nlgb_matrix A, int* n_rows, long long* nnz, int* th
 /* Override the autotuner (threads_per_row in {1,2,4,8,16,32}, tile_rows a
  * multiple of 64 in [64, 2^20]; 0 keeps the current value). */
 int         nlgb_matrix_set_layout(nlgb_matrix A, int threads_per_row, int tile_rows);
+/* General (non-symmetric) square systems: BiCGSTAB or GMRES(restart), FP64,
+ * right-preconditioned by the Jacobi diagonal (jacobi != 0) or not.  Same
+ * solvers as nlSolveSystemIterative(NL_BICGSTAB / NL_GMRES) (reference:
+ * src/lib/OGF/scene_graph/NL/matrix.cpp:390-393), on a matrix handle.
+ * b, x: host or device vectors; x is the initial guess.  res->iterations:
+ * BiCGSTAB iterations or GMRES inner steps. */
+#define NLGB_KRYLOV_BICGSTAB 1
+#define NLGB_KRYLOV_GMRES    2
+int         nlgb_solve_krylov(nlgb_matrix A, const double* b, double* x, int method, double eps,
+                              long long max_iter, int restart, int jacobi, nlgb_result* res);
+
 /* Mesh system builders on the GPU.  Replace the host-side row emission of
  * Graphite's mesh_compute_LSCM and mesh_smooth commands (reference:
  * src/lib/OGF/mesh/commands/mesh_grob_surface_commands.cpp:759 and :703,

@@ -83,3 +83,21 @@ def test_krylov_edge_cases(gpu_ok):
         vals, info = solver.solve_opennl(cd.to_rows(), eps=1e-14, max_iter=6, solver=method,
                                          inner_iterations=4)
         assert info["status"] == "max_iter" and info["iterations"] == 6
+
+
+@pytest.mark.parametrize("method", ["bicgstab", "gmres"])
+def test_handle_api_equals_matrix_api(gpu_ok, method):
+    """nlgb_solve_krylov on a matrix handle and nlSolveSystemIterative on an
+    NLMatrix run the same solver on the same CRS: identical results."""
+    cd = systems.convection_diffusion(34, 31, seed=7)
+    A = solver.Matrix(cd.rp, cd.ci, cd.va)
+    xh, ih = A.solve_krylov(cd.rhs[0], method=method, eps=1e-11, restart=25)
+    assert ih.status == "converged" and ih.true_rel_residual <= 1.5e-11 and ih.seconds > 0
+    M = nl_matrix(cd)
+    P = nl.nlNewJacobiPreconditioner(M)
+    x = np.zeros(cd.n)
+    code = nl.NL_BICGSTAB if method == "bicgstab" else nl.NL_GMRES
+    its = nl.nlSolveSystemIterative(nl.nlHostBlas(), M, P, cd.rhs[0], x, code, 1e-11, 5 * cd.n, 25)
+    assert its == ih.iterations and np.array_equal(x, xh)
+    nl.nlDeleteMatrix(P)
+    nl.nlDeleteMatrix(M)
