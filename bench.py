@@ -75,7 +75,7 @@ def parse_args():
     p.add_argument("--no-spmv", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--profile-case", choices=["spmv", "batch", "batch_small", "batch_lscm", "plain", "mixed",
-                                              "plain_lscm", "mixed_lscm"], default=None,
+                                              "plain_lscm", "mixed_lscm", "kernels"], default=None,
                    help="run one small case for an ncu capture and exit")
     p.add_argument("--workload", choices=["serving", "configs"], default="serving",
                    help="configs: measure the other benchmark configurations and exit")
@@ -180,6 +180,9 @@ def profile_case(which):
     spmv:  3 FP64 SpMVs on the 2048^2 cotangent Laplacian (k_spmv);
     batch: one persistent-kernel launch over 8 mid-size systems, 300
            iterations each (k_batch);
+    kernels: every kernel family once at sizes beyond L2 (assembly, mesh
+           builders, FP64 / mixed PCG kernels one by one, BiCGSTAB, GMRES,
+           SpMV);
     plain_lscm / mixed_lscm: 40 iterations on the 1.3M-unknown LSCM normal
            equations (808^2 grid), graph path;
     batch_lscm: the 1.3M-unknown LSCM system alone in the persistent kernel,
@@ -206,6 +209,31 @@ def profile_case(which):
         else:
             x, info = A.solve(fs.rhs[0], max_iter=20, precision="double" if which == "plain" else "mixed")
             print(json.dumps({"case": which, "iterations": info.iterations, "ms": info.seconds * 1e3}))
+        return
+    if which == "kernels":
+        # every kernel family once, at sizes beyond L2: least-squares assembly
+        # (LSCM 808^2 rows), the GPU mesh builders, FP64 and mixed PCG
+        # iterations (kernels launched one by one), BiCGSTAB and GMRES on a
+        # non-symmetric 1M-unknown system, the standalone SpMV
+        from graphitethree_gb300 import meshes
+        os.environ["NLGB_EAGER_SOLVE"] = "1"
+        M, rhs, _ = solver.assemble(systems.lscm_system(808, 808, seed=1))
+        M.close()
+        V, F = meshes.height_field(1024, 1024, seed=2)
+        solver.build_lscm(V, F)[0].close()
+        solver.build_fairing(V, F, 1e-2)[0].close()
+        fs = systems.fairing_system(2048, 2048, seed=2, n_rhs=1)
+        A = solver.Matrix(fs.rp, fs.ci, fs.va)
+        A.solve(fs.rhs[0], max_iter=8, eps=1e-30)
+        A.solve(fs.rhs[0], max_iter=8, eps=1e-30, precision="mixed")
+        A.spmv(fs.rhs[0])
+        A.close()
+        cd = systems.convection_diffusion(1024, 1024, seed=8)
+        K = solver.Matrix(cd.rp, cd.ci, cd.va)
+        K.solve_krylov(cd.rhs[0], method="bicgstab", max_iter=4, eps=1e-30)
+        K.solve_krylov(cd.rhs[0], method="gmres", max_iter=4, restart=4, eps=1e-30)
+        K.close()
+        print(json.dumps({"case": which, "done": True}))
         return
     if which in ("plain_lscm", "mixed_lscm"):
         # 40 iterations on the LSCM normal equations of an 808 x 808 grid
