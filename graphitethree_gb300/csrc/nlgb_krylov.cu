@@ -9,7 +9,10 @@
 // whose Jacobians are not symmetric.  Published algorithms restated here:
 // BiCGSTAB, H. A. van der Vorst, SIAM J. Sci. Stat. Comput. 13 (1992);
 // GMRES(m), Y. Saad & M. H. Schultz, SIAM J. Sci. Stat. Comput. 7 (1986),
-// with modified Gram-Schmidt and Givens rotations.
+// with Givens rotations and classical Gram-Schmidt applied twice (CGS2; as
+// stable as modified Gram-Schmidt in practice, L. Giraud, J. Langou &
+// M. Rozloznik 2005) so that an inner step needs two multi-dot passes
+// instead of 2(j + 1) dependent dot/axpy passes.
 //
 // Layout: the matrix's own tiles (DeviceCRS::tile_rows, threads per row);
 // every dot product is a set of per-tile partials reduced in a fixed order
@@ -43,6 +46,7 @@ struct KrState {
   int pad_;
   double H[(kMaxRestart + 1) * kMaxRestart];   // column-major, (m + 1) x m
   double cs[kMaxRestart], sn[kMaxRestart], g[kMaxRestart + 1], y[kMaxRestart];
+  double hr[kMaxRestart + 1];       // GMRES: coefficients of the current Gram-Schmidt round
 };
 
 struct KrView {
@@ -53,6 +57,8 @@ struct KrView {
   const double* dinv;
   double* part;      // n_tiles * kParts
   KrState* st;
+  double* mpart;     // GMRES: n_tiles * (m + 1) multi-dot partials
+  int mstride;
 };
 
 __device__ __forceinline__ bool running(const KrView& v) {
@@ -230,7 +236,8 @@ __global__ void k_kr_true_scalar(KrView v) {
 // ---------------------------------------------------------------------------
 // GMRES(m) (right preconditioning, M^-1 = D^-1), one cycle:
 //   r = b - A x, beta = ||r||, V0 = r / beta, g = beta e1
-//   for j < m: w = A M^-1 V_j; modified Gram-Schmidt against V_0..V_j (H);
+//   for j < m: w = A M^-1 V_j; classical Gram-Schmidt against V_0..V_j,
+//              twice (CGS2: h = V^T w, w -= V h; again; H_j = h + h2);
 //              H_{j+1,j} = ||w||, V_{j+1} = w / H_{j+1,j}; Givens rotations
 //              on column j, g; |g_{j+1}| is the residual norm
 //   y = H^-1 g (upper triangular), x += M^-1 (V y)
@@ -293,39 +300,58 @@ __global__ void k_gm_precond(KrView v, GmVecs w, int j) {
     w.u[i] = v.dinv[i] * Vj[i];
 }
 
-// V_{j+1} = A u; partial of V_{j+1}.V_0 (the first Gram-Schmidt dot)
+// V_{j+1} = A u
 template <int T>
 __global__ void __launch_bounds__(kCTA) k_gm_spmv(KrView v, GmVecs w, int j) {
   if (!gm_active(v, j)) return;
   double* Wn = w.V + (size_t)(j + 1) * w.ld;
-  const double* V0 = w.V;
-  double a[1] = {0.0};
-  tile_spmv<T>(v, w.u, [&](int i, double q) { Wn[i] = q; a[0] = fma(q, V0[i], a[0]); });
-  put_tile<1>(v, 0, a);
+  tile_spmv<T>(v, w.u, [&](int i, double q) { Wn[i] = q; });
 }
 
-// H_{i,j} = canonical sum of the partials
-__global__ void k_gm_h(KrView v, int i, int j) {
+// Gram-Schmidt round, 1/3: per-tile partials of V_i . w for every i <= j
+// (one sweep over the tile per i; w stays in L1 between them).  Measured on
+// GB300: grouping eight coefficients per sweep was not faster.
+__global__ void __launch_bounds__(kCTA) k_gm_multidot(KrView v, GmVecs w, int j) {
   if (!gm_active(v, j)) return;
-  double o[1];
-  sums<1>(v, 0, o);
-  if (threadIdx.x == 0) v.st->H[j * (kMaxRestart + 1) + i] = o[0];
+  const double* Wn = w.V + (size_t)(j + 1) * w.ld;
+  for (int i = 0; i <= j; ++i) {
+    const double* Vi = w.V + (size_t)i * w.ld;
+    double a[1] = {0.0};
+    for (int r = lo_of(v) + threadIdx.x; r < hi_of(v); r += kCTA) a[0] = fma(Wn[r], Vi[r], a[0]);
+    block_sum<1>(a);
+    if (threadIdx.x == 0) v.mpart[(size_t)blockIdx.x * v.mstride + i] = a[0];
+  }
 }
 
-// w -= H_{i,j} V_i, then the partial of w.V_{i+1} (i + 1 <= j) or of w.w
-__global__ void __launch_bounds__(kCTA) k_gm_mgs(KrView v, GmVecs w, int i, int j) {
+// 2/3: CTA i reduces coefficient i over the tiles in the canonical order
+// (thread t sums tiles t, t + 256, ..., then the fixed block tree).
+__global__ void __launch_bounds__(kCTA) k_gm_hreduce(KrView v, int j, int round) {
+  if (!gm_active(v, j)) return;
+  const int i = blockIdx.x;
+  double a[1] = {0.0};
+  for (int t = threadIdx.x; t < v.n_tiles; t += kCTA) a[0] += v.mpart[(size_t)t * v.mstride + i];
+  block_sum<1>(a);
+  if (threadIdx.x == 0) {
+    double* Hj = v.st->H + j * (kMaxRestart + 1);
+    v.st->hr[i] = a[0];
+    Hj[i] = round == 0 ? a[0] : Hj[i] + a[0];
+  }
+}
+
+// 3/3: w -= sum_i hr_i V_i (i in order); after the second round also the
+// partial of w.w for the norm.
+__global__ void __launch_bounds__(kCTA) k_gm_update(KrView v, GmVecs w, int j, int with_norm) {
   if (!gm_active(v, j)) return;
   double* Wn = w.V + (size_t)(j + 1) * w.ld;
-  const double* Vi = w.V + (size_t)i * w.ld;
-  const double* Vn = i + 1 <= j ? w.V + (size_t)(i + 1) * w.ld : Wn;
-  const double h = v.st->H[j * (kMaxRestart + 1) + i];
+  const double* hr = v.st->hr;
   double a[1] = {0.0};
   for (int r = lo_of(v) + threadIdx.x; r < hi_of(v); r += kCTA) {
-    const double x = Wn[r] - h * Vi[r];
+    double x = Wn[r];
+    for (int i = 0; i <= j; ++i) x -= hr[i] * w.V[(size_t)i * w.ld + r];
     Wn[r] = x;
-    a[0] = fma(x, Vn[r], a[0]);
+    a[0] = fma(x, x, a[0]);
   }
-  put_tile<1>(v, 0, a);
+  if (with_norm) put_tile<1>(v, 0, a);
 }
 
 // H_{j+1,j} = ||w||, V_{j+1} /= it; Givens rotations; cycle control.
@@ -422,6 +448,9 @@ cudaError_t krylov_solve(const DeviceCRS& A, const double* dinv, const double* b
   NLGB_CUDA_TRY(cudaMallocAsync(&work, sizeof(double) * ld * n_vec + 256, s));
   cudaError_t e = cudaMallocAsync(&part, sizeof(double) * (size_t)n_tiles * kParts, s);
   if (e == cudaSuccess) e = cudaMallocAsync(&st, sizeof(KrState), s);
+  double* mpart = nullptr;
+  if (e == cudaSuccess && method == KRYLOV_GMRES)
+    e = cudaMallocAsync(&mpart, sizeof(double) * (size_t)n_tiles * (m + 1), s);
   KrState h;
   std::memset(&h, 0, sizeof(h));
   h.thresh2 = eps * eps;
@@ -429,7 +458,7 @@ cudaError_t krylov_solve(const DeviceCRS& A, const double* dinv, const double* b
   h.status = ST_RUNNING;
   h.m = m;
   if (e == cudaSuccess) e = cudaMemcpyAsync(st, &h, sizeof(h), cudaMemcpyHostToDevice, s);
-  KrView v{n, tile_rows, n_tiles, A.rp, A.ci, A.va, dinv, part, st};
+  KrView v{n, tile_rows, n_tiles, A.rp, A.ci, A.va, dinv, part, st, mpart, m + 1};
   long long launches = 0;
   auto poll = [&](int* status) {
     cudaError_t pe = cudaMemcpyAsync(status, &st->status, sizeof(int), cudaMemcpyDeviceToHost, s);
@@ -470,13 +499,14 @@ cudaError_t krylov_solve(const DeviceCRS& A, const double* dinv, const double* b
       for (int j = 0; j < m; ++j) {
         k_gm_precond<<<grid1(n), 256, 0, s>>>(v, w, j);
         NLGB_KR_T((k_gm_spmv<T><<<n_tiles, kCTA, 0, s>>>(v, w, j)));
-        for (int i = 0; i <= j; ++i) {
-          k_gm_h<<<1, kCTA, 0, s>>>(v, i, j);
-          k_gm_mgs<<<n_tiles, kCTA, 0, s>>>(v, w, i, j);
+        for (int round = 0; round < 2; ++round) {     // CGS2
+          k_gm_multidot<<<n_tiles, kCTA, 0, s>>>(v, w, j);
+          k_gm_hreduce<<<j + 1, kCTA, 0, s>>>(v, j, round);
+          k_gm_update<<<n_tiles, kCTA, 0, s>>>(v, w, j, round);
         }
         k_gm_norm<<<1, kCTA, 0, s>>>(v, j);
         k_gm_scale<<<grid1(n), 256, 0, s>>>(v, w, j);
-        launches += 5 + 2LL * (j + 1);
+        launches += 10;
       }
       k_gm_solve_y<<<1, 32, 0, s>>>(v);
       k_gm_update_x<<<grid1(n), 256, 0, s>>>(v, w);
@@ -497,6 +527,7 @@ cudaError_t krylov_solve(const DeviceCRS& A, const double* dinv, const double* b
   cudaFreeAsync(work, s);
   if (part) cudaFreeAsync(part, s);
   if (st) cudaFreeAsync(st, s);
+  if (mpart) cudaFreeAsync(mpart, s);
   if (e != cudaSuccess) return e;
   if (res) {
     res->status = h.status;

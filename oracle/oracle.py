@@ -230,7 +230,8 @@ def bicgstab(rp, ci, va, b, x0=None, eps: float = 1e-10, max_iter: int | None = 
 def gmres(rp, ci, va, b, x0=None, eps: float = 1e-10, restart: int = 30,
           max_iter: int | None = None, jacobi: bool = True):
     """Restarted right-preconditioned GMRES(m) (Saad & Schultz 1986) with
-    modified Gram-Schmidt and Givens rotations, M^-1 = D^-1 (or the
+    classical Gram-Schmidt applied twice (CGS2) and Givens rotations,
+    M^-1 = D^-1 (or the
     identity): the algorithm of nlgb_krylov.cu in numpy.  Convergence is
     decided on the true residual at the start of a cycle; a cycle ends early
     when its residual estimate reaches eps.  Returns (x, status, inner
@@ -264,9 +265,11 @@ def gmres(rp, ci, va, b, x0=None, eps: float = 1e-10, restart: int = 30,
         k = 0
         for j in range(m):
             w = A @ (dinv * V[j])
-            for i in range(j + 1):
-                H[i, j] = w @ V[i]
-                w = w - H[i, j] * V[i]
+            h = V[: j + 1] @ w                   # classical Gram-Schmidt, twice (CGS2)
+            w = w - V[: j + 1].T @ h
+            h2 = V[: j + 1] @ w
+            w = w - V[: j + 1].T @ h2
+            H[: j + 1, j] = h + h2
             hn = np.sqrt(w @ w)
             H[j + 1, j] = hn
             for i in range(j):
