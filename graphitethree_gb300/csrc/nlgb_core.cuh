@@ -68,6 +68,7 @@ struct __align__(16) SysState {
   int pad_;
   long long iter_at_fallback;  // FP32 iterations done before the FP64 fallback
   long long iter_stop;         // > 0: a graph chunk pauses (status unchanged) at this iteration
+  long long coop_epoch;        // single-kernel iterations run in this solve (grid-barrier targets)
 };
 
 // Algorithmic HBM bytes of one solve (n rows, z nonzeros), from its final

@@ -116,6 +116,10 @@ class PcgSolver {
   void* st_host_ = nullptr;     // pinned staging
   const volatile int* abort_flag_ = nullptr;
   cudaGraphExec_t plain_exec_ = nullptr, mixed_exec_ = nullptr;
+  // single-kernel cooperative iterations (small and mid-size systems)
+  bool use_coop_ = false;
+  int coop_grid_ = 0;
+  unsigned long long* coop_bar_ = nullptr;
   cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
   bool mixed_alloc_ = false;
   long long graph_launches_ = 0;

@@ -126,6 +126,103 @@ __global__ void __launch_bounds__(kCTA) k_update_p(SysView s) {
   for (int t = vec_t0(s), t1 = vec_t1(s); t < t1; ++t) tile_update_p(s, t, beta);
 }
 
+// ---------------------------------------------------------------------------
+// One whole FP64 PCG iteration in one cooperative kernel (small and mid-size
+// systems, all tiles in one resident wave): SpMV + p.q, grid barrier, x / r
+// update, grid barrier, p update; the kernel boundary orders the next
+// iteration's SpMV after this p update.  Every CTA reduces the tile partials
+// in the canonical order and applies the same scalar steps to its own copy
+// of the state (identical results), so the phases need no extra barrier for
+// the scalars; CTA 0 writes the state back.  The tile procedures, reductions
+// and scalar steps are those of the three-kernel iteration: the iterates are
+// bit-identical.  Replaces three kernel boundaries and three last-CTA
+// reduction tails per iteration by two barriers.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long coop_atom_add(unsigned long long* p) {
+  unsigned long long old;
+  asm volatile("atom.acq_rel.gpu.global.add.u64 %0, [%1], 1;" : "=l"(old) : "l"(p) : "memory");
+  return old;
+}
+__device__ __forceinline__ unsigned long long coop_ld_acquire(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned long long coop_clock_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Grid barrier on a monotonic counter (one arrival per CTA per barrier):
+// returns false in every thread if the wait exceeded 4 s.
+__device__ bool coop_grid_sync(unsigned long long* bar, unsigned long long target) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    coop_atom_add(bar);
+    const unsigned long long t0 = coop_clock_ns();
+    unsigned int spins = 0;
+    while (coop_ld_acquire(bar) < target) {
+      if ((++spins & 63u) == 0u && coop_clock_ns() - t0 > 4000000000ULL) { ok = 0; break; }
+    }
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+template <int T>
+__global__ void __launch_bounds__(kCTA) k_iter(SysView s, unsigned long long* bar) {
+  __shared__ SysState sst;
+  if (threadIdx.x == 0) sst = *s.st;      // written by the previous kernel
+  __syncthreads();
+  if (sst.status != ST_RUNNING) return;
+  const int G = gridDim.x;
+  const unsigned long long base = (unsigned long long)sst.coop_epoch * 2ULL * (unsigned long long)G;
+  for (int t = blockIdx.x; t < s.n_tiles; t += G) {
+    const double v = tile_spmv_pq<T>(s, t);
+    if (threadIdx.x == 0) __stcg(s.part + (size_t)t * kParts + kSlotPQ, v);
+  }
+  bool ok = coop_grid_sync(bar, base + G);
+  if (ok) {
+    const int comp[1] = {kSlotPQ};
+    double o[1];
+    canon_reduce<1>(s.part, s.n_tiles, comp, o);
+    if (threadIdx.x == 0) scalar_after_pq(&sst, o[0]);
+    __syncthreads();
+    if (sst.status == ST_RUNNING) {
+      const double alpha = sst.alpha;
+      for (int t = blockIdx.x; t < s.n_tiles; t += G) {
+        double v[2];
+        tile_update_xr(s, t, alpha, v);
+        if (threadIdx.x == 0) {
+          __stcg(s.part + (size_t)t * kParts + kSlotXR, v[0]);
+          __stcg(s.part + (size_t)t * kParts + kSlotXR + 1, v[1]);
+        }
+      }
+    }
+    // every CTA takes the second barrier (the epoch arithmetic counts both)
+    ok = coop_grid_sync(bar, base + 2ULL * G);
+    if (ok && sst.status == ST_RUNNING) {
+      const int comp2[2] = {kSlotXR, kSlotXR + 1};
+      double o2[2];
+      canon_reduce<2>(s.part, s.n_tiles, comp2, o2);
+      if (threadIdx.x == 0) scalar_after_xr(&sst, o2[0], o2[1]);
+      __syncthreads();
+      if (sst.status == ST_RUNNING) {
+        const double beta = sst.beta;
+        for (int t = blockIdx.x; t < s.n_tiles; t += G) tile_update_p(s, t, beta);
+      }
+    }
+  }
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    if (!ok) sst.status = ST_DEVICE_ERR;
+    sst.coop_epoch += 1;
+    *s.st = sst;
+  }
+}
+
 // Termination guard of a while-node body (single thread).  use_handle == 0:
 // launched outside a graph (eager mode), the host reads the status instead.
 __global__ void k_guard(SysView s, cudaGraphConditionalHandle h, int need_mode, int use_handle) {
@@ -311,6 +408,34 @@ static long long resident_slots() {
   return 8LL * sms;
 }
 
+// CTAs of the single-kernel iteration k_iter<T> resident at once (0 if the
+// occupancy cannot be queried).
+// Above ~640 CTAs the single-counter barrier and the per-CTA canonical
+// reductions (CTAs x tiles partial reads) cost more than the two kernel
+// boundaries they replace (measured on GB300: 512 CTAs 30 vs 38 us per
+// iteration, 834-1,024 CTAs 47-64 vs 39-50 us).
+constexpr long long kCoopMaxCtas = 640;
+
+static long long coop_wave(int tpr) {
+  const void* fn = nullptr;
+  switch (tpr) {
+    case 1: fn = (const void*)k_iter<1>; break;
+    case 2: fn = (const void*)k_iter<2>; break;
+    case 4: fn = (const void*)k_iter<4>; break;
+    case 8: fn = (const void*)k_iter<8>; break;
+    case 16: fn = (const void*)k_iter<16>; break;
+    default: fn = (const void*)k_iter<32>; break;
+  }
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kCTA, 0) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return std::min<long long>((long long)per_sm * sms, kCoopMaxCtas);
+}
+
 TuneChoice autotune(int n, long long nnz, int max_row, const int* hist33) {
   // Threads per row: the smallest power of two with at most ~8 nonzeros per
   // lane for the typical row (measured on GB300 with the 7-nonzero cotangent
@@ -340,10 +465,15 @@ TuneChoice autotune(int n, long long nnz, int max_row, const int* hist33) {
   // rows with at most 4,096 tiles; among equal costs the fewest tiles (each
   // scalar is a reduction over the tiles, so three waves of 384-row tiles
   // are slower than one wave of 1,152).  Small systems keep 128-row tiles:
-  // one wave of CTAs as small as they go.
+  // one wave of CTAs as small as they go; systems just above one resident
+  // wave of the single-kernel iteration (k_iter) at 128 rows take 256-row
+  // tiles, so that they still fit that wave (one tile per CTA).
   const long long slots = resident_slots();
+  const long long cw = coop_wave(tpr);
   int tile = 128;
-  if ((long long)n > slots * 128) {
+  if (cw > 0 && (long long)n > 128 * cw && (long long)n <= 256 * cw) {
+    tile = 256;
+  } else if ((long long)n > slots * 128) {
     long long best_cost = -1;
     for (int t = 128; t <= 16384; t += 128) {
       const long long nt = ((long long)n + t - 1) / t;
@@ -512,17 +642,18 @@ template <int T> struct PlainKernels {
   static const void* mx_spmv() { return (const void*)k_mx_spmv_pq<T>; }
 };
 
-struct KernelSet { const void *init, *spmv, *fin, *mx_outer, *mx_spmv; };
+struct KernelSet { const void *init, *spmv, *fin, *mx_outer, *mx_spmv, *iter; };
 static KernelSet kernels_for(int tpr) {
   switch (tpr) {
-#define NLGB_KS(T) case T: return {PlainKernels<T>::init(), PlainKernels<T>::spmv(), PlainKernels<T>::fin(), PlainKernels<T>::mx_outer(), PlainKernels<T>::mx_spmv()};
+#define NLGB_KS(T) case T: return {PlainKernels<T>::init(), PlainKernels<T>::spmv(), PlainKernels<T>::fin(), PlainKernels<T>::mx_outer(), PlainKernels<T>::mx_spmv(), (const void*)k_iter<T>};
     NLGB_KS(1) NLGB_KS(2) NLGB_KS(4) NLGB_KS(8) NLGB_KS(16)
-    default: return {PlainKernels<32>::init(), PlainKernels<32>::spmv(), PlainKernels<32>::fin(), PlainKernels<32>::mx_outer(), PlainKernels<32>::mx_spmv()};
+    default: return {PlainKernels<32>::init(), PlainKernels<32>::spmv(), PlainKernels<32>::fin(), PlainKernels<32>::mx_outer(), PlainKernels<32>::mx_spmv(), (const void*)k_iter<32>};
 #undef NLGB_KS
   }
 }
 
 constexpr int kUnrollPlain = 4;   // CG iterations per while-body pass
+constexpr int kCoopTilesPerCta = 1;   // measured: two tiles per CTA lose to three kernels
 constexpr int kUnrollInner = 4;
 constexpr long long kMaxItersBetweenUpdates = 1000;   // mixed: forced reliable update
 
@@ -533,6 +664,8 @@ void PcgSolver::release() {
   if (mixed_exec_) cudaGraphExecDestroy(mixed_exec_);
   plain_exec_ = mixed_exec_ = nullptr;
   cudaFree(b_); cudaFree(x_); cudaFree(r_); cudaFree(p_); cudaFree(q_); cudaFree(part_);
+  cudaFree(coop_bar_);
+  coop_bar_ = nullptr;
   cudaFree(r32_); cudaFree(p32_); cudaFree(q32_); cudaFree(c32_); cudaFree(st_);
   if (st_host_) cudaFreeHost(st_host_);
   if (ev0_) cudaEventDestroy(ev0_);
@@ -552,6 +685,20 @@ cudaError_t PcgSolver::bind(DeviceCRS* A, cudaStream_t stream) {
   tpr_ = A->tpr;
   tile_rows_ = A->tile_rows;
   n_tiles_ = std::max(1, (n_ + tile_rows_ - 1) / tile_rows_);
+  // One cooperative kernel per iteration when the tiles fit in one resident
+  // wave of it at no more than kCoopTilesPerCta tiles per CTA (latency-bound
+  // sizes); larger systems keep one kernel per phase at full occupancy.
+  int dev = 0, sms = 0, per_sm = 0;
+  use_coop_ = false;
+  if (cudaGetDevice(&dev) == cudaSuccess &&
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernels_for(tpr_).iter, kCTA, 0) == cudaSuccess &&
+      per_sm > 0) {
+    const long long wave = std::min<long long>((long long)per_sm * sms, kCoopMaxCtas);
+    use_coop_ = n_tiles_ <= kCoopTilesPerCta * wave;
+    coop_grid_ = (int)std::min<long long>(n_tiles_, wave);
+  }
+  cudaGetLastError();
   return alloc(false);
 }
 
@@ -568,6 +715,7 @@ cudaError_t PcgSolver::alloc(bool mixed) {
     NLGB_CUDA_TRY(cudaMallocHost(&st_host_, sizeof(SysState)));
     NLGB_CUDA_TRY(cudaEventCreate(&ev0_));
     NLGB_CUDA_TRY(cudaEventCreate(&ev1_));
+    NLGB_CUDA_TRY(cudaMalloc(&coop_bar_, 256));
   }
   if (mixed && !mixed_alloc_) {
     const size_t n4 = (size_t)std::max(4, n_ + 4) * sizeof(float);
@@ -608,7 +756,19 @@ cudaError_t PcgSolver::build_plain_graph() {
   cudaGraph_t body;
   NLGB_CUDA_TRY(add_while(g, &n_loop, n_init, h, &body));
   prev = nullptr;
+  unsigned long long* bar = coop_bar_;
+  void* a_it[] = {&v, &bar};
   for (int u = 0; u < kUnrollPlain; ++u) {
+    if (use_coop_) {
+      cudaGraphNode_t n1;
+      NLGB_CUDA_TRY(add_kernel(body, &n1, prev, ks.iter, coop_grid_, kCTA, a_it));
+      cudaKernelNodeAttrValue coop;
+      std::memset(&coop, 0, sizeof(coop));
+      coop.cooperative = 1;
+      NLGB_CUDA_TRY(cudaGraphKernelNodeSetAttribute(n1, cudaKernelNodeAttributeCooperative, &coop));
+      prev = n1;
+      continue;
+    }
     cudaGraphNode_t n1, n2, n3;
     NLGB_CUDA_TRY(add_kernel(body, &n1, prev, ks.spmv, n_tiles_, kCTA, a1));
     const int vg = (n_tiles_ + vec_tiles_for(tile_rows_) - 1) / vec_tiles_for(tile_rows_);
@@ -852,7 +1012,16 @@ cudaError_t PcgSolver::run_eager(bool mixed, SysState* h) {
 cudaError_t PcgSolver::run_graph(bool mixed, const SolveParams& prm, long long max_iter,
                                  long long done, int outer, float* ms) {
   if (mixed && !mixed_exec_) NLGB_CUDA_TRY(build_mixed_graph());
-  if (!mixed && !plain_exec_) NLGB_CUDA_TRY(build_plain_graph());
+  if (!mixed && !plain_exec_) {
+    cudaError_t e = build_plain_graph();
+    if (e != cudaSuccess && use_coop_) {
+      // cooperative kernel nodes refused here: one kernel per phase instead
+      cudaGetLastError();
+      use_coop_ = false;
+      e = build_plain_graph();
+    }
+    NLGB_CUDA_TRY(e);
+  }
   SysState* h = (SysState*)st_host_;
   std::memset(h, 0, sizeof(SysState));
   h->thresh2 = prm.eps * prm.eps;
@@ -873,6 +1042,7 @@ cudaError_t PcgSolver::run_graph(bool mixed, const SolveParams& prm, long long m
   const int unroll = mixed ? kUnrollInner : kUnrollPlain;
   h->guard_cap = std::max(0LL, max_iter - done) / unroll + 2LL * (h->max_outer + 2) + 4;
   NLGB_CUDA_TRY(cudaMemcpyAsync(st_, h, sizeof(SysState), cudaMemcpyHostToDevice, stream_));
+  NLGB_CUDA_TRY(cudaMemsetAsync(coop_bar_, 0, sizeof(unsigned long long), stream_));   // coop_epoch = 0 too
   if (mixed) {
     NLGB_CUDA_TRY(cudaMemsetAsync(c32_, 0, (size_t)n_ * sizeof(float), stream_));
     NLGB_CUDA_TRY(cudaMemsetAsync(p32_, 0, (size_t)n_ * sizeof(float), stream_));
@@ -893,7 +1063,8 @@ cudaError_t PcgSolver::run_graph(bool mixed, const SolveParams& prm, long long m
   // (3 per unrolled iteration + the guard); the mixed graph adds 2 kernels
   // per reliable update after the first; plus the first and final kernels.
   const long long passes = h->guard;
-  long long k = 2 + passes * (3LL * unroll + 1);
+  const long long per_iter = (!mixed && use_coop_) ? 1 : 3;
+  long long k = 2 + passes * (per_iter * unroll + 1);
   if (mixed) k += 2LL * std::max(0, h->outer - outer - 1);
   count_launches(k);
   return cudaSuccess;
