@@ -11,10 +11,13 @@ namespace nlgb {
 // Systems with at least this many tiles are run by multi-CTA teams; smaller
 // ones are popped from the queue by single CTAs.
 constexpr int kLargeTiles = 16;
-// A system alone in the server from this many tiles on is continued on the
-// graph executor (measured on GB300: from ~500 tiles the graph path is faster
-// per iteration than a single-system persistent launch).
+// When only large systems are left in the server (at least kGraphMinTiles
+// tiles each, at most kMaxGraphSystems of them), each continues on its own
+// graph executor, one after the other in an epoch (measured on GB300: from
+// ~500 tiles the graph path is faster per iteration than the persistent
+// kernel).
 constexpr int kGraphMinTiles = 384;
+constexpr size_t kMaxGraphSystems = 4;
 
 // Team barrier on monotonic 64-bit arrival counters (never reset within a
 // launch): barrier number e of a team is complete when its counter reaches

@@ -357,7 +357,7 @@ void worker_batched(nlgb_server_s* S) {
   std::vector<SysState> states;
   std::vector<std::pair<Req*, int>> owner;   // system index -> (request, rhs)
   int active_systems = 0;
-  ViewGraph solo;
+  std::vector<std::unique_ptr<ViewGraph>> solos;   // graph executors of large systems
   auto admit_pending = [&]() {
     // first fit in arrival order
     for (size_t i = 0; i < S->pending.size();) {
@@ -400,36 +400,47 @@ void worker_batched(nlgb_server_s* S) {
         owner.push_back({r, k});
       }
     BatchLaunchStats bst;
-    // A lone large FP64 system (everything else finished) continues on the
-    // graph executor, which is faster per iteration than the persistent
-    // kernel once one system fills the GPU (same iterates, see ViewGraph).
-    bool graph_epoch = false;
-    if (views.size() == 1 && !S->aborting) {
-      Req* r = owner[0].first;
-      const int k = owner[0].second;
-      graph_epoch = !req_mixed(S, *r) && views[0].n_tiles >= kGraphMinTiles && r->sys_stage[k] == 1;
+    // When every active system is a large FP64 one (at most kMaxGraphSystems,
+    // everything small finished), each continues on its own graph executor,
+    // one after the other in the epoch: faster per iteration than sharing the
+    // persistent kernel once each fills the GPU alone (same iterates, see
+    // ViewGraph).
+    bool graph_epoch = !views.empty() && views.size() <= kMaxGraphSystems && !S->aborting;
+    for (size_t i = 0; graph_epoch && i < views.size(); ++i) {
+      const Req* r = owner[i].first;
+      const int k = owner[i].second;
+      graph_epoch = !req_mixed(S, *r) && views[i].n_tiles >= kGraphMinTiles && r->sys_stage[k] == 1;
     }
     cudaError_t e = cudaSuccess;
     if (graph_epoch) {
-      float gms = 0.f;
-      const long long before = owner[0].first->sys_iter[owner[0].second];
-      e = solo.run(views[0], S->cfg.epoch_iters, sc, &gms);
+      while (solos.size() < views.size()) solos.emplace_back(new ViewGraph());
+      std::vector<float> gms(views.size(), 0.f);
+      std::vector<long long> before(views.size());
+      for (size_t i = 0; i < views.size() && e == cudaSuccess; ++i) {
+        before[i] = owner[i].first->sys_iter[owner[i].second];
+        e = solos[i]->run(views[i], S->cfg.epoch_iters, sc, &gms[i]);
+      }
       if (e == cudaSuccess) {
         intake(S, false);
         admit_pending();
-        states.resize(1);
-        e = cudaMemcpyAsync(states.data(), views[0].st, sizeof(SysState), cudaMemcpyDeviceToHost, sc);
+        states.resize(views.size());
+        for (size_t i = 0; i < views.size() && e == cudaSuccess; ++i)
+          e = cudaMemcpyAsync(&states[i], views[i].st, sizeof(SysState), cudaMemcpyDeviceToHost, sc);
       }
       if (e == cudaSuccess) e = cudaStreamSynchronize(sc);
-      if (e == cudaSuccess) e = solo.finish(before, states[0].iter);
-      bst.ms = gms;
+      double total_ms = 0.0, bytes = 0.0;
+      for (size_t i = 0; i < views.size() && e == cudaSuccess; ++i) {
+        e = solos[i]->finish(before[i], states[i].iter);
+        total_ms += gms[i];
+        const Req* r = owner[i].first;
+        bytes += double(states[i].iter - before[i]) * (12.0 * double(r->A.nnz) + 108.0 * double(r->A.n));
+      }
+      bst.ms = total_ms;
       if (e == cudaSuccess) {
-        const Req* r = owner[0].first;
         std::lock_guard<std::mutex> lk(S->mu);
-        S->st.graph_s += gms * 1e-3;
+        S->st.graph_s += total_ms * 1e-3;
         S->st.graph_epochs += 1;
-        S->st.graph_algo_bytes +=
-            double(states[0].iter - before) * (12.0 * double(r->A.nnz) + 108.0 * double(r->A.n));
+        S->st.graph_algo_bytes += bytes;
       }
     } else {
       e = runner.launch(views, work, S->aborting ? 1 : S->cfg.epoch_iters);

@@ -177,3 +177,25 @@ def test_switch_back_from_graph_when_requests_arrive(gpu_ok):
         assert [i.iterations for i in infs] == ia
         assert np.array_equal(x, xa)
     srv.close()
+
+
+def test_large_systems_share_graph_epochs(gpu_ok):
+    """Two large FP64 systems and nothing else: after their first epoch both
+    continue as graph chunks within the same epochs; each result equals its
+    own single-system solve bit for bit."""
+    fa = systems.fairing_system(420, 400, seed=41, n_rhs=1)
+    fb = systems.fairing_system(400, 410, seed=42, n_rhs=1)
+    alone = []
+    for fs in (fa, fb):
+        A = solver.Matrix(fs.rp, fs.ci, fs.va)
+        assert A.n // A.tile_rows >= 384
+        alone.append(A.solve(fs.rhs[0]))
+    srv = solver.Server(precision="double", epoch_iters=32)
+    ta, tb = srv.submit_square(fa), srv.submit_square(fb)
+    for t, (x1, i1) in zip((ta, tb), alone):
+        x, infs, _ = srv.wait(t)
+        assert infs[0].status == "converged" and infs[0].iterations == i1.iterations
+        assert np.array_equal(x[0], x1)
+    st = srv.stats()
+    srv.close()
+    assert st["graph_epochs"] >= 2 and st["graph_s"] > 0
