@@ -559,8 +559,8 @@ def main():
     p50 = float(np.percentile(lat, 50))
     p99 = float(np.percentile(lat, 99))
     st_last, res_last = steps[-1]
-    # the persistent kernel alone: a lone large FP64 system that the server
-    # continued as graph chunks is reported separately (graph_chunks)
+    # the persistent kernel alone: the iterations of large FP64 systems that
+    # the server continued as graph chunks are accounted separately
     kb_bytes = st_last["algo_bytes"] - st_last["graph_algo_bytes"]
     kb_s = st_last["kernel_s"] - st_last["graph_s"]
     kb_launches = max(1, st_last["epochs"] - st_last["graph_epochs"])

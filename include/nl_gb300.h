@@ -202,9 +202,10 @@ typedef struct {
     double    algo_bytes;        /* algorithmic HBM bytes over all systems     */
     size_t    peak_bytes;        /* peak admitted device footprint             */
     size_t    budget_bytes;
-    double    graph_s;           /* part of kernel_s spent in graph chunks (a
-                                    lone large FP64 system continued on the
-                                    single-system graph executor)            */
+    double    graph_s;           /* part of kernel_s spent in graph chunks
+                                    (large FP64 systems continued on the
+                                    single-system graph executor once only
+                                    such systems are left)                   */
     double    graph_algo_bytes;  /* part of algo_bytes: iterations run there   */
     long long graph_epochs;      /* part of epochs run as graph chunks         */
 } nlgb_server_stats;
