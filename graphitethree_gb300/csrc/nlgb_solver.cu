@@ -886,9 +886,18 @@ cudaError_t ViewGraph::build(const SysView& v) {
   return cudaSuccess;
 }
 
+// Everything the graph embeds: a slot freed and reallocated from the
+// stream-ordered pool may return the same state and vector addresses for a
+// different matrix, so every pointer and size is compared.
+static bool same_view(const SysView& a, const SysView& b) {
+  return a.n == b.n && a.tile_rows == b.tile_rows && a.n_tiles == b.n_tiles && a.tpr == b.tpr &&
+         a.rp == b.rp && a.ci == b.ci && a.va == b.va && a.dinv == b.dinv && a.b == b.b &&
+         a.x == b.x && a.r == b.r && a.p == b.p && a.q == b.q && a.part == b.part && a.st == b.st &&
+         a.abort_flag == b.abort_flag;
+}
+
 cudaError_t ViewGraph::run(const SysView& v, long long iters, cudaStream_t s, float* ms) {
-  if (!exec_ || v.st != view_.st || v.x != view_.x || v.n_tiles != view_.n_tiles || v.tpr != view_.tpr)
-    NLGB_CUDA_TRY(build(v));
+  if (!exec_ || !same_view(v, view_)) NLGB_CUDA_TRY(build(v));
   NLGB_CUDA_TRY(cudaEventRecord(e0_, s));
   k_chunk_start<<<1, 1, 0, s>>>(v.st, std::max(1LL, iters), kUnrollPlain);
   NLGB_CUDA_TRY(cudaGetLastError());

@@ -199,3 +199,20 @@ def test_large_systems_share_graph_epochs(gpu_ok):
     st = srv.stats()
     srv.close()
     assert st["graph_epochs"] >= 2 and st["graph_s"] > 0
+
+
+def test_graph_continuation_after_slot_reuse(gpu_ok):
+    """Two different large systems of the same size, one after the other in
+    one server: the second's slot may come back at the first's addresses
+    (stream-ordered pool); its graph chunks must run on its own matrix."""
+    fa = systems.fairing_system(420, 400, seed=51, n_rhs=1)
+    fb = systems.fairing_system(420, 400, seed=52, n_rhs=1, lam=3e-2)
+    srv = solver.Server(precision="double", epoch_iters=32)
+    for fs in (fa, fb):
+        A = solver.Matrix(fs.rp, fs.ci, fs.va)
+        x1, i1 = A.solve(fs.rhs[0])
+        x, infs, _ = srv.wait(srv.submit_square(fs))
+        assert infs[0].status == "converged" and infs[0].iterations == i1.iterations
+        assert np.array_equal(x[0], x1)
+    assert srv.stats()["graph_epochs"] >= 2
+    srv.close()
