@@ -447,6 +447,8 @@ int nlgb_build_lscm(int n_verts, const double* xyz, int n_tris, const int* tris,
   *A_out = nullptr;
   if (n_verts < 3 || n_tris < 0 || !xyz || (n_tris > 0 && !tris))
     return fail(NLGB_E_INVALID, "nlgb_build_lscm: bad arguments");
+  if (n_verts > (1 << 30) - 1 || (long long)n_tris * 12 > (1LL << 40))
+    return fail(NLGB_E_INVALID, "nlgb_build_lscm: mesh too large (2 n_verts variables must fit in int)");
   const int pv[2] = {pins ? pins[0] : 0, pins ? pins[1] : n_verts - 1};
   const double uv[4] = {pin_uv ? pin_uv[0] : 0.0, pin_uv ? pin_uv[1] : 0.0,
                         pin_uv ? pin_uv[2] : 1.0, pin_uv ? pin_uv[3] : 1.0};

@@ -70,7 +70,7 @@ __global__ void k_lscm_rows(int n_tris, const double* __restrict__ xyz, const in
                             int4 locked, int* __restrict__ col, double* __restrict__ val) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_tris) return;
-  const int f[3] = {tris[3 * t], tris[3 * t + 1], tris[3 * t + 2]};
+  const int f[3] = {tris[3LL * t], tris[3LL * t + 1], tris[3LL * t + 2]};
   double p[3][3];
   for (int j = 0; j < 3; ++j)
     for (int c = 0; c < 3; ++c) p[j][c] = xyz[3 * (long long)f[j] + c];
@@ -107,7 +107,7 @@ __global__ void k_cotan_rows(int n_tris, const double* __restrict__ xyz, const i
   const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (r >= 3LL * n_tris) return;
   const int t = (int)(r / 3), k = (int)(r % 3);
-  const int o = tris[3 * t + k], i = tris[3 * t + (k + 1) % 3], j = tris[3 * t + (k + 2) % 3];
+  const int o = tris[3LL * t + k], i = tris[3LL * t + (k + 1) % 3], j = tris[3LL * t + (k + 2) % 3];
   double u[3], v[3], c[3];
   for (int q = 0; q < 3; ++q) {
     u[q] = sub(xyz[3 * (long long)i + q], xyz[3 * (long long)o + q]);

@@ -658,7 +658,7 @@ long long nlgb_server_submit_mesh(nlgb_server S, int mesh_kind, int n_verts, con
   const bool lscm = mesh_kind == NLGB_MESH_LSCM;
   if (!S || (mesh_kind != NLGB_MESH_LSCM && mesh_kind != NLGB_MESH_FAIRING) || n_verts < 3 ||
       n_tris < 0 || !xyz || (n_tris > 0 && !tris) || !x_out || n_rhs < 1 || (lscm && n_rhs != 1) ||
-      (!lscm && (!b || !(lambda >= 0.0)))) {
+      (!lscm && (!b || !(lambda >= 0.0))) || n_verts > (1 << 30) - 1) {
     set_error("nlgb_server_submit_mesh: bad arguments");
     return NLGB_E_INVALID;
   }
