@@ -33,7 +33,9 @@ Reported:
               cores) on the same sample: every request assembled and timed;
               systems over 250k unknowns timed on 200 iterations and scaled
               to the oracle's own iteration count for them (committed
-              fixture oracle/serving_sample_iterations.json).
+              fixture oracle/serving_sample_iterations.json);
+              cpu_baseline_1thread: the same with one thread;
+  hbm         peak device footprint admitted by the server vs its budget.
 `--impl reference` runs only the CPU reference arm (the oracle port: the
 reference's own OpenNL source is not in the checkout) and prints its line.
 """
@@ -415,7 +417,7 @@ def sample_iterations_fixture(args):
     return {r["request"]: r for r in fx["systems"]}
 
 
-def cpu_arm(objs, args):
+def cpu_arm(objs, args, threads: int | None = None):
     """The oracle (C, OpenMP on all host cores): row assembly + FP64
     Jacobi-PCG for every request of the sample, in arrival order.  Systems up
     to CPU_FULL_LIMIT unknowns are solved to completion; a larger one runs
@@ -424,7 +426,7 @@ def cpu_arm(objs, args):
     (committed fixture).  Without the fixture the larger requests are left
     out and the sample says so."""
     from oracle import oracle
-    threads = oracle.max_threads()
+    threads = threads or oracle.max_threads()
     fx = sample_iterations_fixture(args)
     total, done, full, scaled, skipped = 0.0, 0, [], [], []
     for i, (kind, o) in enumerate(objs):
@@ -607,8 +609,10 @@ def main():
                  "speedup_device": value / (R / stp["kernel_s"])}
     spmv = None if args.no_spmv else spmv_roofline(peak)
     cpu = None
+    cpu1 = None
     if not args.no_cpu and rank == 0:
         cpu = cpu_arm(objs, args)
+        cpu1 = cpu_arm(objs, args, threads=1)
 
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
@@ -623,6 +627,8 @@ def main():
         "roofline_other": other,
         "spmv_fp64": spmv,
         "cpu_baseline": cpu,
+        "cpu_baseline_1thread": None if cpu1 is None else {k: cpu1[k] for k in ("value", "unit", "cores")},
+        "hbm": {"peak_admitted_gb": st_last["peak_bytes"] / 1e9, "budget_gb": st_last["budget_bytes"] / 1e9},
         "clocks": clk,
         "gpu_launches": int(launches),
         "parity": {"all_converged": all(s == "converged" for s in statuses),
