@@ -9,8 +9,8 @@ log-uniform in [1e3, 1e6], square-ish grid patches with the seeded bump
 model, Poisson arrivals at `--rate` per second -- submitted through the C ABI
 (nlgb_server_submit_rows / _crs with host buffers) to the continuous-batching
 server (HBM budget 150 GB, precision AUTO: mixed FP32/FP64 with FP64
-fallback for square systems, FP64 for least-squares normal equations) and
-drained.
+fallback for square systems, double-float -- FP64-class float pairs on the
+FP32 pipe -- for least-squares normal equations) and drained.
 Every step re-submits the same sample from scratch (assembly, upload, solve,
 download: nothing is cached).
 
@@ -24,7 +24,7 @@ Reported:
               single-system PCG, one request at a time);
   roofline    achieved algorithmic GB/s (bytes from the iteration counts,
               CUDA-event time) of the executor that dominates the step --
-              the FP64 PCG iteration graph continuing the large systems, or
+              the PCG iteration graph continuing the large systems, or
               the persistent batched kernel -- vs the measured HBM peak;
               roofline_other: the other one;
   spmv_fp64   the FP64 CRS SpMV on the 2048^2 cotangent Laplacian (4.2M
@@ -83,7 +83,7 @@ def parse_args():
     p.add_argument("--no-spmv", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--profile-case", choices=["spmv", "batch", "batch_small", "batch_lscm", "plain", "mixed",
-                                              "plain_lscm", "mixed_lscm", "kernels"], default=None,
+                                              "plain_lscm", "mixed_lscm", "df_lscm", "kernels"], default=None,
                    help="run one small case for an ncu capture and exit")
     p.add_argument("--workload", choices=["serving", "configs"], default="serving",
                    help="configs: measure the other benchmark configurations and exit")
@@ -191,8 +191,9 @@ def profile_case(which):
     kernels: every kernel family once at sizes beyond L2 (assembly, mesh
            builders, FP64 / mixed PCG kernels one by one, BiCGSTAB, GMRES,
            SpMV);
-    plain_lscm / mixed_lscm: 40 iterations on the 1.3M-unknown LSCM normal
-           equations (808^2 grid), graph path;
+    plain_lscm / mixed_lscm / df_lscm: 40 iterations on the 1.3M-unknown
+           LSCM normal equations (808^2 grid), graph path, in FP64, mixed or
+           double-float;
     batch_lscm: the 1.3M-unknown LSCM system alone in the persistent kernel,
            200 FP64 iterations;
     batch_small: one 4,604-unknown LSCM system in the persistent kernel,
@@ -243,12 +244,12 @@ def profile_case(which):
         K.close()
         print(json.dumps({"case": which, "done": True}))
         return
-    if which in ("plain_lscm", "mixed_lscm"):
+    if which in ("plain_lscm", "mixed_lscm", "df_lscm"):
         # 40 iterations on the LSCM normal equations of an 808 x 808 grid
         # (1,305,724 unknowns): graph-captured single-system PCG
         M, rhs, _ = solver.assemble(systems.lscm_system(808, 808, seed=1))
-        x, info = M.solve(rhs[0], max_iter=40, eps=1e-30,
-                          precision="double" if which == "plain_lscm" else "mixed")
+        prec = {"plain_lscm": "double", "mixed_lscm": "mixed", "df_lscm": "df"}[which]
+        x, info = M.solve(rhs[0], max_iter=40, eps=1e-30, precision=prec)
         print(json.dumps({"case": which, "iterations": info.iterations, "ms": info.seconds * 1e3,
                           "n": M.n, "nnz": M.nnz, "tile_rows": M.tile_rows, "tpr": M.threads_per_row}))
         return
@@ -495,7 +496,8 @@ def config(args):
             "requests": args.requests, "rate_per_s": args.rate, "rel_residual": args.eps,
             "hbm_budget_gb": args.budget_gb,
             "precision": "auto: mixed FP32/FP64 (with FP64 fallback) for the square fairing "
-                         "systems, FP64 for the least-squares LSCM normal equations",
+                         "systems, double-float (float pairs, ~48-bit significand, FP32 pipe; "
+                         "OpenNL's stopping rule) for the least-squares LSCM normal equations",
             "l2": "inputs larger than L2 for the large requests; every step re-uploads and "
                   "re-assembles (no cached data)"}
 
@@ -581,7 +583,8 @@ def main():
                           "1.3M-unknown LSCM system (0.88 DRAM byte per algorithmic byte, "
                           "profiles/k_batch_lscm808.md)"}
     g_ach = g_bytes / g_s / 1e9 if g_s > 0 else 0.0
-    gr = {"bound": "hbm", "kernel": "FP64 PCG iteration graph (k_spmv_pq + k_update_xr + k_update_p), "
+    gr = {"bound": "hbm", "kernel": "PCG iteration graph (k_spmv_pq + k_update_xr + k_update_p; "
+                                    "double-float for the least-squares systems under AUTO), "
                                     "one launch per chunk of a large system",
           "achieved": g_ach, "peak": peak, "unit": "GB/s", "frac": g_ach / peak,
           "traffic": GRAPH_DRAM_PER_ALGO_BYTE * g_bytes / g_launches,
@@ -590,8 +593,8 @@ def main():
           "traffic_note": "dram read+write per launch, scaled from the ncu capture of k_spmv_pq on the "
                           "1.3M-unknown LSCM system (1.03 DRAM byte per algorithmic byte; the vector "
                           "kernels stream exactly their bytes), profiles/k_spmv_pq_lscm808_fairing2048.md"}
-    fp64_note = ("the FP64 phases are co-limited by GB300's FP64 pipe (65-81 % busy in the captures), "
-                 "not only by HBM")
+    fp64_note = ("FP64 phases are co-limited by GB300's FP64 pipe (65-81 % busy in the captures); "
+                 "the double-float phases run on the FP32 pipe")
     roofline, other = (gr, kb) if g_s > kb_s else (kb, gr)
     roofline = {**roofline, "fp64_note": fp64_note}
     statuses = [i.status for infos, _ in res_last for i in infos]
@@ -617,7 +620,7 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_wall / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64+df(f32 pairs)+f32",
         "data": "synthetic (seeded serving-stream sample; no public dataset)",
         "config": config(args),
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

@@ -57,7 +57,7 @@ class NlgbParams(C.Structure):
 class NlgbResult(C.Structure):
     _fields_ = [("status", C.c_int), ("iterations", C.c_longlong), ("refinement_steps", C.c_int),
                 ("rel_residual", C.c_double), ("true_rel_residual", C.c_double),
-                ("seconds", C.c_double), ("algo_bytes", C.c_double)]
+                ("seconds", C.c_double), ("algo_bytes", C.c_double), ("precision", C.c_int)]
 
 
 class NlgbServerConfig(C.Structure):

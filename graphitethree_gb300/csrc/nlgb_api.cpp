@@ -240,7 +240,7 @@ int nlgb_solve(nlgb_matrix A, const double* b, double* x, const nlgb_params* prm
   nlgb_default_params(&p);
   if (prm) p = *prm;
   if (p.precision != NL_GB300_PRECISION_DOUBLE && p.precision != NL_GB300_PRECISION_MIXED &&
-      p.precision != NL_GB300_PRECISION_AUTO)
+      p.precision != NL_GB300_PRECISION_AUTO && p.precision != NL_GB300_PRECISION_DOUBLE_FLOAT)
     return fail(NLGB_E_INVALID, "nlgb_solve: unknown precision");
   // a matrix given directly is square: AUTO means mixed
   if (p.precision == NL_GB300_PRECISION_AUTO) p.precision = NL_GB300_PRECISION_MIXED;
@@ -272,6 +272,7 @@ int nlgb_solve(nlgb_matrix A, const double* b, double* x, const nlgb_params* prm
     res->true_rel_residual = r.true_rel_residual;
     res->seconds = r.seconds;
     res->algo_bytes = r.algo_bytes;
+    res->precision = r.precision;
   }
   return NLGB_OK;
 }
@@ -287,7 +288,7 @@ int nlgb_batch_solve(int n_sys, const nlgb_matrix* A, const double* const* b, do
   nlgb_default_params(&p);
   if (prm) p = *prm;
   if (p.precision != NL_GB300_PRECISION_DOUBLE && p.precision != NL_GB300_PRECISION_MIXED &&
-      p.precision != NL_GB300_PRECISION_AUTO)
+      p.precision != NL_GB300_PRECISION_AUTO && p.precision != NL_GB300_PRECISION_DOUBLE_FLOAT)
     return fail(NLGB_E_INVALID, "nlgb_batch_solve: unknown precision");
   // a matrix given directly is square: AUTO means mixed
   if (p.precision == NL_GB300_PRECISION_AUTO) p.precision = NL_GB300_PRECISION_MIXED;
@@ -308,8 +309,10 @@ int nlgb_batch_solve(int n_sys, const nlgb_matrix* A, const double* const* b, do
     if (runner.init(s) != cudaSuccess) rc = NLGB_E_DEVICE;
     for (int i = 0; i < n_sys && rc == NLGB_OK; ++i) {
       DeviceCRS& M = A[i]->A;
-      if (crs_prepare(M, mixed, s) != cudaSuccess || slots[i].alloc(&M, mixed, s) != cudaSuccess ||
-          slots[i].start(b[i], x[i], sp, s) != cudaSuccess) {
+      bool dfl = false;
+      if (crs_prepare(M, mixed, s) != cudaSuccess ||
+          (p.precision == NL_GB300_PRECISION_DOUBLE_FLOAT && crs_prepare_df(M, &dfl, s) != cudaSuccess) ||
+          slots[i].alloc(&M, mixed, s, dfl) != cudaSuccess || slots[i].start(b[i], x[i], sp, s) != cudaSuccess) {
         rc = NLGB_E_DEVICE;
         break;
       }
@@ -323,7 +326,8 @@ int nlgb_batch_solve(int n_sys, const nlgb_matrix* A, const double* const* b, do
     if (rc == NLGB_OK && kernel_seconds) *kernel_seconds = st.ms * 1e-3;
     std::vector<SysState> hs((size_t)n_sys);
     for (int i = 0; i < n_sys && rc == NLGB_OK; ++i) {
-      if (cudaMemcpyAsync(x[i], slots[i].view.x, sizeof(double) * A[i]->A.n, cudaMemcpyDefault, s) != cudaSuccess ||
+      if ((slots[i].df && df_unpack(slots[i].view.x, A[i]->A.n, s) != cudaSuccess) ||
+          cudaMemcpyAsync(x[i], slots[i].view.x, sizeof(double) * A[i]->A.n, cudaMemcpyDefault, s) != cudaSuccess ||
           cudaMemcpyAsync(&hs[i], slots[i].view.st, sizeof(SysState), cudaMemcpyDeviceToHost, s) != cudaSuccess)
         rc = NLGB_E_DEVICE;
     }
@@ -338,6 +342,8 @@ int nlgb_batch_solve(int n_sys, const nlgb_matrix* A, const double* const* b, do
         res[i].true_rel_residual = h.bnorm2 > 0 ? std::sqrt(h.rr_true / h.bnorm2) : 0.0;
         res[i].seconds = st.ms * 1e-3;
         res[i].algo_bytes = algo_bytes(A[i]->A.n, A[i]->A.nnz, h);
+        res[i].precision = mixed ? NL_GB300_PRECISION_MIXED
+                                 : (slots[i].df ? NL_GB300_PRECISION_DOUBLE_FLOAT : NL_GB300_PRECISION_DOUBLE);
       }
     }
     for (auto& sl : slots) sl.release(s);

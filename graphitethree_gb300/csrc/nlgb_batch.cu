@@ -146,10 +146,11 @@ __device__ void get_sums(const SysView& s, int slot, double (&o)[K]) {
 #ifndef NLGB_HOT_PHASE
 #define NLGB_HOT_PHASE __noinline__
 #endif
+template <bool D>
 __device__ __noinline__ void ph_residual(const SysView& s, int r, int k) {
   for (int t = r; t < s.n_tiles; t += k) {
     double v[3];
-    NLGB_TPR_SWITCH(tile_residual<T, true>(s, t, v));
+    NLGB_TPR_SWITCH((phase_residual<D, T, true>(s, t, v)));
     put_parts(s, t, kSlotInit, v, 3);
   }
 }
@@ -160,22 +161,25 @@ __device__ __noinline__ void ph_mx_outer(const SysView& s, int r, int k) {
     put_parts(s, t, kSlotInit, v, 4);
   }
 }
+template <bool D>
 __device__ NLGB_HOT_PHASE void ph_spmv_pq(const SysView& s, int r, int k) {
   for (int t = r; t < s.n_tiles; t += k) {
     double v[1];
-    NLGB_TPR_SWITCH(v[0] = tile_spmv_pq<T, true>(s, t));
+    NLGB_TPR_SWITCH((v[0] = phase_spmv_pq<D, T, true>(s, t)));
     put_parts(s, t, kSlotPQ, v, 1);
   }
 }
+template <bool D>
 __device__ NLGB_HOT_PHASE void ph_update_xr(const SysView& s, int r, int k, double alpha) {
   for (int t = r; t < s.n_tiles; t += k) {
     double v[2];
-    tile_update_xr(s, t, alpha, v);
+    phase_update_xr<D>(s, t, alpha, v);
     put_parts(s, t, kSlotXR, v, 2);
   }
 }
+template <bool D>
 __device__ NLGB_HOT_PHASE void ph_update_p(const SysView& s, int r, int k, double beta) {
-  for (int t = r; t < s.n_tiles; t += k) tile_update_p(s, t, beta);
+  for (int t = r; t < s.n_tiles; t += k) phase_update_p<D>(s, t, beta);
 }
 __device__ __noinline__ void ph_mx_update_p(const SysView& s, int r, int k, double beta) {
   for (int t = r; t < s.n_tiles; t += k) tile_mx_update_p(s, t, beta);
@@ -197,13 +201,14 @@ __device__ __noinline__ void ph_mx_update_cr(const SysView& s, int r, int k, dou
 __device__ __noinline__ void ph_mx_apply(const SysView& s, int r, int k) {
   for (int t = r; t < s.n_tiles; t += k) tile_mx_apply(s, t);
 }
+template <bool D>
 __device__ __noinline__ void ph_final(const SysView& s, int r, int k, bool zero_rhs) {
   for (int t = r; t < s.n_tiles; t += k) {
     double v[1] = {0.0};
     if (zero_rhs) {
       tile_zero_x(s, t);
     } else {
-      NLGB_TPR_SWITCH(v[0] = tile_true_rr<T, true>(s, t));
+      NLGB_TPR_SWITCH((v[0] = phase_true_rr<D, T, true>(s, t)));
     }
     put_parts(s, t, kSlotFinal, v, 1);
   }
@@ -230,7 +235,8 @@ __device__ void run_system_once(const SysView& s, SysState* st, int r, int k, Te
   long long done_iters = 0;
   if (st->stage == 0) {
     if (!mixed) {
-      ph_residual(s, r, k);
+      if (s.df) ph_residual<true>(s, r, k);
+      else ph_residual<false>(s, r, k);
       if (!team_sync(bar, k, r, err)) { NLGB_SCALAR(st->status = ST_DEVICE_ERR; st->stage = 3); return; }
       const Sums4 o = sums_of(s, kSlotInit, 3);
       NLGB_SCALAR(scalar_after_init(st, o.v[0], o.v[1], o.v[2]); st->stage = st->status == ST_RUNNING ? 1 : 2);
@@ -246,14 +252,16 @@ __device__ void run_system_once(const SysView& s, SysState* st, int r, int k, Te
   while (st->stage == 1 && (budget <= 0 || done_iters < budget)) {
     if (!mixed) {
       // q = A p, p.q
-      ph_spmv_pq(s, r, k);
+      if (s.df) ph_spmv_pq<true>(s, r, k);
+      else ph_spmv_pq<false>(s, r, k);
       if (!team_sync(bar, k, r, err)) break;
       {
         const Sums4 o = sums_of(s, kSlotPQ, 1);
         NLGB_SCALAR(scalar_after_pq(st, o.v[0]));
       }
       if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
-      ph_update_xr(s, r, k, st->alpha);
+      if (s.df) ph_update_xr<true>(s, r, k, st->alpha);
+      else ph_update_xr<false>(s, r, k, st->alpha);
       if (!team_sync(bar, k, r, err)) break;
       {
         const Sums4 o = sums_of(s, kSlotXR, 2);
@@ -261,7 +269,8 @@ __device__ void run_system_once(const SysView& s, SysState* st, int r, int k, Te
       }
       ++done_iters;
       if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
-      ph_update_p(s, r, k, st->beta);
+      if (s.df) ph_update_p<true>(s, r, k, st->beta);
+      else ph_update_p<false>(s, r, k, st->beta);
       if (!team_sync(bar, k, r, err)) break;
     } else {
       // FP32 PCG iteration with FP64 reliable updates; same phase order as
@@ -308,7 +317,8 @@ __device__ void run_system_once(const SysView& s, SysState* st, int r, int k, Te
   }
   if (st->stage == 2) {
     // final true residual (FP64) of the returned x; x = 0 when b == 0
-    ph_final(s, r, k, st->zero_rhs != 0);
+    if (s.df) ph_final<true>(s, r, k, st->zero_rhs != 0);
+    else ph_final<false>(s, r, k, st->zero_rhs != 0);
     if (!team_sync(bar, k, r, err)) { NLGB_SCALAR(st->status = ST_DEVICE_ERR; st->stage = 3); return; }
     const Sums4 o = sums_of(s, kSlotFinal, 1);
     NLGB_SCALAR(st->rr_true = o.v[0]; st->stage = 3);
@@ -602,9 +612,10 @@ size_t SystemSlot::bytes_for(int n, int tile_rows, bool mixed) {
   return mixed ? (5 * n8 + 4 * n4 + parts + st) : (5 * n8 + parts + st);
 }
 
-cudaError_t SystemSlot::alloc(DeviceCRS* Am, bool mx, cudaStream_t s) {
+cudaError_t SystemSlot::alloc(DeviceCRS* Am, bool mx, cudaStream_t s, bool dfl) {
   A = Am;
   mixed = mx;
+  df = dfl && !mx && Am->vadf != nullptr && Am->dinvdf != nullptr;
   const int n = A->n;
   bytes = bytes_for(n, A->tile_rows, mixed);
   NLGB_CUDA_TRY(cudaMallocAsync(&block, bytes, s));
@@ -618,6 +629,11 @@ cudaError_t SystemSlot::alloc(DeviceCRS* Am, bool mx, cudaStream_t s) {
   view.tpr = A->tpr;
   view.rp = A->rp; view.ci = A->ci; view.va = A->va; view.va32 = A->va32;
   view.dinv = A->dinv; view.dinv32 = A->dinv32;
+  if (df) {
+    view.df = 1;
+    view.vadf = A->vadf;
+    view.dinvdf = A->dinvdf;
+  }
   view.b = reinterpret_cast<double*>(p); p += n8;
   view.x = reinterpret_cast<double*>(p); p += n8;
   view.r = reinterpret_cast<double*>(p); p += n8;
@@ -640,7 +656,8 @@ cudaError_t SystemSlot::start(const double* b, const double* x0, const SolvePara
   const size_t n = (size_t)view.n;
   NLGB_CUDA_TRY(cudaMemcpyAsync(const_cast<double*>(view.b), b, n * sizeof(double), cudaMemcpyDefault, s));
   if (x0) NLGB_CUDA_TRY(cudaMemcpyAsync(view.x, x0, n * sizeof(double), cudaMemcpyDefault, s));
-  else NLGB_CUDA_TRY(cudaMemsetAsync(view.x, 0, n * sizeof(double), s));
+  else NLGB_CUDA_TRY(cudaMemsetAsync(view.x, 0, n * sizeof(double), s));   // 0.0 in either form
+  if (df && x0) NLGB_CUDA_TRY(df_pack(view.x, (long long)n, s));
   if (mixed) {
     NLGB_CUDA_TRY(cudaMemsetAsync(view.p32, 0, n * sizeof(float), s));
     NLGB_CUDA_TRY(cudaMemsetAsync(view.c32, 0, n * sizeof(float), s));

@@ -82,10 +82,13 @@ struct SystemSlot {
   void* block = nullptr;
   size_t bytes = 0;
   bool mixed = false;
+  bool df = false;     // double-float iteration: x holds float pairs until df_unpack
   SysView view{};
   static size_t bytes_for(int n, int tile_rows, bool mixed);
-  cudaError_t alloc(DeviceCRS* A, bool mixed, cudaStream_t s);
-  // b, x0: host or device vectors of n doubles (x0 may be null: zero start).
+  // df: A must have its double-float copies (crs_prepare_df said usable).
+  cudaError_t alloc(DeviceCRS* A, bool mixed, cudaStream_t s, bool df = false);
+  // b, x0: host or device vectors of n doubles (x0 may be null: zero start);
+  // a double-float slot packs x after the upload.
   cudaError_t start(const double* b, const double* x0, const SolveParams& prm, cudaStream_t s);
   void release(cudaStream_t s);
 };

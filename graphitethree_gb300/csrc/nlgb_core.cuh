@@ -17,6 +17,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "nlgb_df.cuh"
+
 namespace nlgb {
 
 constexpr int kCTA = 256;            // threads per CTA for every solver kernel
@@ -100,12 +102,15 @@ struct SysView {
   int tile_rows;         // rows per tile (even; the autotuner uses multiples of 128)
   int n_tiles;
   int tpr;               // threads per row used by the SpMV (1..32)
+  int df;                // 1: double-float iteration (x, r, p, q hold float2 pairs)
   const int* rp;         // CRS row pointers (n+1)
   const int* ci;         // CRS column indices
   const double* va;      // FP64 values
   const float* va32;     // FP32 values (mixed), may be null
+  const float2* vadf;    // double-float values, may be null
   const double* dinv;    // Jacobi: 1/diag (1 where diag == 0)
   const float* dinv32;
+  const float2* dinvdf;
   const double* b;
   double* x;
   double* r;
@@ -342,6 +347,254 @@ __device__ double tile_true_rr(const SysView& s, int tile) {
     });
   block_sum<1>(acc);
   return acc[0];
+}
+
+// ---------------------------------------------------------------------------
+// Double-float tile procedures: the FP64 iteration above (same phases, slots,
+// scalar steps and canonical reductions) with r, p, q and x holding (hi, lo)
+// float pairs in their 8-byte slots and the matrix and D^-1 read from
+// double-float copies, so that the iteration runs on the FP32 pipe.  The
+// initial and final residuals are FP64 (x converted on the fly).  A thread's
+// partial dot products are double-float; the CTA reduces them in
+// double-float (warp butterflies, then the eight warps in order) and hands
+// one double per value to the canonical tile reduction.
+// ---------------------------------------------------------------------------
+template <int K>
+__device__ __forceinline__ void df_block_sum(float2 (&v)[K], double (&out)[K]) {
+  __shared__ float2 red[K][kWarps];
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      float2 t;
+      t.x = __shfl_xor_sync(0xffffffffu, v[k].x, o);
+      t.y = __shfl_xor_sync(0xffffffffu, v[k].y, o);
+      v[k] = df::dadd(v[k], t);   // commutative: every lane ends with the same value
+    }
+  }
+  __syncthreads();   // protect red[] from a previous use
+  if (l == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) red[k][w] = v[k];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    float2 s = red[k][0];
+#pragma unroll
+    for (int i = 1; i < kWarps; ++i) s = df::dadd(s, red[k][i]);
+    out[k] = df::to_double(s);
+  }
+}
+
+// a_row . x in double-float with T threads per row (all 32 lanes call it).
+template <int T, bool kCoh>
+__device__ __forceinline__ float2 row_dot_df(const int* __restrict__ rp, const int* __restrict__ ci,
+                                             const float2* __restrict__ va, const float2* __restrict__ x,
+                                             int row, bool valid, int lane) {
+  float2 sum = df::make(0.f, 0.f);
+  if (valid) {
+    const int k0 = __ldg(rp + row), k1 = __ldg(rp + row + 1);
+#pragma unroll 2
+    for (int k = k0 + lane; k < k1; k += T) {
+      const int c = __ldg(ci + k);
+      const float2 xc = kCoh ? __ldcg(x + c) : __ldg(x + c);
+      sum = df::mac(sum, __ldg(va + k), xc);
+    }
+  }
+#pragma unroll
+  for (int o = T / 2; o > 0; o >>= 1) {
+    float2 t;
+    t.x = __shfl_xor_sync(0xffffffffu, sum.x, o);
+    t.y = __shfl_xor_sync(0xffffffffu, sum.y, o);
+    sum = df::dadd(sum, t);
+  }
+  return sum;
+}
+
+// a_row . x in FP64 with x held as double-float (initial / final residual).
+template <int T, bool kCoh>
+__device__ __forceinline__ double row_dot_xdf(const int* __restrict__ rp, const int* __restrict__ ci,
+                                              const double* __restrict__ va, const float2* __restrict__ x,
+                                              int row, bool valid, int lane) {
+  double sum = 0.0;
+  if (valid) {
+    const int k0 = __ldg(rp + row), k1 = __ldg(rp + row + 1);
+    for (int k = k0 + lane; k < k1; k += T) {
+      const int c = __ldg(ci + k);
+      const float2 xc = kCoh ? __ldcg(x + c) : __ldg(x + c);
+      sum = fma(__ldg(va + k), df::to_double(xc), sum);
+    }
+  }
+  return subwarp_sum<T, double>(sum);
+}
+
+// r = b - A x (FP64, rounded to double-float), p = D^-1 r; returns
+// (b.b, r.D^-1 r, r.r).
+template <int T, bool kCoh = false>
+__device__ void tile_df_residual(const SysView& s, int tile, double (&out)[3]) {
+  const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
+  const float2* x2 = reinterpret_cast<const float2*>(s.x);
+  float2* r2 = reinterpret_cast<float2*>(s.r);
+  float2* p2 = reinterpret_cast<float2*>(s.p);
+  const int sub = threadIdx.x / T, lane = threadIdx.x % T;
+  constexpr int RPP = kCTA / T;
+  double bb[1] = {0.0};
+  float2 v[2] = {df::make(0.f, 0.f), df::make(0.f, 0.f)};
+  for (int base = lo; base < hi; base += RPP) {
+    const int row = base + sub;
+    const bool valid = row < hi;
+    const double ax = row_dot_xdf<T, kCoh>(s.rp, s.ci, s.va, x2, row, valid, lane);
+    if (valid && lane == 0) {
+      const double bi = s.b[row];
+      const float2 ri = df::from_double(bi - ax);
+      const float2 zi = df::dmul(__ldg(s.dinvdf + row), ri);
+      r2[row] = ri;
+      p2[row] = zi;
+      bb[0] = fma(bi, bi, bb[0]);
+      v[0] = df::mac(v[0], zi, ri);
+      v[1] = df::mac(v[1], ri, ri);
+    }
+  }
+  double o[2];
+  df_block_sum<2>(v, o);
+  block_sum<1>(bb);
+  out[0] = bb[0]; out[1] = o[0]; out[2] = o[1];
+}
+
+// q = A p on the tile; returns sum_i p_i q_i.
+template <int T, bool kCoh = false>
+__device__ double tile_df_spmv_pq(const SysView& s, int tile) {
+  const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
+  const float2* p2 = reinterpret_cast<const float2*>(s.p);
+  float2* q2 = reinterpret_cast<float2*>(s.q);
+  const int sub = threadIdx.x / T, lane = threadIdx.x % T;
+  constexpr int RPP = kCTA / T;
+  float2 acc[1] = {df::make(0.f, 0.f)};
+  for (int base = lo; base < hi; base += RPP) {
+    const int row = base + sub;
+    const bool valid = row < hi;
+    const float2 qv = row_dot_df<T, kCoh>(s.rp, s.ci, s.vadf, p2, row, valid, lane);
+    if (valid && lane == 0) {
+      q2[row] = qv;
+      acc[0] = df::mac(acc[0], __ldcg(p2 + row), qv);
+    }
+  }
+  double o[1];
+  df_block_sum<1>(acc, o);
+  return o[0];
+}
+
+// x += a p, r -= a q; returns (r.D^-1 r, r.r).
+__device__ __forceinline__ void tile_df_update_xr(const SysView& s, int tile, double alpha,
+                                                  double (&out)[2]) {
+  const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
+  const float2 a = df::from_double(alpha), na = df::neg(a);
+  float4* x4 = reinterpret_cast<float4*>(s.x);
+  float4* r4 = reinterpret_cast<float4*>(s.r);
+  const float4* p4 = reinterpret_cast<const float4*>(s.p);
+  const float4* q4 = reinterpret_cast<const float4*>(s.q);
+  const float4* d4 = reinterpret_cast<const float4*>(s.dinvdf);
+  float2 v[2] = {df::make(0.f, 0.f), df::make(0.f, 0.f)};
+  pair_loop(lo, hi,
+    [&](int i2) {
+      const float4 xv = __ldcg(x4 + i2), rv = __ldcg(r4 + i2);
+      const float4 pv = __ldcg(p4 + i2), qv = __ldcg(q4 + i2), dv = __ldg(d4 + i2);
+      const float2 x0 = df::mac(df::make(xv.x, xv.y), a, df::make(pv.x, pv.y));
+      const float2 x1 = df::mac(df::make(xv.z, xv.w), a, df::make(pv.z, pv.w));
+      const float2 r0 = df::mac(df::make(rv.x, rv.y), na, df::make(qv.x, qv.y));
+      const float2 r1 = df::mac(df::make(rv.z, rv.w), na, df::make(qv.z, qv.w));
+      x4[i2] = make_float4(x0.x, x0.y, x1.x, x1.y);
+      r4[i2] = make_float4(r0.x, r0.y, r1.x, r1.y);
+      const float2 z0 = df::dmul(df::make(dv.x, dv.y), r0);
+      const float2 z1 = df::dmul(df::make(dv.z, dv.w), r1);
+      v[0] = df::mac(v[0], z0, r0); v[0] = df::mac(v[0], z1, r1);
+      v[1] = df::mac(v[1], r0, r0); v[1] = df::mac(v[1], r1, r1);
+    },
+    [&](int i) {
+      float2* x2 = reinterpret_cast<float2*>(s.x);
+      float2* r2 = reinterpret_cast<float2*>(s.r);
+      x2[i] = df::mac(__ldcg(x2 + i), a, __ldcg(reinterpret_cast<const float2*>(s.p) + i));
+      const float2 ri = df::mac(__ldcg(r2 + i), na, __ldcg(reinterpret_cast<const float2*>(s.q) + i));
+      r2[i] = ri;
+      const float2 zi = df::dmul(__ldg(s.dinvdf + i), ri);
+      v[0] = df::mac(v[0], zi, ri);
+      v[1] = df::mac(v[1], ri, ri);
+    });
+  df_block_sum<2>(v, out);
+}
+
+// p = D^-1 r + beta p.
+__device__ __forceinline__ void tile_df_update_p(const SysView& s, int tile, double beta) {
+  const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
+  const float2 bt = df::from_double(beta);
+  float4* p4 = reinterpret_cast<float4*>(s.p);
+  const float4* r4 = reinterpret_cast<const float4*>(s.r);
+  const float4* d4 = reinterpret_cast<const float4*>(s.dinvdf);
+  pair_loop(lo, hi,
+    [&](int i2) {
+      const float4 rv = __ldcg(r4 + i2), dv = __ldg(d4 + i2), pv = __ldcg(p4 + i2);
+      const float2 p0 = df::mac(df::dmul(df::make(dv.x, dv.y), df::make(rv.x, rv.y)), bt,
+                                df::make(pv.x, pv.y));
+      const float2 p1 = df::mac(df::dmul(df::make(dv.z, dv.w), df::make(rv.z, rv.w)), bt,
+                                df::make(pv.z, pv.w));
+      p4[i2] = make_float4(p0.x, p0.y, p1.x, p1.y);
+    },
+    [&](int i) {
+      float2* p2 = reinterpret_cast<float2*>(s.p);
+      const float2 zi = df::dmul(__ldg(s.dinvdf + i), __ldcg(reinterpret_cast<const float2*>(s.r) + i));
+      p2[i] = df::mac(zi, bt, __ldcg(p2 + i));
+    });
+}
+
+// ||b - A x||^2 on the tile (FP64, x held as double-float).
+template <int T, bool kCoh = false>
+__device__ double tile_df_true_rr(const SysView& s, int tile) {
+  const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
+  const float2* x2 = reinterpret_cast<const float2*>(s.x);
+  const int sub = threadIdx.x / T, lane = threadIdx.x % T;
+  constexpr int RPP = kCTA / T;
+  double acc[1] = {0.0};
+  for (int base = lo; base < hi; base += RPP) {
+    const int row = base + sub;
+    const bool valid = row < hi;
+    const double ax = row_dot_xdf<T, kCoh>(s.rp, s.ci, s.va, x2, row, valid, lane);
+    if (valid && lane == 0) {
+      const double ri = s.b[row] - ax;
+      acc[0] = fma(ri, ri, acc[0]);
+    }
+  }
+  block_sum<1>(acc);
+  return acc[0];
+}
+
+// Compile-time selection between the FP64 (D = false) and double-float
+// (D = true) procedures of the same phase.
+template <bool D, int T, bool kCoh = false>
+__device__ __forceinline__ void phase_residual(const SysView& s, int tile, double (&out)[3]) {
+  if constexpr (D) tile_df_residual<T, kCoh>(s, tile, out);
+  else tile_residual<T, kCoh>(s, tile, out);
+}
+template <bool D, int T, bool kCoh = false>
+__device__ __forceinline__ double phase_spmv_pq(const SysView& s, int tile) {
+  if constexpr (D) return tile_df_spmv_pq<T, kCoh>(s, tile);
+  else return tile_spmv_pq<T, kCoh>(s, tile);
+}
+template <bool D>
+__device__ __forceinline__ void phase_update_xr(const SysView& s, int tile, double alpha, double (&out)[2]) {
+  if constexpr (D) tile_df_update_xr(s, tile, alpha, out);
+  else tile_update_xr(s, tile, alpha, out);
+}
+template <bool D>
+__device__ __forceinline__ void phase_update_p(const SysView& s, int tile, double beta) {
+  if constexpr (D) tile_df_update_p(s, tile, beta);
+  else tile_update_p(s, tile, beta);
+}
+template <bool D, int T, bool kCoh = false>
+__device__ __forceinline__ double phase_true_rr(const SysView& s, int tile) {
+  if constexpr (D) return tile_df_true_rr<T, kCoh>(s, tile);
+  else return tile_true_rr<T, kCoh>(s, tile);
 }
 
 // ---------------------------------------------------------------------------

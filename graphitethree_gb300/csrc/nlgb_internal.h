@@ -39,6 +39,9 @@ struct DeviceCRS {
   float* va32 = nullptr;   // lazily built for the mixed-precision solver
   double* dinv = nullptr;  // Jacobi inverse diagonal (lazily built)
   float* dinv32 = nullptr;
+  float2* vadf = nullptr;    // double-float copies (hi, lo) of va and dinv,
+  float2* dinvdf = nullptr;  //   lazily built for the double-float solver
+  int df_state = 0;          // double-float range check: 0 not run, 1 usable, -1 out of range
   int tpr = 0;             // threads per row chosen by the autotuner
   int tile_rows = 0;
   int max_row = 0;         // longest row (nnz)
@@ -51,6 +54,15 @@ cudaError_t crs_adopt_device(DeviceCRS& A, int n, int m, long long nnz, int* rp,
                              double* va, cudaStream_t s);
 void crs_free(DeviceCRS& A);
 cudaError_t crs_prepare(DeviceCRS& A, bool need_fp32, cudaStream_t s);  // jacobi, fp32, tuning
+// crs_prepare plus the double-float copies; *usable is false (and no copy is
+// made) when a value or 1/diagonal lies outside [2^-100, 2^100] or is not
+// finite: the double-float iteration would lose its precision there, and
+// the caller runs FP64 instead.
+cudaError_t crs_prepare_df(DeviceCRS& A, bool* usable, cudaStream_t s);
+// In-place conversion of a device vector between FP64 and double-float
+// (hi, lo) pairs, element by element (stream-ordered).
+cudaError_t df_pack(double* x, long long n, cudaStream_t s);
+cudaError_t df_unpack(double* x, long long n, cudaStream_t s);
 long long device_bytes(const DeviceCRS& A);
 
 // Autotuner: threads per row and tile rows from the nnz-per-row histogram.
@@ -65,7 +77,7 @@ cudaError_t spmv32(const DeviceCRS& A, const float* x, float* y, cudaStream_t s)
 struct SolveParams {
   double eps = 1e-10;
   long long max_iter = -1;     // -1: 5 n
-  int precision = 0;           // 0 FP64, 1 mixed
+  int precision = 0;           // 0 FP64, 1 mixed, 3 double-float (NL_GB300_PRECISION_*)
   double inner_eps = 0.1;      // mixed: reliable update when the FP32 residual fell by this factor
   int max_outer = 100000;      // mixed: cap on reliable updates
   int tpr = 0;                 // 0: autotuned
@@ -79,9 +91,11 @@ struct SolveResult {
   double true_rel_residual = 0;  // ||b - A x|| / ||b|| recomputed in FP64
   double seconds = 0;
   double algo_bytes = 0;         // algorithmic HBM bytes of the solve
+  int precision = 0;             // precision that ran (0 FP64, 1 mixed, 3 double-float)
 };
 
-// Plain FP64 or mixed FP32/FP64-refined Jacobi-PCG on one resident matrix.
+// Plain FP64, double-float, or mixed FP32/FP64-refined Jacobi-PCG on one
+// resident matrix.
 // The whole iteration loop is a single CUDA-graph launch (while-conditional
 // node); the host waits once per solve.
 class PcgSolver {
@@ -99,10 +113,10 @@ class PcgSolver {
 
  private:
   cudaError_t alloc(bool mixed);
-  cudaError_t run_graph(bool mixed, const SolveParams& prm, long long max_iter, long long done,
-                        int outer, float* ms);
-  cudaError_t run_eager(bool mixed, SysState* h);
-  cudaError_t build_plain_graph();
+  cudaError_t run_graph(bool mixed, bool df, const SolveParams& prm, long long max_iter,
+                        long long done, int outer, float* ms);
+  cudaError_t run_eager(bool mixed, bool df, SysState* h);
+  cudaError_t build_plain_graph(bool df);
   cudaError_t build_mixed_graph();
   void release();
 
@@ -115,7 +129,7 @@ class PcgSolver {
   void* st_ = nullptr;          // SysState (device)
   void* st_host_ = nullptr;     // pinned staging
   const volatile int* abort_flag_ = nullptr;
-  cudaGraphExec_t plain_exec_ = nullptr, mixed_exec_ = nullptr;
+  cudaGraphExec_t plain_exec_ = nullptr, mixed_exec_ = nullptr, df_exec_ = nullptr;
   // single-kernel cooperative iterations (small and mid-size systems)
   bool use_coop_ = false;
   int coop_grid_ = 0;

@@ -306,6 +306,7 @@ extern "C" int nlgb_solve_noalloc(int n, const int* rp, const int* ci, const dou
     res->true_rel_residual = h.bnorm2 > 0 ? std::sqrt(h.rr_true / h.bnorm2) : 0.0;
     res->seconds = 0.0;
     res->algo_bytes = algo_bytes(n, nnz, h);
+    res->precision = NL_GB300_PRECISION_DOUBLE;
   }
   return NLGB_OK;
 }

@@ -91,7 +91,9 @@ double percentile(std::vector<double> v, double q) {
   return i + 1 < v.size() ? v[i] * (1.0 - f) + v[i + 1] * f : v[i];
 }
 
-size_t estimate_bytes(const Req& r, bool mixed) {
+size_t estimate_bytes(const Req& r, int precision) {
+  const bool mixed = precision == NL_GB300_PRECISION_MIXED;
+  const bool dfl = precision == NL_GB300_PRECISION_DOUBLE_FLOAT;
   const size_t slot = SystemSlot::bytes_for(r.n, 128, mixed);
   size_t nnz = 0, upload = 0;
   if (r.kind == 0) {
@@ -115,7 +117,8 @@ size_t estimate_bytes(const Req& r, bool mixed) {
     upload = (size_t)r.row_ptr[r.n_rows] * 24 + (size_t)r.n_rows * (16 + 8 * r.n_rhs) +
              (size_t)r.n_vars * 8 * r.n_rhs + (size_t)r.n * 8 * r.n_rhs;
   }
-  const size_t mat = (size_t)(r.n + 1) * 4 + nnz * (12 + (mixed ? 4 : 0)) + (size_t)r.n * 12;
+  const size_t mat = (size_t)(r.n + 1) * 4 + nnz * (12 + (mixed ? 4 : 0) + (dfl ? 8 : 0)) +
+                     (size_t)r.n * (12 + (dfl ? 8 : 0));
   return mat + upload + (size_t)r.n_rhs * slot;
 }
 
@@ -149,28 +152,36 @@ namespace {
 // Precision of one request: NL_GB300_PRECISION_AUTO runs square systems in
 // mixed precision and least-squares row submissions (normal equations,
 // kappa(A^T A) = kappa(A)^2, too ill-conditioned for FP32 values on meshes)
-// in FP64 from the start, instead of spending an FP32 phase before the
-// fallback.
+// in double-float from the start (FP64-class rounding on the FP32 pipe),
+// instead of spending an FP32 phase before the fallback.
+int req_precision(const nlgb_server_s* S, const Req& r) {
+  if (S->cfg.precision == NL_GB300_PRECISION_AUTO) {
+    const bool ls = (r.kind == 1 && r.least_squares) || (r.kind == 2 && r.mesh_kind == NLGB_MESH_LSCM);
+    return ls ? NL_GB300_PRECISION_DOUBLE_FLOAT : NL_GB300_PRECISION_MIXED;
+  }
+  return S->cfg.precision;
+}
 bool req_mixed(const nlgb_server_s* S, const Req& r) {
-  if (S->cfg.precision == NL_GB300_PRECISION_MIXED) return true;
-  if (S->cfg.precision == NL_GB300_PRECISION_AUTO)
-    return !((r.kind == 1 && r.least_squares) || (r.kind == 2 && r.mesh_kind == NLGB_MESH_LSCM));
-  return false;
+  return req_precision(S, r) == NL_GB300_PRECISION_MIXED;
 }
 
-SolveParams params_of(const nlgb_server_s* S, bool mixed) {
+SolveParams params_of(const nlgb_server_s* S, int precision) {
   SolveParams p;
   p.eps = S->cfg.eps;
   p.max_iter = S->cfg.max_iter;
-  p.precision = mixed ? NL_GB300_PRECISION_MIXED : NL_GB300_PRECISION_DOUBLE;
+  p.precision = precision;
   p.inner_eps = S->cfg.inner_eps;
   p.max_outer = 100000;
   return p;
 }
 
 // Upload / assemble a request on stream `s` and start its systems.
-bool admit(nlgb_server_s* S, Req* r, cudaStream_t s) {
-  const bool mixed = req_mixed(S, *r);
+// df_slots: the slots run the double-float iteration in the persistent
+// kernel (x packed as float pairs); the serial worker keeps FP64 slots and
+// lets the single-system solver convert.
+bool admit(nlgb_server_s* S, Req* r, cudaStream_t s, bool df_slots) {
+  const int prec = req_precision(S, *r);
+  const bool mixed = prec == NL_GB300_PRECISION_MIXED;
   cudaError_t e = cudaSuccess;
   if (r->kind == 0) {
     e = crs_upload(r->A, r->n, r->n, r->rp.data(), r->ci.data(), r->va.data(), s);
@@ -222,15 +233,17 @@ bool admit(nlgb_server_s* S, Req* r, cudaStream_t s) {
     cudaFree(drp); cudaFree(dcol); cudaFree(dval); cudaFree(drhs); cudaFree(dw); cudaFree(dxl);
   }
   if (e == cudaSuccess) e = crs_prepare(r->A, mixed, s);
+  bool dfl = false;   // false also when the matrix is outside double-float's range: FP64 runs
+  if (e == cudaSuccess && prec == NL_GB300_PRECISION_DOUBLE_FLOAT) e = crs_prepare_df(r->A, &dfl, s);
   if (e == cudaSuccess) {
     // true footprint now known
     const size_t actual = (size_t)device_bytes(r->A) + (size_t)r->n_rhs * SystemSlot::bytes_for(r->n, r->A.tile_rows, mixed);
     S->used = S->used - std::min(S->used, r->bytes) + actual;
     r->bytes = actual;
     r->slots.resize((size_t)r->n_rhs);
-    const SolveParams prm = params_of(S, mixed);
+    const SolveParams prm = params_of(S, prec);
     for (int k = 0; k < r->n_rhs && e == cudaSuccess; ++k) {
-      e = r->slots[k].alloc(&r->A, mixed, s);
+      e = r->slots[k].alloc(&r->A, mixed, s, dfl && df_slots);
       if (e != cudaSuccess) break;
       const double* bk = r->kind == 0 ? r->b.data() + (size_t)k * r->n : r->d_rhs + (size_t)k * r->n;
       const double* xk = r->x0.empty() ? nullptr : r->x0.data() + (size_t)k * r->n;
@@ -284,8 +297,10 @@ void finish_request(nlgb_server_s* S, Req* r, bool ok) {
   S->cv_done.notify_all();
 }
 
-void fill_result(nlgb_result& o, const SysState& h, double secs, long long n, long long nnz) {
+void fill_result(nlgb_result& o, const SysState& h, double secs, long long n, long long nnz,
+                 int precision) {
   o.algo_bytes = algo_bytes(n, nnz, h);
+  o.precision = precision;
   o.status = h.status;
   o.iterations = h.iter;
   o.refinement_steps = h.outer;
@@ -372,7 +387,7 @@ void worker_batched(nlgb_server_s* S) {
         S->st.peak_bytes = std::max(S->st.peak_bytes, S->used);
       }
       S->pending.erase(S->pending.begin() + (long)i);
-      if (admit(S, r, su)) {
+      if (admit(S, r, su, true)) {
         r->state = R_ACTIVE;
         S->active.push_back(r);
         active_systems += r->n_rhs;
@@ -473,7 +488,10 @@ void worker_batched(nlgb_server_s* S) {
         SysState h = states[i];
         if (h.stage != 3) h.status = ST_ABORTED;
         r->sys_done[k] = 1;
-        fill_result(r->res[k], h, bst.ms * 1e-3, r->A.n, r->A.nnz);
+        fill_result(r->res[k], h, bst.ms * 1e-3, r->A.n, r->A.nnz,
+                    r->slots[k].mixed ? NL_GB300_PRECISION_MIXED
+                                      : (r->slots[k].df ? NL_GB300_PRECISION_DOUBLE_FLOAT
+                                                        : NL_GB300_PRECISION_DOUBLE));
       }
     }
     for (size_t i = 0; i < S->active.size();) {
@@ -483,6 +501,7 @@ void worker_batched(nlgb_server_s* S) {
       if (!all) { ++i; continue; }
       bool ok = true;
       for (int k = 0; k < r->n_rhs; ++k) {
+        if (r->slots[k].df && df_unpack(r->slots[k].view.x, r->n, su) != cudaSuccess) ok = false;
         if (cudaMemcpyAsync(r->x_out + (size_t)k * r->n, r->slots[k].view.x, sizeof(double) * r->n,
                             cudaMemcpyDeviceToHost, su) != cudaSuccess) ok = false;
         if (r->res[k].status != NL_GB300_STATUS_CONVERGED) r->status = r->res[k].status;
@@ -514,7 +533,7 @@ void worker_serial(nlgb_server_s* S) {
     if (S->pending.empty()) continue;
     Req* r = S->pending.front();
     S->pending.erase(S->pending.begin());
-    r->bytes = estimate_bytes(*r, req_mixed(S, *r));
+    r->bytes = estimate_bytes(*r, req_precision(S, *r));
     S->used += r->bytes;
     {
       std::lock_guard<std::mutex> lk(S->mu);
@@ -522,8 +541,8 @@ void worker_serial(nlgb_server_s* S) {
     }
     // Reuse the admission upload/assembly, then solve each right-hand side
     // with the graph-captured single-system solver.
-    bool ok = admit(S, r, s);
-    const SolveParams prm = params_of(S, req_mixed(S, *r));
+    bool ok = admit(S, r, s, false);
+    const SolveParams prm = params_of(S, req_precision(S, *r));
     if (ok) {
       PcgSolver pcg;
       ok = pcg.bind(&r->A, s) == cudaSuccess;
@@ -539,6 +558,7 @@ void worker_serial(nlgb_server_s* S) {
         o.rel_residual = sr.rel_residual; o.true_rel_residual = sr.true_rel_residual;
         o.seconds = sr.seconds;
         o.algo_bytes = sr.algo_bytes;
+        o.precision = sr.precision;
         if (sr.status != NL_GB300_STATUS_CONVERGED) r->status = sr.status;
         std::lock_guard<std::mutex> lk(S->mu);
         S->st.kernel_s += sr.seconds;
@@ -604,7 +624,7 @@ nlgb_server nlgb_server_create(const nlgb_server_config* cfg) {
   if (S->cfg.epoch_iters <= 0) S->cfg.epoch_iters = 256;
   if (S->cfg.max_systems <= 0) S->cfg.max_systems = 8192;
   if (S->cfg.precision != NL_GB300_PRECISION_MIXED && S->cfg.precision != NL_GB300_PRECISION_DOUBLE &&
-      S->cfg.precision != NL_GB300_PRECISION_AUTO) {
+      S->cfg.precision != NL_GB300_PRECISION_AUTO && S->cfg.precision != NL_GB300_PRECISION_DOUBLE_FLOAT) {
     set_error("nlgb_server_create: unknown precision");
     delete S;
     return nullptr;
@@ -647,7 +667,7 @@ long long nlgb_server_submit_crs(nlgb_server S, int n, const int* rp, const int*
   if (x0) r->x0.assign(x0, x0 + (size_t)n * n_rhs);
   r->x_out = x_out;
   r->arrival = arrival_s;
-  r->bytes = estimate_bytes(*r, req_mixed(S, *r));
+  r->bytes = estimate_bytes(*r, req_precision(S, *r));
   return enqueue(S, std::move(r));
 }
 
@@ -692,7 +712,7 @@ long long nlgb_server_submit_mesh(nlgb_server S, int mesh_kind, int n_verts, con
   if (x0) r->x0.assign(x0, x0 + (size_t)n_rhs * r->n);
   r->x_out = x_out;
   r->arrival = arrival_s;
-  r->bytes = estimate_bytes(*r, req_mixed(S, *r));
+  r->bytes = estimate_bytes(*r, req_precision(S, *r));
   return enqueue(S, std::move(r));
 }
 
@@ -733,7 +753,7 @@ long long nlgb_server_submit_rows(nlgb_server S, int least_squares, long long n_
   if (x0) r->x0.assign(x0, x0 + (size_t)n_free * n_rhs);
   r->x_out = x_out;
   r->arrival = arrival_s;
-  r->bytes = estimate_bytes(*r, req_mixed(S, *r));
+  r->bytes = estimate_bytes(*r, req_precision(S, *r));
   return enqueue(S, std::move(r));
 }
 

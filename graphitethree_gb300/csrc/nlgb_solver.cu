@@ -50,10 +50,11 @@ __device__ __forceinline__ int ld_mode(const SysState* st) { return __ldcg(&st->
 // ---------------------------------------------------------------------------
 // Plain FP64 kernels.
 // ---------------------------------------------------------------------------
-template <int T>
+// D: double-float iteration (the same kernels on float pairs).
+template <int T, bool D>
 __global__ void __launch_bounds__(kCTA) k_init(SysView s) {
   double v[3];
-  tile_residual<T>(s, blockIdx.x, v);
+  phase_residual<D, T>(s, blockIdx.x, v);
   if (publish_elect<3>(s, blockIdx.x, v, kSlotInit, &s.st->cnt[0])) {
     const int comp[3] = {kSlotInit, kSlotInit + 1, kSlotInit + 2};
     double o[3];
@@ -62,10 +63,10 @@ __global__ void __launch_bounds__(kCTA) k_init(SysView s) {
   }
 }
 
-template <int T>
+template <int T, bool D>
 __global__ void __launch_bounds__(kCTA) k_spmv_pq(SysView s) {
   if (ld_status(s.st) != ST_RUNNING) return;
-  double v[1] = {tile_spmv_pq<T>(s, blockIdx.x)};
+  double v[1] = {phase_spmv_pq<D, T>(s, blockIdx.x)};
   if (publish_elect<1>(s, blockIdx.x, v, kSlotPQ, &s.st->cnt[1])) {
     const int comp[1] = {kSlotPQ};
     double o[1];
@@ -104,12 +105,13 @@ __device__ __forceinline__ bool elect_last(unsigned int* counter) {
   return am_last != 0;
 }
 
+template <bool D>
 __global__ void __launch_bounds__(kCTA) k_update_xr(SysView s) {
   if (ld_status(s.st) != ST_RUNNING) return;
   const double alpha = __ldcg(&s.st->alpha);
   for (int t = vec_t0(s), t1 = vec_t1(s); t < t1; ++t) {
     double v[2];
-    tile_update_xr(s, t, alpha, v);
+    phase_update_xr<D>(s, t, alpha, v);
     store_parts<2>(s, t, v, kSlotXR);
   }
   if (elect_last(&s.st->cnt[2])) {
@@ -120,10 +122,11 @@ __global__ void __launch_bounds__(kCTA) k_update_xr(SysView s) {
   }
 }
 
+template <bool D>
 __global__ void __launch_bounds__(kCTA) k_update_p(SysView s) {
   if (ld_status(s.st) != ST_RUNNING) return;
   const double beta = __ldcg(&s.st->beta);
-  for (int t = vec_t0(s), t1 = vec_t1(s); t < t1; ++t) tile_update_p(s, t, beta);
+  for (int t = vec_t0(s), t1 = vec_t1(s); t < t1; ++t) phase_update_p<D>(s, t, beta);
 }
 
 // ---------------------------------------------------------------------------
@@ -172,7 +175,7 @@ __device__ bool coop_grid_sync(unsigned long long* bar, unsigned long long targe
   return ok != 0;
 }
 
-template <int T>
+template <int T, bool D>
 __global__ void __launch_bounds__(kCTA) k_iter(SysView s, unsigned long long* bar) {
   __shared__ SysState sst;
   if (threadIdx.x == 0) sst = *s.st;      // written by the previous kernel
@@ -181,7 +184,7 @@ __global__ void __launch_bounds__(kCTA) k_iter(SysView s, unsigned long long* ba
   const int G = gridDim.x;
   const unsigned long long base = (unsigned long long)sst.coop_epoch * 2ULL * (unsigned long long)G;
   for (int t = blockIdx.x; t < s.n_tiles; t += G) {
-    const double v = tile_spmv_pq<T>(s, t);
+    const double v = phase_spmv_pq<D, T>(s, t);
     if (threadIdx.x == 0) __stcg(s.part + (size_t)t * kParts + kSlotPQ, v);
   }
   bool ok = coop_grid_sync(bar, base + G);
@@ -195,7 +198,7 @@ __global__ void __launch_bounds__(kCTA) k_iter(SysView s, unsigned long long* ba
       const double alpha = sst.alpha;
       for (int t = blockIdx.x; t < s.n_tiles; t += G) {
         double v[2];
-        tile_update_xr(s, t, alpha, v);
+        phase_update_xr<D>(s, t, alpha, v);
         if (threadIdx.x == 0) {
           __stcg(s.part + (size_t)t * kParts + kSlotXR, v[0]);
           __stcg(s.part + (size_t)t * kParts + kSlotXR + 1, v[1]);
@@ -212,7 +215,7 @@ __global__ void __launch_bounds__(kCTA) k_iter(SysView s, unsigned long long* ba
       __syncthreads();
       if (sst.status == ST_RUNNING) {
         const double beta = sst.beta;
-        for (int t = blockIdx.x; t < s.n_tiles; t += G) tile_update_p(s, t, beta);
+        for (int t = blockIdx.x; t < s.n_tiles; t += G) phase_update_p<D>(s, t, beta);
       }
     }
   }
@@ -257,13 +260,13 @@ __global__ void k_chunk_end(SysState* st) {
 }
 
 // ||b - A x||^2 of the final iterate; zeroes x when b == 0.
-template <int T>
+template <int T, bool D>
 __global__ void __launch_bounds__(kCTA) k_final(SysView s) {
   double v[1] = {0.0};
   if (__ldcg(&s.st->zero_rhs)) {
-    tile_zero_x(s, blockIdx.x);
+    tile_zero_x(s, blockIdx.x);   // all-zero bits: 0.0 in either representation
   } else {
-    v[0] = tile_true_rr<T>(s, blockIdx.x);
+    v[0] = phase_true_rr<D, T>(s, blockIdx.x);
   }
   if (publish_elect<1>(s, blockIdx.x, v, kSlotFinal, &s.st->cnt[3])) {
     const int comp[1] = {kSlotFinal};
@@ -369,6 +372,51 @@ __global__ void k_to_f32(long long n, const double* __restrict__ a, float* __res
     b[i] = float(a[i]);
 }
 
+__global__ void k_to_df(long long n, const double* __restrict__ a, float2* __restrict__ b) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    b[i] = df::from_double(a[i]);
+}
+
+// In place, element by element: a double becomes its (hi, lo) float pair in
+// the same 8 bytes, and back.
+__global__ void k_df_pack(long long n, double* x) {
+  float2* x2 = reinterpret_cast<float2*>(x);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double v = x[i];
+    x2[i] = df::from_double(v);
+  }
+}
+__global__ void k_df_unpack(long long n, double* x) {
+  float2* x2 = reinterpret_cast<float2*>(x);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float2 v = x2[i];
+    x[i] = df::to_double(v);
+  }
+}
+
+// Largest biased FP64 exponent of a[0..n) (2047 for Inf/NaN) and smallest
+// one among its nonzero entries (0 for subnormals): out[0] max, out[1] min.
+__global__ void k_exp_range(long long n, const double* __restrict__ a, int* out) {
+  int mx = 0, mn = 4096;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(a[i]);
+    if ((bits << 1) == 0ULL) continue;   // +-0
+    const int e = (int)((bits >> 52) & 0x7ffULL);
+    mx = max(mx, e);
+    mn = min(mn, e);
+  }
+  mx = __reduce_max_sync(0xffffffffu, mx);
+  mn = __reduce_min_sync(0xffffffffu, mn);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(out, mx);
+    atomicMin(out + 1, mn);
+  }
+}
+
 // Histogram of row lengths: bins 0..31 exact, bin 32 = longer; max length.
 __global__ void k_row_hist(int n, const int* __restrict__ rp, int* hist33, int* maxlen) {
   __shared__ int h[33];
@@ -416,23 +464,39 @@ static long long resident_slots() {
 // iteration, 834-1,024 CTAs 47-64 vs 39-50 us).
 constexpr long long kCoopMaxCtas = 640;
 
-static long long coop_wave(int tpr) {
-  const void* fn = nullptr;
+template <bool D>
+static const void* iter_kernel(int tpr) {
   switch (tpr) {
-    case 1: fn = (const void*)k_iter<1>; break;
-    case 2: fn = (const void*)k_iter<2>; break;
-    case 4: fn = (const void*)k_iter<4>; break;
-    case 8: fn = (const void*)k_iter<8>; break;
-    case 16: fn = (const void*)k_iter<16>; break;
-    default: fn = (const void*)k_iter<32>; break;
+    case 1: return (const void*)k_iter<1, D>;
+    case 2: return (const void*)k_iter<2, D>;
+    case 4: return (const void*)k_iter<4, D>;
+    case 8: return (const void*)k_iter<8, D>;
+    case 16: return (const void*)k_iter<16, D>;
+    default: return (const void*)k_iter<32, D>;
   }
-  int dev = 0, sms = 0, per_sm = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess ||
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kCTA, 0) != cudaSuccess) {
+}
+
+// Resident CTAs per SM of the single-kernel iteration: the smaller of its
+// FP64 and double-float forms, so that a matrix's layout and executor do not
+// depend on the precision it is solved in (0 if it cannot be queried).
+static int coop_per_sm(int tpr) {
+  int a = 0, b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, iter_kernel<false>(tpr), kCTA, 0) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, iter_kernel<true>(tpr), kCTA, 0) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
+  return std::min(a, b);
+}
+
+static long long coop_wave(int tpr) {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  const int per_sm = coop_per_sm(tpr);
   return std::min<long long>((long long)per_sm * sms, kCoopMaxCtas);
 }
 
@@ -531,6 +595,7 @@ void crs_free(DeviceCRS& A) {
   if (!A.owns) { A = DeviceCRS(); return; }
   cudaFree(A.rp); cudaFree(A.ci); cudaFree(A.va); cudaFree(A.va32);
   cudaFree(A.dinv); cudaFree(A.dinv32);
+  cudaFree(A.vadf); cudaFree(A.dinvdf);
   A = DeviceCRS();
 }
 
@@ -539,6 +604,8 @@ long long device_bytes(const DeviceCRS& A) {
   if (A.va32) b += A.nnz * 4;
   if (A.dinv) b += (long long)A.n * 8;
   if (A.dinv32) b += (long long)A.n * 4;
+  if (A.vadf) b += A.nnz * 8;
+  if (A.dinvdf) b += (long long)A.n * 8;
   return b;
 }
 
@@ -570,6 +637,67 @@ cudaError_t crs_prepare(DeviceCRS& A, bool need_fp32, cudaStream_t s) {
     NLGB_CUDA_TRY(cudaGetLastError());
   }
   return cudaSuccess;
+}
+
+// Exponent range [2^-100, 2^100] for the double-float copies: the low
+// halves (2^-24 of the high ones) stay normal floats, and products and sums
+// of a few such values stay finite.
+constexpr int kDfMinExp = 1023 - 100, kDfMaxExp = 1023 + 100;
+
+static cudaError_t exp_range(long long n, const double* a, int* host2, cudaStream_t s) {
+  host2[0] = 0; host2[1] = 4096;
+  if (n <= 0) return cudaSuccess;
+  int* d = nullptr;
+  NLGB_CUDA_TRY(cudaMallocAsync(&d, 2 * sizeof(int), s));
+  NLGB_CUDA_TRY(cudaMemcpyAsync(d, host2, 2 * sizeof(int), cudaMemcpyHostToDevice, s));
+  k_exp_range<<<grid_for(n, 256), 256, 0, s>>>(n, a, d);
+  count_launches(1);
+  NLGB_CUDA_TRY(cudaGetLastError());
+  NLGB_CUDA_TRY(cudaMemcpyAsync(host2, d, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  NLGB_CUDA_TRY(cudaStreamSynchronize(s));
+  NLGB_CUDA_TRY(cudaFreeAsync(d, s));
+  return cudaSuccess;
+}
+
+cudaError_t crs_prepare_df(DeviceCRS& A, bool* usable, cudaStream_t s) {
+  NLGB_CUDA_TRY(crs_prepare(A, false, s));
+  if (A.df_state == 0) {
+    int rv[2], rd[2];
+    NLGB_CUDA_TRY(exp_range(A.nnz, A.va, rv, s));
+    NLGB_CUDA_TRY(exp_range(A.n, A.dinv, rd, s));
+    const bool ok = rv[0] <= kDfMaxExp && rd[0] <= kDfMaxExp &&
+                    (A.nnz == 0 || rv[1] >= kDfMinExp) && (A.n == 0 || rd[1] >= kDfMinExp);
+    A.df_state = ok ? 1 : -1;
+  }
+  if (A.df_state > 0 && !A.vadf) {
+    NLGB_CUDA_TRY(cudaMalloc(&A.vadf, (size_t)std::max(1LL, A.nnz) * sizeof(float2)));
+    NLGB_CUDA_TRY(cudaMalloc(&A.dinvdf, (size_t)std::max(1, A.n) * sizeof(float2)));
+    if (A.nnz > 0) {
+      k_to_df<<<grid_for(A.nnz, 256), 256, 0, s>>>(A.nnz, A.va, A.vadf);
+      count_launches(1);
+    }
+    if (A.n > 0) {
+      k_to_df<<<grid_for(A.n, 256), 256, 0, s>>>(A.n, A.dinv, A.dinvdf);
+      count_launches(1);
+    }
+    NLGB_CUDA_TRY(cudaGetLastError());
+  }
+  *usable = A.df_state > 0;
+  return cudaSuccess;
+}
+
+cudaError_t df_pack(double* x, long long n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_df_pack<<<grid_for(n, 256), 256, 0, s>>>(n, x);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t df_unpack(double* x, long long n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_df_unpack<<<grid_for(n, 256), 256, 0, s>>>(n, x);
+  count_launches(1);
+  return cudaGetLastError();
 }
 
 template <typename V, typename X>
@@ -634,22 +762,28 @@ static cudaError_t add_while(cudaGraph_t g, cudaGraphNode_t* node, cudaGraphNode
   return add_cond(g, node, dep, h, cudaGraphCondTypeWhile, body);
 }
 
-template <int T> struct PlainKernels {
-  static const void* init() { return (const void*)k_init<T>; }
-  static const void* spmv() { return (const void*)k_spmv_pq<T>; }
-  static const void* fin() { return (const void*)k_final<T>; }
-  static const void* mx_outer() { return (const void*)k_mx_outer<T>; }
-  static const void* mx_spmv() { return (const void*)k_mx_spmv_pq<T>; }
-};
-
-struct KernelSet { const void *init, *spmv, *fin, *mx_outer, *mx_spmv, *iter; };
-static KernelSet kernels_for(int tpr) {
+// The kernels of one threads-per-row variant; df selects the double-float
+// form of the plain iteration (init, SpMV, vector updates, final residual).
+struct KernelSet { const void *init, *spmv, *fin, *mx_outer, *mx_spmv, *iter, *update_xr, *update_p; };
+template <int T, bool D>
+static KernelSet kernel_set() {
+  return {(const void*)k_init<T, D>, (const void*)k_spmv_pq<T, D>, (const void*)k_final<T, D>,
+          (const void*)k_mx_outer<T>, (const void*)k_mx_spmv_pq<T>, (const void*)k_iter<T, D>,
+          (const void*)k_update_xr<D>, (const void*)k_update_p<D>};
+}
+template <bool D>
+static KernelSet kernels_for_t(int tpr) {
   switch (tpr) {
-#define NLGB_KS(T) case T: return {PlainKernels<T>::init(), PlainKernels<T>::spmv(), PlainKernels<T>::fin(), PlainKernels<T>::mx_outer(), PlainKernels<T>::mx_spmv(), (const void*)k_iter<T>};
-    NLGB_KS(1) NLGB_KS(2) NLGB_KS(4) NLGB_KS(8) NLGB_KS(16)
-    default: return {PlainKernels<32>::init(), PlainKernels<32>::spmv(), PlainKernels<32>::fin(), PlainKernels<32>::mx_outer(), PlainKernels<32>::mx_spmv(), (const void*)k_iter<32>};
-#undef NLGB_KS
+    case 1: return kernel_set<1, D>();
+    case 2: return kernel_set<2, D>();
+    case 4: return kernel_set<4, D>();
+    case 8: return kernel_set<8, D>();
+    case 16: return kernel_set<16, D>();
+    default: return kernel_set<32, D>();
   }
+}
+static KernelSet kernels_for(int tpr, bool df) {
+  return df ? kernels_for_t<true>(tpr) : kernels_for_t<false>(tpr);
 }
 
 constexpr int kUnrollPlain = 4;   // CG iterations per while-body pass
@@ -662,7 +796,8 @@ PcgSolver::~PcgSolver() { release(); }
 void PcgSolver::release() {
   if (plain_exec_) cudaGraphExecDestroy(plain_exec_);
   if (mixed_exec_) cudaGraphExecDestroy(mixed_exec_);
-  plain_exec_ = mixed_exec_ = nullptr;
+  if (df_exec_) cudaGraphExecDestroy(df_exec_);
+  plain_exec_ = mixed_exec_ = df_exec_ = nullptr;
   cudaFree(b_); cudaFree(x_); cudaFree(r_); cudaFree(p_); cudaFree(q_); cudaFree(part_);
   cudaFree(coop_bar_);
   coop_bar_ = nullptr;
@@ -692,8 +827,7 @@ cudaError_t PcgSolver::bind(DeviceCRS* A, cudaStream_t stream) {
   use_coop_ = false;
   if (cudaGetDevice(&dev) == cudaSuccess &&
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernels_for(tpr_).iter, kCTA, 0) == cudaSuccess &&
-      per_sm > 0) {
+      (per_sm = coop_per_sm(tpr_)) > 0) {
     const long long wave = std::min<long long>((long long)per_sm * sms, kCoopMaxCtas);
     use_coop_ = n_tiles_ <= kCoopTilesPerCta * wave;
     coop_grid_ = (int)std::min<long long>(n_tiles_, wave);
@@ -730,22 +864,23 @@ cudaError_t PcgSolver::alloc(bool mixed) {
 
 static SysView make_view(DeviceCRS* A, int tile_rows, int n_tiles, double* b, double* x, double* r,
                          double* p, double* q, float* r32, float* p32, float* q32, float* c32,
-                         double* part, void* st, const volatile int* abort_flag) {
+                         double* part, void* st, const volatile int* abort_flag, bool df = false) {
   SysView v;
   std::memset(&v, 0, sizeof(v));
   v.n = A->n; v.tile_rows = tile_rows; v.n_tiles = n_tiles; v.tpr = A->tpr;
-  v.rp = A->rp; v.ci = A->ci; v.va = A->va; v.va32 = A->va32;
-  v.dinv = A->dinv; v.dinv32 = A->dinv32;
+  v.df = df ? 1 : 0;
+  v.rp = A->rp; v.ci = A->ci; v.va = A->va; v.va32 = A->va32; v.vadf = A->vadf;
+  v.dinv = A->dinv; v.dinv32 = A->dinv32; v.dinvdf = A->dinvdf;
   v.b = b; v.x = x; v.r = r; v.p = p; v.q = q;
   v.r32 = r32; v.p32 = p32; v.q32 = q32; v.c32 = c32;
   v.part = part; v.st = (SysState*)st; v.abort_flag = abort_flag;
   return v;
 }
 
-cudaError_t PcgSolver::build_plain_graph() {
+cudaError_t PcgSolver::build_plain_graph(bool df) {
   SysView v = make_view(A_, tile_rows_, n_tiles_, b_, x_, r_, p_, q_, nullptr, nullptr, nullptr,
-                        nullptr, part_, st_, abort_flag_);
-  const KernelSet ks = kernels_for(tpr_);
+                        nullptr, part_, st_, abort_flag_, df);
+  const KernelSet ks = kernels_for(tpr_, df);
   cudaGraph_t g;
   NLGB_CUDA_TRY(cudaGraphCreate(&g, 0));
   cudaGraphConditionalHandle h;
@@ -772,8 +907,8 @@ cudaError_t PcgSolver::build_plain_graph() {
     cudaGraphNode_t n1, n2, n3;
     NLGB_CUDA_TRY(add_kernel(body, &n1, prev, ks.spmv, n_tiles_, kCTA, a1));
     const int vg = (n_tiles_ + vec_tiles_for(tile_rows_) - 1) / vec_tiles_for(tile_rows_);
-    NLGB_CUDA_TRY(add_kernel(body, &n2, n1, (const void*)k_update_xr, vg, kCTA, a1));
-    NLGB_CUDA_TRY(add_kernel(body, &n3, n2, (const void*)k_update_p, vg, kCTA, a1));
+    NLGB_CUDA_TRY(add_kernel(body, &n2, n1, ks.update_xr, vg, kCTA, a1));
+    NLGB_CUDA_TRY(add_kernel(body, &n3, n2, ks.update_p, vg, kCTA, a1));
     prev = n3;
   }
   int need_mode = -1, use_handle = 1;
@@ -781,7 +916,7 @@ cudaError_t PcgSolver::build_plain_graph() {
   cudaGraphNode_t n_g;
   NLGB_CUDA_TRY(add_kernel(body, &n_g, prev, (const void*)k_guard, 1, 1, ag));
   NLGB_CUDA_TRY(add_kernel(g, &n_fin, n_loop, ks.fin, n_tiles_, kCTA, a1));
-  cudaError_t e = cudaGraphInstantiate(&plain_exec_, g, 0);
+  cudaError_t e = cudaGraphInstantiate(df ? &df_exec_ : &plain_exec_, g, 0);
   cudaGraphDestroy(g);
   NLGB_CUDA_TRY(e);
   return cudaSuccess;
@@ -790,7 +925,7 @@ cudaError_t PcgSolver::build_plain_graph() {
 cudaError_t PcgSolver::build_mixed_graph() {
   SysView v = make_view(A_, tile_rows_, n_tiles_, b_, x_, r_, p_, q_, r32_, p32_, q32_, c32_,
                         part_, st_, abort_flag_);
-  const KernelSet ks = kernels_for(tpr_);
+  const KernelSet ks = kernels_for(tpr_, false);
   // [initial FP64 residual] -> while { ( p update ; q = A32 p, p.q ;
   //   c/r update -> IF(update due) { x += c ; FP64 residual } ) x U ; guard }
   // -> final FP64 residual.
@@ -855,7 +990,7 @@ cudaError_t ViewGraph::build(const SysView& v) {
   if (!e0_) NLGB_CUDA_TRY(cudaEventCreate(&e0_));
   if (!e1_) NLGB_CUDA_TRY(cudaEventCreate(&e1_));
   view_ = v;
-  const KernelSet ks = kernels_for(v.tpr);
+  const KernelSet ks = kernels_for(v.tpr, v.df != 0);
   cudaGraph_t g;
   NLGB_CUDA_TRY(cudaGraphCreate(&g, 0));
   cudaGraphConditionalHandle h;
@@ -868,8 +1003,8 @@ cudaError_t ViewGraph::build(const SysView& v) {
   for (int u = 0; u < kUnrollPlain; ++u) {
     cudaGraphNode_t n1, n2, n3;
     NLGB_CUDA_TRY(add_kernel(body, &n1, prev, ks.spmv, v.n_tiles, kCTA, a1));
-    NLGB_CUDA_TRY(add_kernel(body, &n2, n1, (const void*)k_update_xr, vg, kCTA, a1));
-    NLGB_CUDA_TRY(add_kernel(body, &n3, n2, (const void*)k_update_p, vg, kCTA, a1));
+    NLGB_CUDA_TRY(add_kernel(body, &n2, n1, ks.update_xr, vg, kCTA, a1));
+    NLGB_CUDA_TRY(add_kernel(body, &n3, n2, ks.update_p, vg, kCTA, a1));
     prev = n3;
   }
   int need_mode = -1, use_handle = 1;
@@ -891,6 +1026,7 @@ cudaError_t ViewGraph::build(const SysView& v) {
 // different matrix, so every pointer and size is compared.
 static bool same_view(const SysView& a, const SysView& b) {
   return a.n == b.n && a.tile_rows == b.tile_rows && a.n_tiles == b.n_tiles && a.tpr == b.tpr &&
+         a.df == b.df && a.vadf == b.vadf && a.dinvdf == b.dinvdf &&
          a.rp == b.rp && a.ci == b.ci && a.va == b.va && a.dinv == b.dinv && a.b == b.b &&
          a.x == b.x && a.r == b.r && a.p == b.p && a.q == b.q && a.part == b.part && a.st == b.st &&
          a.abort_flag == b.abort_flag;
@@ -914,7 +1050,7 @@ cudaError_t ViewGraph::run(const SysView& v, long long iters, cudaStream_t s, fl
 
 // Eager mode: the chunk's kernels launched one by one (profiling only).
 cudaError_t ViewGraph::run_eager(cudaStream_t s, long long iters) {
-  const KernelSet ks = kernels_for(view_.tpr);
+  const KernelSet ks = kernels_for(view_.tpr, view_.df != 0);
   const int vg = (view_.n_tiles + vec_tiles_for(view_.tile_rows) - 1) / vec_tiles_for(view_.tile_rows);
   const cudaGraphConditionalHandle none = 0;
   const int need = -1, no_handle = 0;
@@ -928,8 +1064,8 @@ cudaError_t ViewGraph::run_eager(cudaStream_t s, long long iters) {
   for (long long pass = 0; pass * kUnrollPlain < std::max(1LL, iters) && status == ST_RUNNING; ++pass) {
     for (int u = 0; u < kUnrollPlain; ++u) {
       NLGB_CUDA_TRY(cudaLaunchKernel(ks.spmv, dim3(view_.n_tiles), dim3(kCTA), a1, 0, s));
-      NLGB_CUDA_TRY(cudaLaunchKernel((const void*)k_update_xr, dim3(vg), dim3(kCTA), a1, 0, s));
-      NLGB_CUDA_TRY(cudaLaunchKernel((const void*)k_update_p, dim3(vg), dim3(kCTA), a1, 0, s));
+      NLGB_CUDA_TRY(cudaLaunchKernel(ks.update_xr, dim3(vg), dim3(kCTA), a1, 0, s));
+      NLGB_CUDA_TRY(cudaLaunchKernel(ks.update_p, dim3(vg), dim3(kCTA), a1, 0, s));
       launched += 3;
     }
     NLGB_CUDA_TRY(cudaLaunchKernel((const void*)k_guard, dim3(1), dim3(1), ag, 0, s));
@@ -974,10 +1110,10 @@ static bool eager_mode() {
   return on;
 }
 
-cudaError_t PcgSolver::run_eager(bool mixed, SysState* h) {
+cudaError_t PcgSolver::run_eager(bool mixed, bool df, SysState* h) {
   SysView v = make_view(A_, tile_rows_, n_tiles_, b_, x_, r_, p_, q_, r32_, p32_, q32_, c32_,
-                        part_, st_, abort_flag_);
-  const KernelSet ks = kernels_for(tpr_);
+                        part_, st_, abort_flag_, df && !mixed);
+  const KernelSet ks = kernels_for(tpr_, df && !mixed);
   const int vg = (n_tiles_ + vec_tiles_for(tile_rows_) - 1) / vec_tiles_for(tile_rows_);
   const cudaGraphConditionalHandle none = 0;
   const int need = -1, no_handle = 0;
@@ -1001,8 +1137,8 @@ cudaError_t PcgSolver::run_eager(bool mixed, SysState* h) {
         NLGB_CUDA_TRY(go(ks.mx_outer, n_tiles_, kCTA, a1));
       } else {
         NLGB_CUDA_TRY(go(ks.spmv, n_tiles_, kCTA, a1));
-        NLGB_CUDA_TRY(go((const void*)k_update_xr, vg, kCTA, a1));
-        NLGB_CUDA_TRY(go((const void*)k_update_p, vg, kCTA, a1));
+        NLGB_CUDA_TRY(go(ks.update_xr, vg, kCTA, a1));
+        NLGB_CUDA_TRY(go(ks.update_p, vg, kCTA, a1));
       }
     }
     NLGB_CUDA_TRY(go((const void*)k_guard, 1, 1, ag));
@@ -1015,19 +1151,26 @@ cudaError_t PcgSolver::run_eager(bool mixed, SysState* h) {
   return cudaSuccess;
 }
 
-// Runs one graph (mixed or plain) on the internal b_ / x_; `done` > 0
+// Runs one graph (mixed, plain FP64 or plain double-float: df) on the
+// internal b_ / x_ (x_ already packed as double-float for df); `done` > 0
 // continues a mixed solve that fell back to FP64 after `done` iterations.
 // Leaves the final state in st_host_.
-cudaError_t PcgSolver::run_graph(bool mixed, const SolveParams& prm, long long max_iter,
+cudaError_t PcgSolver::run_graph(bool mixed, bool df, const SolveParams& prm, long long max_iter,
                                  long long done, int outer, float* ms) {
+  if (mixed) df = false;
+  cudaGraphExec_t* plain = df ? &df_exec_ : &plain_exec_;
   if (mixed && !mixed_exec_) NLGB_CUDA_TRY(build_mixed_graph());
-  if (!mixed && !plain_exec_) {
-    cudaError_t e = build_plain_graph();
+  if (!mixed && !*plain) {
+    cudaError_t e = build_plain_graph(df);
     if (e != cudaSuccess && use_coop_) {
       // cooperative kernel nodes refused here: one kernel per phase instead
+      // (both plain graphs are rebuilt so that they keep one executor)
       cudaGetLastError();
       use_coop_ = false;
-      e = build_plain_graph();
+      if (plain_exec_) cudaGraphExecDestroy(plain_exec_);
+      if (df_exec_) cudaGraphExecDestroy(df_exec_);
+      plain_exec_ = df_exec_ = nullptr;
+      e = build_plain_graph(df);
     }
     NLGB_CUDA_TRY(e);
   }
@@ -1058,9 +1201,9 @@ cudaError_t PcgSolver::run_graph(bool mixed, const SolveParams& prm, long long m
   }
   NLGB_CUDA_TRY(cudaEventRecord(ev0_, stream_));
   if (eager_mode()) {
-    NLGB_CUDA_TRY(run_eager(mixed, h));
+    NLGB_CUDA_TRY(run_eager(mixed, df, h));
   } else {
-    NLGB_CUDA_TRY(cudaGraphLaunch(mixed ? mixed_exec_ : plain_exec_, stream_));
+    NLGB_CUDA_TRY(cudaGraphLaunch(mixed ? mixed_exec_ : *plain, stream_));
   }
   NLGB_CUDA_TRY(cudaEventRecord(ev1_, stream_));
   NLGB_CUDA_TRY(cudaMemcpyAsync(h, st_, sizeof(SysState), cudaMemcpyDeviceToHost, stream_));
@@ -1081,15 +1224,20 @@ cudaError_t PcgSolver::run_graph(bool mixed, const SolveParams& prm, long long m
 
 cudaError_t PcgSolver::solve(const double* b, double* x, const SolveParams& prm, SolveResult* res) {
   const bool mixed = prm.precision == 1;
+  bool df = false;
   if (mixed) {
     NLGB_CUDA_TRY(crs_prepare(*A_, true, stream_));
     NLGB_CUDA_TRY(alloc(true));
+  } else if (prm.precision == 3) {
+    NLGB_CUDA_TRY(crs_prepare_df(*A_, &df, stream_));   // false: out of range, FP64 runs
   }
   const long long max_iter = prm.max_iter >= 0 ? prm.max_iter : 5LL * n_;
   NLGB_CUDA_TRY(cudaMemcpyAsync(b_, b, (size_t)n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
   NLGB_CUDA_TRY(cudaMemcpyAsync(x_, x, (size_t)n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
+  if (df) NLGB_CUDA_TRY(df_pack(x_, n_, stream_));
   float ms = 0.f;
-  NLGB_CUDA_TRY(run_graph(mixed, prm, max_iter, 0, 0, &ms));
+  NLGB_CUDA_TRY(run_graph(mixed, df, prm, max_iter, 0, 0, &ms));
+  if (df) NLGB_CUDA_TRY(df_unpack(x_, n_, stream_));
   SysState* h = (SysState*)st_host_;
   if (mixed && h->status == ST_STAGNATION && !h->fell_back) {
     // FP32 cannot track this system (kappa * u32 ~ 1): continue it with the
@@ -1097,7 +1245,7 @@ cudaError_t PcgSolver::solve(const double* b, double* x, const SolveParams& prm,
     const long long done = h->iter;
     const int outer = h->outer;
     float ms2 = 0.f;
-    NLGB_CUDA_TRY(run_graph(false, prm, max_iter, done, outer, &ms2));
+    NLGB_CUDA_TRY(run_graph(false, false, prm, max_iter, done, outer, &ms2));
     ms += ms2;
   }
   NLGB_CUDA_TRY(cudaMemcpyAsync(x, x_, (size_t)n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
@@ -1111,6 +1259,7 @@ cudaError_t PcgSolver::solve(const double* b, double* x, const SolveParams& prm,
     res->true_rel_residual = bb > 0 ? std::sqrt(h->rr_true / bb) : 0.0;
     res->seconds = ms * 1e-3;
     res->algo_bytes = algo_bytes(n_, A_->nnz, *h);
+    res->precision = mixed ? 1 : (df ? 3 : 0);
   }
   return cudaSuccess;
 }

@@ -21,7 +21,11 @@ from .systems import RowStream
 
 K = _lib.header_constants()
 PRECISION = {"double": K["NL_GB300_PRECISION_DOUBLE"], "fp64": K["NL_GB300_PRECISION_DOUBLE"],
-             "mixed": K["NL_GB300_PRECISION_MIXED"], "auto": K["NL_GB300_PRECISION_AUTO"]}
+             "mixed": K["NL_GB300_PRECISION_MIXED"], "auto": K["NL_GB300_PRECISION_AUTO"],
+             "df": K["NL_GB300_PRECISION_DOUBLE_FLOAT"],
+             "double-float": K["NL_GB300_PRECISION_DOUBLE_FLOAT"]}
+PRECISION_NAME = {K["NL_GB300_PRECISION_DOUBLE"]: "double", K["NL_GB300_PRECISION_MIXED"]: "mixed",
+                  K["NL_GB300_PRECISION_DOUBLE_FLOAT"]: "df"}
 STATUS = {K[n]: n.replace("NL_GB300_STATUS_", "").lower() for n in K if n.startswith("NL_GB300_STATUS_")}
 
 
@@ -38,6 +42,13 @@ class SolveInfo:
     true_rel_residual: float
     seconds: float
     algo_bytes: float = 0.0
+    precision: str = ""          # precision that ran: "double", "mixed" or "df"
+
+
+def _info(r) -> SolveInfo:
+    return SolveInfo(STATUS.get(r.status, str(r.status)), r.iterations, r.refinement_steps,
+                     r.rel_residual, r.true_rel_residual, r.seconds, r.algo_bytes,
+                     PRECISION_NAME.get(r.precision, str(r.precision)))
 
 
 def _ptr(a, t):
@@ -124,8 +135,7 @@ class Matrix:
         r = _lib.NlgbResult()
         _check(L.nlgb_solve(self._h, _ptr(b, None), _ptr(x, None), ctypes.byref(p), ctypes.byref(r)),
                "nlgb_solve")
-        return x, SolveInfo(STATUS.get(r.status, str(r.status)), r.iterations, r.refinement_steps,
-                            r.rel_residual, r.true_rel_residual, r.seconds, r.algo_bytes)
+        return x, _info(r)
 
     def solve_krylov(self, b, method: str = "bicgstab", x0=None, eps: float = 1e-10,
                      max_iter: int = -1, restart: int = 30, jacobi: bool = True):
@@ -149,8 +159,7 @@ class Matrix:
         r = _lib.NlgbResult()
         _check(L.nlgb_solve(self._h, ctypes.c_void_p(b_ptr), ctypes.c_void_p(x_ptr), ctypes.byref(p),
                             ctypes.byref(r)), "nlgb_solve")
-        return SolveInfo(STATUS.get(r.status, str(r.status)), r.iterations, r.refinement_steps,
-                         r.rel_residual, r.true_rel_residual, r.seconds, r.algo_bytes)
+        return _info(r)
 
 
 def batch_solve(mats, bs, x0s=None, eps: float = 1e-10, max_iter: int = -1,
@@ -170,8 +179,7 @@ def batch_solve(mats, bs, x0s=None, eps: float = 1e-10, max_iter: int = -1,
     R = (_lib.NlgbResult * n)()
     secs = ctypes.c_double()
     _check(L.nlgb_batch_solve(n, A, B, X, ctypes.byref(p), R, ctypes.byref(secs)), "nlgb_batch_solve")
-    infos = [SolveInfo(STATUS.get(r.status, str(r.status)), r.iterations, r.refinement_steps,
-                       r.rel_residual, r.true_rel_residual, r.seconds, r.algo_bytes) for r in R]
+    infos = [_info(r) for r in R]
     return xs, infos, secs.value
 
 
@@ -276,8 +284,7 @@ class Server:
         R = (_lib.NlgbResult * out.shape[0])()
         lat = ctypes.c_double()
         rc = _lib.load().nlgb_server_wait(self._h, ticket, R, ctypes.byref(lat))
-        infos = [SolveInfo(STATUS.get(r.status, str(r.status)), r.iterations, r.refinement_steps,
-                           r.rel_residual, r.true_rel_residual, r.seconds, r.algo_bytes) for r in R]
+        infos = [_info(r) for r in R]
         if rc != 0:
             raise SolverError(f"request {ticket} failed: {_lib.last_error()}")
         return out, infos, lat.value

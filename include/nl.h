@@ -85,7 +85,7 @@ typedef void*          NLContext;
 #define NL_NNZ                 0x10d
 #define NL_NB_SYSTEMS          0x10e
 /* library-specific parameters */
-#define NL_GB300_PRECISION         0x1a0 /* NL_GB300_PRECISION_DOUBLE/_MIXED/_AUTO */
+#define NL_GB300_PRECISION         0x1a0 /* NL_GB300_PRECISION_DOUBLE/_MIXED/_AUTO/_DOUBLE_FLOAT */
 #define NL_GB300_INNER_THRESHOLD   0x1a1 /* mixed: FP64 reliable update once the FP32 residual fell by this factor (default 0.1) */
 #define NL_GB300_REFINEMENT_STEPS  0x1a2 /* query: outer FP64 refinement steps used */
 #define NL_GB300_STATUS            0x1a3 /* query: NL_GB300_STATUS_* of the last solve */
@@ -96,10 +96,16 @@ typedef void*          NLContext;
 
 #define NL_GB300_PRECISION_DOUBLE 0x0
 #define NL_GB300_PRECISION_MIXED  0x1
-/* AUTO: FP64 for least-squares systems (normal equations: kappa(A^T A) =
- * kappa(A)^2, beyond what FP32 values can represent on mesh problems), mixed
- * for systems given as square rows or CRS. */
+/* AUTO: double-float for least-squares systems (normal equations:
+ * kappa(A^T A) = kappa(A)^2, beyond what FP32 values can represent on mesh
+ * problems), mixed for systems given as square rows or CRS. */
 #define NL_GB300_PRECISION_AUTO   0x2
+/* DOUBLE_FLOAT: the FP64 Jacobi-PCG (same stopping rule on the recursive
+ * residual, true FP64 residual reported) with r, p, q, x, the matrix and
+ * 1/diag held as unevaluated float pairs hi + lo (~48 significand bits)
+ * computed on the FP32 pipe; the initial and final residuals are FP64.
+ * Matrices with a value or 1/diagonal outside [2^-100, 2^100] run in FP64. */
+#define NL_GB300_PRECISION_DOUBLE_FLOAT 0x3
 
 #define NL_GB300_STATUS_NONE       0
 #define NL_GB300_STATUS_CONVERGED  1

@@ -31,8 +31,9 @@ typedef struct nlgb_matrix_s* nlgb_matrix;
 typedef struct {
     double    eps;            /* stop when ||b-Ax|| <= eps ||b||           */
     long long max_iter;       /* < 0: 5 n                                  */
-    int       precision;      /* NL_GB300_PRECISION_DOUBLE / _MIXED (_AUTO
-                                 = _MIXED for a matrix given directly)    */
+    int       precision;      /* NL_GB300_PRECISION_DOUBLE / _MIXED /
+                                 _DOUBLE_FLOAT (_AUTO = _MIXED for a matrix
+                                 given directly)                          */
     double    inner_eps;      /* mixed: reliable-update factor (0.1)       */
     int       max_outer;      /* mixed: cap on reliable updates (100000)   */
 } nlgb_params;
@@ -47,7 +48,11 @@ typedef struct {
     double    algo_bytes;         /* algorithmic HBM bytes moved by the solve:
                                      per FP64 iteration 12 nnz + 108 n, per FP32
                                      iteration 8 nnz + 56 n, per reliable update
-                                     12 nnz + 52 n, + initial/final residuals */
+                                     12 nnz + 52 n, + initial/final residuals;
+                                     a double-float iteration counts as FP64 */
+    int       precision;          /* precision that ran: NL_GB300_PRECISION_DOUBLE,
+                                     _MIXED (also after an FP64 fallback) or
+                                     _DOUBLE_FLOAT                         */
 } nlgb_result;
 
 /* ---- device / errors ---- */
@@ -182,7 +187,8 @@ typedef struct {
     size_t    hbm_budget_bytes;  /* admission limit (default 150e9)            */
     int       mode;              /* NLGB_SERVER_BATCHED / NLGB_SERVER_SERIAL    */
     int       precision;         /* NL_GB300_PRECISION_MIXED (default) / _DOUBLE /
-                                    _AUTO: FP64 for least-squares row
+                                    _DOUBLE_FLOAT / _AUTO: double-float for
+                                    least-squares row and LSCM mesh
                                     submissions, mixed for the others     */
     double    eps;               /* relative residual (default 1e-10)          */
     long long max_iter;          /* < 0: 5 n per system                         */
