@@ -9,8 +9,8 @@ log-uniform in [1e3, 1e6], square-ish grid patches with the seeded bump
 model, Poisson arrivals at `--rate` per second -- submitted through the C ABI
 (nlgb_server_submit_rows / _crs with host buffers) to the continuous-batching
 server (HBM budget 150 GB, precision AUTO: mixed FP32/FP64 with FP64
-fallback for square systems, double-float -- FP64-class float pairs on the
-FP32 pipe -- for least-squares normal equations) and drained.
+fallback for square systems, FP64 for least-squares normal equations) and
+drained.
 Every step re-submits the same sample from scratch (assembly, upload, solve,
 download: nothing is cached).
 
@@ -496,8 +496,7 @@ def config(args):
             "requests": args.requests, "rate_per_s": args.rate, "rel_residual": args.eps,
             "hbm_budget_gb": args.budget_gb,
             "precision": "auto: mixed FP32/FP64 (with FP64 fallback) for the square fairing "
-                         "systems, double-float (float pairs, ~48-bit significand, FP32 pipe; "
-                         "OpenNL's stopping rule) for the least-squares LSCM normal equations",
+                         "systems, FP64 for the least-squares LSCM normal equations",
             "l2": "inputs larger than L2 for the large requests; every step re-uploads and "
                   "re-assembles (no cached data)"}
 
@@ -583,8 +582,7 @@ def main():
                           "1.3M-unknown LSCM system (0.88 DRAM byte per algorithmic byte, "
                           "profiles/k_batch_lscm808.md)"}
     g_ach = g_bytes / g_s / 1e9 if g_s > 0 else 0.0
-    gr = {"bound": "hbm", "kernel": "PCG iteration graph (k_spmv_pq + k_update_xr + k_update_p; "
-                                    "double-float for the least-squares systems under AUTO), "
+    gr = {"bound": "hbm", "kernel": "FP64 PCG iteration graph (k_spmv_pq + k_update_xr + k_update_p), "
                                     "one launch per chunk of a large system",
           "achieved": g_ach, "peak": peak, "unit": "GB/s", "frac": g_ach / peak,
           "traffic": GRAPH_DRAM_PER_ALGO_BYTE * g_bytes / g_launches,
@@ -593,8 +591,8 @@ def main():
           "traffic_note": "dram read+write per launch, scaled from the ncu capture of k_spmv_pq on the "
                           "1.3M-unknown LSCM system (1.03 DRAM byte per algorithmic byte; the vector "
                           "kernels stream exactly their bytes), profiles/k_spmv_pq_lscm808_fairing2048.md"}
-    fp64_note = ("FP64 phases are co-limited by GB300's FP64 pipe (65-81 % busy in the captures); "
-                 "the double-float phases run on the FP32 pipe")
+    fp64_note = ("the FP64 phases are co-limited by GB300's FP64 pipe (65-81 % busy in the captures), "
+                 "not only by HBM")
     roofline, other = (gr, kb) if g_s > kb_s else (kb, gr)
     roofline = {**roofline, "fp64_note": fp64_note}
     statuses = [i.status for infos, _ in res_last for i in infos]
@@ -620,7 +618,7 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_wall / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64+df(f32 pairs)+f32",
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64",
         "data": "synthetic (seeded serving-stream sample; no public dataset)",
         "config": config(args),
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

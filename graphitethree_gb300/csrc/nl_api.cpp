@@ -262,11 +262,11 @@ void ij_to_rows(Context* c) {
 }
 
 // Upload the row stream and assemble the system on the GPU.
-// NL_GB300_PRECISION_AUTO: double-float for least-squares (normal-equation)
-// systems, mixed for square ones.
+// NL_GB300_PRECISION_AUTO: FP64 for least-squares (normal-equation) systems,
+// mixed for square ones.
 int effective_precision(const Context* c) {
   if (c->precision != NL_GB300_PRECISION_AUTO) return c->precision;
-  return c->least_squares ? NL_GB300_PRECISION_DOUBLE_FLOAT : NL_GB300_PRECISION_MIXED;
+  return c->least_squares ? NL_GB300_PRECISION_DOUBLE : NL_GB300_PRECISION_MIXED;
 }
 
 bool assemble(Context* c) {

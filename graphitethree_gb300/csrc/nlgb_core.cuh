@@ -389,20 +389,33 @@ __device__ __forceinline__ void df_block_sum(float2 (&v)[K], double (&out)[K]) {
 }
 
 // a_row . x in double-float with T threads per row (all 32 lanes call it).
+// The lane's products are summed unnormalised: the heads through TwoSum,
+// every error term into one float tail, normalised once at the end.  The
+// dependency chain per nonzero is then one addition deep, and the loop is
+// unrolled four times, so that more gathers are in flight (the FP32
+// arithmetic is far from any limit; the loop is bound by memory latency).
 template <int T, bool kCoh>
 __device__ __forceinline__ float2 row_dot_df(const int* __restrict__ rp, const int* __restrict__ ci,
                                              const float2* __restrict__ va, const float2* __restrict__ x,
                                              int row, bool valid, int lane) {
-  float2 sum = df::make(0.f, 0.f);
+  float hs = 0.f, tl = 0.f;
   if (valid) {
     const int k0 = __ldg(rp + row), k1 = __ldg(rp + row + 1);
-#pragma unroll 2
+#pragma unroll 4
     for (int k = k0 + lane; k < k1; k += T) {
       const int c = __ldg(ci + k);
       const float2 xc = kCoh ? __ldcg(x + c) : __ldg(x + c);
-      sum = df::mac(sum, __ldg(va + k), xc);
+      const float2 a = __ldg(va + k);
+      const float p = df::mul(a.x, xc.x);
+      float e = df::fma(a.x, xc.x, -p);
+      e = df::fma(a.x, xc.y, e);
+      e = df::fma(a.y, xc.x, e);
+      const float2 t = df::two_sum(hs, p);
+      hs = t.x;
+      tl = df::add(tl, df::add(t.y, e));
     }
   }
+  float2 sum = df::fast_two_sum(hs, tl);
 #pragma unroll
   for (int o = T / 2; o > 0; o >>= 1) {
     float2 t;

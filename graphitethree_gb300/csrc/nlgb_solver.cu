@@ -63,8 +63,10 @@ __global__ void __launch_bounds__(kCTA) k_init(SysView s) {
   }
 }
 
+// Eight CTAs per SM (32 registers): the tile autotuner sizes one wave of
+// CTAs on that residency.
 template <int T, bool D>
-__global__ void __launch_bounds__(kCTA) k_spmv_pq(SysView s) {
+__global__ void __launch_bounds__(kCTA, 8) k_spmv_pq(SysView s) {
   if (ld_status(s.st) != ST_RUNNING) return;
   double v[1] = {phase_spmv_pq<D, T>(s, blockIdx.x)};
   if (publish_elect<1>(s, blockIdx.x, v, kSlotPQ, &s.st->cnt[1])) {

@@ -96,15 +96,18 @@ typedef void*          NLContext;
 
 #define NL_GB300_PRECISION_DOUBLE 0x0
 #define NL_GB300_PRECISION_MIXED  0x1
-/* AUTO: double-float for least-squares systems (normal equations:
- * kappa(A^T A) = kappa(A)^2, beyond what FP32 values can represent on mesh
- * problems), mixed for systems given as square rows or CRS. */
+/* AUTO: FP64 for least-squares systems (normal equations: kappa(A^T A) =
+ * kappa(A)^2, beyond what FP32 values can represent on mesh problems), mixed
+ * for systems given as square rows or CRS. */
 #define NL_GB300_PRECISION_AUTO   0x2
 /* DOUBLE_FLOAT: the FP64 Jacobi-PCG (same stopping rule on the recursive
  * residual, true FP64 residual reported) with r, p, q, x, the matrix and
  * 1/diag held as unevaluated float pairs hi + lo (~48 significand bits)
  * computed on the FP32 pipe; the initial and final residuals are FP64.
- * Matrices with a value or 1/diagonal outside [2^-100, 2^100] run in FP64. */
+ * Matrices with a value or 1/diagonal outside [2^-100, 2^100] run in FP64.
+ * Opt-in: on very ill-conditioned systems (kappa ~ 1e10) it needs more
+ * iterations than FP64 and its recursive residual drifts further from the
+ * true one. */
 #define NL_GB300_PRECISION_DOUBLE_FLOAT 0x3
 
 #define NL_GB300_STATUS_NONE       0

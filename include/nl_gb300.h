@@ -187,7 +187,7 @@ typedef struct {
     size_t    hbm_budget_bytes;  /* admission limit (default 150e9)            */
     int       mode;              /* NLGB_SERVER_BATCHED / NLGB_SERVER_SERIAL    */
     int       precision;         /* NL_GB300_PRECISION_MIXED (default) / _DOUBLE /
-                                    _DOUBLE_FLOAT / _AUTO: double-float for
+                                    _DOUBLE_FLOAT / _AUTO: FP64 for
                                     least-squares row and LSCM mesh
                                     submissions, mixed for the others     */
     double    eps;               /* relative residual (default 1e-10)          */

@@ -120,7 +120,7 @@ def test_builders_reject_bad_input(gpu_ok):
 def test_server_mesh_requests(gpu_ok, precision):
     """Mesh submissions: the server builds the systems on the GPU at
     admission; the results equal the builder + single-system solve, bit for
-    bit (same matrix bits, same iterates), LSCM in double-float under AUTO."""
+    bit (same matrix bits, same iterates), LSCM in FP64 under AUTO."""
     V1, F1 = meshes.height_field(36, 30, seed=11)
     V2, F2 = meshes.height_field(44, 40, seed=12)
     fs = systems.fairing_system(44, 40, seed=12, n_rhs=2)
@@ -132,7 +132,7 @@ def test_server_mesh_requests(gpu_ok, precision):
     srv.close()
     M1, rhs1, _ = solver.build_lscm(V1, F1)
     M2, _ = solver.build_fairing(V2, F2, 1e-2)
-    p1 = "df" if precision == "auto" else "mixed"
+    p1 = "double" if precision == "auto" else "mixed"
     xs1, is1 = M1.solve(rhs1, precision=p1)
     assert i1[0].status == "converged" and np.array_equal(x1[0], xs1)
     if precision == "auto":

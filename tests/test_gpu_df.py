@@ -7,8 +7,8 @@ near the threshold; the solution against the oracle's direct solve; the
 iteration count close to FP64's; bit-identical results on every executor
 (cooperative single-kernel graph, three-kernel graph, persistent batched
 kernel, server epochs and graph chunks, serial server); the FP64 fallback
-for a matrix outside double-float's exponent range; AUTO picking
-double-float for least-squares systems through the OpenNL context API."""
+for a matrix outside double-float's exponent range; the OpenNL context API
+with NL_GB300_PRECISION_DOUBLE_FLOAT."""
 import numpy as np
 import pytest
 
@@ -83,20 +83,20 @@ def test_df_same_on_every_executor(gpu_ok):
 
 
 def test_df_in_mix_equals_alone(gpu_ok):
-    """Double-float, FP64 and mixed systems side by side in one batched
-    server (AUTO and explicit): each equals its own solve alone."""
+    """Double-float least-squares and square systems side by side in one
+    batched server: each equals its own solve alone."""
     reqs = [("rows", systems.lscm_system(50, 47, seed=21)),
             ("square", systems.fairing_system(80, 75, seed=22)),
             ("rows", systems.lscm_system(90, 80, seed=23))]
     alone = []
     for kind, obj in reqs:
-        srv = solver.Server(precision="auto")
+        srv = solver.Server(precision="df")
         t = srv.submit_rows(obj) if kind == "rows" else srv.submit_square(obj)
         x, infs, _ = srv.wait(t)
         alone.append((x.copy(), [i.iterations for i in infs], [i.precision for i in infs]))
         srv.close()
-    assert alone[0][2] == ["df"] and alone[1][2][0] == "mixed"
-    srv = solver.Server(precision="auto", epoch_iters=48)
+    assert alone[0][2] == ["df"] and alone[1][2][0] == "df"
+    srv = solver.Server(precision="df", epoch_iters=48)
     ts = [srv.submit_rows(o, 0.001 * i) if k == "rows" else srv.submit_square(o, 0.001 * i)
           for i, (k, o) in enumerate(reqs)]
     for t, (xa, ia, pa) in zip(ts, alone):
@@ -134,13 +134,14 @@ def test_df_out_of_range_runs_fp64(gpu_ok):
     assert np.array_equal(x, x64) and info.iterations == i64.iterations
 
 
-def test_opennl_auto_least_squares_is_double_float(gpu_ok):
-    """OpenNL context API: NL_GB300_PRECISION_AUTO solves a least-squares
-    system in double-float; the result equals the explicit double-float
-    solve and is within 1e-8 of FP64's at eps = 1e-12."""
+def test_opennl_context_double_float(gpu_ok):
+    """OpenNL context API: NL_GB300_PRECISION_DOUBLE_FLOAT on a
+    least-squares system is within 1e-8 of FP64's solution at eps = 1e-12,
+    and AUTO stays FP64 for least-squares systems (bit-identical to it)."""
     rs = systems.lscm_system(40, 36, seed=41)
     xa, ia = solver.solve_opennl(rs, precision="auto", eps=1e-12)
     xf, if_ = solver.solve_opennl(rs, precision="df", eps=1e-12)
     xd, id_ = solver.solve_opennl(rs, precision="double", eps=1e-12)
-    assert np.array_equal(xa, xf) and ia["iterations"] == if_["iterations"]
-    assert rel(xa, xd) <= 1e-8
+    assert if_["ok"] and if_["status"] == "converged"
+    assert np.array_equal(xa, xd) and ia["iterations"] == id_["iterations"]
+    assert rel(xf, xd) <= 1e-8

@@ -115,24 +115,24 @@ def test_abort_fails_waiting_requests(gpu_ok):
     srv.close()
 
 
-def test_auto_precision_least_squares_in_double_float(gpu_ok):
-    """AUTO: least-squares row submissions start in double-float (no FP32
-    phase, no reliable update; iterates identical to the double-float
-    server), square systems run in mixed precision (reliable updates, same
-    result as the mixed server)."""
+def test_auto_precision_least_squares_in_fp64(gpu_ok):
+    """AUTO: least-squares row submissions start in FP64 (no FP32 phase, no
+    reliable update; iterates identical to the FP64 server), square systems
+    run in mixed precision (reliable updates, same result as the mixed
+    server)."""
     rs = systems.lscm_system(44, 41, seed=11)
     fs = systems.fairing_system(64, 60, seed=12)
     out = {}
-    for precision in ("auto", "df", "mixed"):
+    for precision in ("auto", "double", "mixed"):
         srv = solver.Server(precision=precision)
         t1, t2 = srv.submit_rows(rs), srv.submit_square(fs)
         out[precision] = (srv.wait(t1), srv.wait(t2))
         srv.close()
     (xa1, ia1, _), (xa2, ia2, _) = out["auto"]
-    (xd1, id1, _), _ = out["df"]
+    (xd1, id1, _), _ = out["double"]
     _, (xm2, im2, _) = out["mixed"]
     assert ia1[0].status == "converged" and ia1[0].refinement_steps == 0
-    assert ia1[0].precision == id1[0].precision == "df"
+    assert ia1[0].precision == id1[0].precision == "double"
     assert np.array_equal(xa1, xd1) and ia1[0].iterations == id1[0].iterations
     assert all(i.status == "converged" and i.refinement_steps >= 1 for i in ia2)
     assert all(i.precision == "mixed" for i in ia2)
