@@ -127,7 +127,13 @@ class Matrix:
 
     def solve(self, b, x0=None, eps: float = 1e-10, max_iter: int = -1, precision: str = "double",
               inner_eps: float = 0.1, max_outer: int = 100000):
-        """Solve A x = b.  Host numpy arrays in and out.  Returns (x, SolveInfo)."""
+        """Solve A x = b.  Host numpy arrays in and out.  Returns (x, SolveInfo).
+
+        precision: "double" (OpenNL's FP64 PCG), "mixed" (FP32 inner, FP64
+        reliable updates, FP64 fallback), "df" (OpenNL's PCG in double-float
+        on the FP32 pipe; FP64 for matrices outside its exponent range) or
+        "auto" (mixed for a matrix given directly).  SolveInfo.precision
+        says which ran."""
         L = _lib.load()
         b = np.ascontiguousarray(b, np.float64)
         x = np.zeros(self.n) if x0 is None else np.array(x0, np.float64, copy=True)

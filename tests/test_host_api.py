@@ -38,6 +38,9 @@ def test_parameters_roundtrip(ctx):
     assert nl.nlGetIntegerv(nl.NL_MAX_ITERATIONS) == 123
     assert nl.nlGetIntegerv(nl.NL_GB300_PRECISION) == nl.NL_GB300_PRECISION_MIXED
     assert nl.nlGetError() == nl.NL_NO_ERROR
+    nl.nlSolverParameteri(nl.NL_GB300_PRECISION, nl.NL_GB300_PRECISION_DOUBLE_FLOAT)
+    assert nl.nlGetIntegerv(nl.NL_GB300_PRECISION) == nl.NL_GB300_PRECISION_DOUBLE_FLOAT
+    assert nl.nlGetError() == nl.NL_NO_ERROR
     nl.nlSolverParameteri(nl.NL_GB300_PRECISION, nl.NL_GB300_PRECISION_AUTO)
     assert nl.nlGetIntegerv(nl.NL_GB300_PRECISION) == nl.NL_GB300_PRECISION_AUTO
     nl.nlSolverParameteri(nl.NL_GB300_PRECISION, 7)
