@@ -8,6 +8,10 @@ arm may import this module; the library never does.
 * ``pcg``: FP64 Jacobi-PCG with OpenMP threads (C), the timed CPU baseline
   and the iterative oracle.
 * ``direct_solve``: scipy SuperLU, the FP64 direct oracle.
+* ``pcg_df``: numpy restatement of the double-float Jacobi-PCG (float pairs
+  hi + lo, error-free transformations in float32), for the algorithm's
+  numerical behaviour (iteration growth, accuracy), not its bits: its sums
+  run in row order, the GPU's in tiles.
 * ``dense_normal_equations``: an independent numpy restatement used to pin
   ``assemble`` (no shared code with the C path).
 
@@ -293,6 +297,121 @@ def gmres(rp, ci, va, b, x0=None, eps: float = 1e-10, restart: int = 30,
         for i in range(k - 1, -1, -1):
             y[i] = (g[i] - H[i, i + 1:k] @ y[i + 1:k]) / H[i, i]
         x = x + dinv * (V[:k].T @ y)
+
+
+# --- double-float restatement -------------------------------------------
+# Float pairs hi + lo with the error-free transformations of the GPU's
+# double-float arithmetic: Knuth's TwoSum, Dekker's Fast2Sum and the
+# TwoProduct, composed as Dekker's double-length addition / multiplication.
+# numpy float32 operations round like the FP32 pipe; the TwoProduct's FMA is
+# formed in float64, where the product of two floats is exact, then rounded
+# once more to float32 (an exact FMA except for rare double roundings).
+
+_f32, _f64 = np.float32, np.float64
+
+
+def _two_sum(a, b):
+    s = a + b
+    bb = s - a
+    return s, (a - (s - bb)) + (b - bb)
+
+
+def _fast_two_sum(a, b):
+    s = a + b
+    return s, b - (s - a)
+
+
+def _fma32(a, b, c):
+    return (a.astype(_f64) * b.astype(_f64) + c.astype(_f64)).astype(_f32)
+
+
+def _df(d):
+    d = np.asarray(d, _f64)
+    hi = d.astype(_f32)
+    return hi, (d - hi.astype(_f64)).astype(_f32)
+
+
+def _df_to64(h, l):
+    return h.astype(_f64) + l.astype(_f64)
+
+
+def _df_add(ah, al, bh, bl):
+    s, e = _two_sum(ah, bh)
+    return _fast_two_sum(s, e + (al + bl))
+
+
+def _df_mul(ah, al, bh, bl):
+    p = ah * bh
+    e = _fma32(ah, bh, -p)
+    e = _fma32(ah, bl, e)
+    e = _fma32(al, bh, e)
+    return _fast_two_sum(p, e)
+
+
+def pcg_df(rp, ci, va, b, eps: float = 1e-10, max_iter: int | None = None):
+    """Double-float Jacobi-PCG (OpenNL's recurrence and stopping rule on the
+    recursive residual, zero start).  Returns (x, status, iterations,
+    true_rel_residual) with status 1 converged, 2 max iterations."""
+    rp = np.asarray(rp, np.int64); ci = np.asarray(ci, np.int64)
+    va = np.asarray(va, _f64); b = np.asarray(b, _f64)
+    n = rp.shape[0] - 1
+    max_iter = 5 * n if max_iter is None else max_iter
+    lens = np.diff(rp)
+    cols = [(np.nonzero(lens > j)[0], None) for j in range(int(lens.max(initial=0)))]
+    cols = [(idx, rp[idx] + j) for j, (idx, _) in enumerate(cols)]
+    vh, vl = _df(va)
+    row = np.repeat(np.arange(n), lens)
+    diag = np.zeros(n)
+    np.add.at(diag, row[ci == row], va[ci == row])
+    dh, dl = _df(np.where(diag != 0.0, 1.0 / np.where(diag != 0.0, diag, 1.0), 1.0))
+
+    def spmv(xh, xl):   # row by row in column order, double-float sums
+        sh = np.zeros(n, _f32); sl = np.zeros(n, _f32)
+        for idx, k in cols:
+            ph, pl = _df_mul(vh[k], vl[k], xh[ci[k]], xl[ci[k]])
+            sh[idx], sl[idx] = _df_add(sh[idx], sl[idx], ph, pl)
+        return sh, sl
+
+    def dot(ah, al, bh, bl):
+        return float(np.sum(_df_to64(*_df_mul(ah, al, bh, bl))))
+
+    xh = np.zeros(n, _f32); xl = np.zeros(n, _f32)
+    rh, rl = _df(b)
+    ph, pl = _df_mul(dh, dl, rh, rl)
+    bb = float(b @ b)
+    rho = dot(ph, pl, rh, rl)
+    it, status = 0, 2
+    if not bb > 0.0:
+        return np.zeros(n), 1, 0, 0.0
+    while it < max_iter:
+        qh, ql = spmv(ph, pl)
+        alpha = rho / dot(ph, pl, qh, ql)
+        ah, al = _df(alpha)
+        xh, xl = _df_add(xh, xl, *_df_mul(ah, al, ph, pl))
+        rh, rl = _df_add(rh, rl, *_df_mul(-ah, -al, qh, ql))
+        zh, zl = _df_mul(dh, dl, rh, rl)
+        rz = dot(zh, zl, rh, rl)
+        rr = dot(rh, rl, rh, rl)
+        it += 1
+        if rr <= eps * eps * bb:
+            status = 1
+            break
+        beta = rz / rho
+        rho = rz
+        bh_, bl_ = _df(beta)
+        ph, pl = _df_add(zh, zl, *_df_mul(bh_, bl_, ph, pl))
+    x = _df_to64(xh, xl)
+    r = b - spmv_host(rp, ci, va, x)
+    return x, status, it, float(np.linalg.norm(r) / np.sqrt(bb))
+
+
+def spmv_host(rp, ci, va, x):
+    """y = A x in numpy (FP64)."""
+    rp = np.asarray(rp, np.int64)
+    row = np.repeat(np.arange(rp.shape[0] - 1), np.diff(rp))
+    y = np.zeros(rp.shape[0] - 1)
+    np.add.at(y, row, np.asarray(va, _f64) * np.asarray(x, _f64)[np.asarray(ci, np.int64)])
+    return y
 
 
 def dense_normal_equations(rs):

@@ -133,3 +133,27 @@ def test_oracle_bicgstab_gmres_pinned_to_direct_solve(oracle_mod):
     assert st == 1 and it == 0 and not x.any()
     x, st, it = oracle_mod.gmres(cd.rp, cd.ci, cd.va, cd.rhs[0], eps=1e-14, restart=5, max_iter=7)
     assert st == 2 and it == 7                    # stops inside the second cycle
+
+
+def test_double_float_pcg_restatement(oracle_mod):
+    """The double-float PCG (float pairs on float32 arithmetic) behaves like
+    FP64 CG on LSCM normal equations and a fairing system: converged on the
+    recursive residual, iterations within 15 % of FP64's, true residual
+    near the threshold down to its rounding floor (~5e-12 relative here:
+    the recursive residual drifts from the true one at 2^-48 rounding),
+    solution within 1e-8 of the direct solve at 1e-12."""
+    for rs_or_sq in (systems.lscm_system(24, 20, seed=7), systems.fairing_system(30, 28, seed=3)):
+        if hasattr(rs_or_sq, "rp"):
+            rp, ci, va, b = rs_or_sq.rp, rs_or_sq.ci, rs_or_sq.va, rs_or_sq.rhs[0]
+        else:
+            rp, ci, va, rhs = oracle_mod.assemble_rowstream(rs_or_sq)
+            b = rhs[0]
+        xd = oracle_mod.direct_solve(rp, ci, va, b)
+        for eps in (1e-10, 1e-12):
+            x, st, it, true_rel = oracle_mod.pcg_df(rp, ci, va, b, eps=eps)
+            _, st64, it64, _ = oracle_mod.pcg(rp, ci, va, b, eps=eps)
+            assert st == 1 and st64 == 1
+            assert abs(it - it64) <= max(3, 0.15 * it64)
+            assert true_rel <= max(3 * eps, 1e-11)
+            if eps == 1e-12:
+                assert np.linalg.norm(x - xd) / np.linalg.norm(xd) <= 1e-8
