@@ -1,7 +1,8 @@
 """Eager mode (NLGB_EAGER_SOLVE=1, read once per process): the solver's
 kernels launched one by one instead of through conditional CUDA graphs, so
 that a profiler sees each of them.  Same kernels, same order: results must
-be bit-identical to the graph path, in both precisions."""
+be bit-identical to the graph path, in every precision (FP64, mixed,
+double-float)."""
 import json
 import os
 import subprocess
@@ -26,7 +27,7 @@ fs = systems.fairing_system(70, 60, seed=5, n_rhs=1)
 F = solver.Matrix(fs.rp, fs.ci, fs.va)
 out = {}
 for name, A, b in (("lscm", M, rhs[0]), ("fair", F, fs.rhs[0])):
-    for prec in ("double", "mixed"):
+    for prec in ("double", "mixed", "df"):
         x, info = A.solve(b, precision=prec)
         out[f"{name}_{prec}"] = {"x": x.tolist(), "it": info.iterations, "status": info.status}
 big = systems.fairing_system(420, 400, seed=21, n_rhs=1)
@@ -48,7 +49,7 @@ def test_eager_mode_bit_identical(gpu_ok, tmp_path):
     fs = systems.fairing_system(70, 60, seed=5, n_rhs=1)
     F = solver.Matrix(fs.rp, fs.ci, fs.va)
     for name, A, b in (("lscm", M, rhs[0]), ("fair", F, fs.rhs[0])):
-        for prec in ("double", "mixed"):
+        for prec in ("double", "mixed", "df"):
             x, info = A.solve(b, precision=prec)
             e = eager[f"{name}_{prec}"]
             assert e["status"] == info.status == "converged"
