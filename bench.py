@@ -2,40 +2,45 @@
 """Benchmark: solves/s and p99 latency at relative residual 1e-10 on the
 serving stream (batched mixed-precision server vs plain FP64 GPU PCG).
 
-Workload (one "step"): a seeded sample of R requests drawn from the serving
-stream's distribution -- LSCM parameterisation or cotangent-Laplacian
-fairing (3 right-hand sides) with probability 1/2 each, vertex counts
-log-uniform in [1e3, 1e6], square-ish grid patches with the seeded bump
-model, Poisson arrivals at `--rate` per second -- submitted through the C ABI
-(nlgb_server_submit_rows / _crs with host buffers) to the continuous-batching
-server (HBM budget 150 GB, precision AUTO: mixed FP32/FP64 with FP64
-fallback for square systems, FP64 for least-squares normal equations) and
-drained.
-Every step re-submits the same sample from scratch (assembly, upload, solve,
-download: nothing is cached).
+Workload (one "step"): a window of the serving stream of the configuration
+"serving stream" -- Poisson arrivals at `--rate` per second during `--window`
+seconds, each request an LSCM parameterisation or a cotangent-Laplacian
+fairing (3 right-hand sides) with probability 1/2, vertex count log-uniform
+in [1e3, 1e6], a seeded square-ish grid patch with the bump model -- replayed
+in real time through the C ABI (nlgb_server_submit_mesh with host buffers:
+the server uploads the mesh, builds the system on the GPU, solves, and
+copies the solution back to the host) to the continuous-batching server
+(HBM budget 150 GB, least-attained-service epochs, precision AUTO: mixed
+FP32/FP64 for the square fairing systems, FP64 for the least-squares LSCM
+normal equations).  The step ends `--drain` seconds after the window; the
+server is then aborted.  Every step replays the same seeded stream from
+scratch (upload, build, solve, download: nothing is cached).
 
 Reported:
-  value       R / (device time of the server's persistent-kernel epochs) --
-              throughput with the inputs resident in HBM;
-  e2e         R / (first arrival -> last result on the host), through the
-              C ABI with host buffers (uploads and downloads included);
-  latency     p50 / p99 from arrival to result on the host;
-  plain_fp64  the same sample through the serial FP64 server (graph-captured
-              single-system PCG, one request at a time);
+  e2e         completed requests / (window + drain): a request counts when
+              its solution is on the host before the step ends;
+  value       completed requests / device time of the server's solver
+              epochs in the step (the GPU-side throughput);
+  latency     p50 / p99 from arrival to solution on the host over every
+              request of the window, an unfinished one counted as censored
+              at the end of the step (p50 / p99 of the completed ones
+              beside it);
+  plain_fp64  the same stream through the serial FP64 server (graph-captured
+              single-system PCG, one request at a time, first come first
+              served);
   roofline    achieved algorithmic GB/s (bytes from the iteration counts,
-              CUDA-event time) of the executor that dominates the step --
-              the PCG iteration graph continuing the large systems, or
-              the persistent batched kernel -- vs the measured HBM peak;
-              roofline_other: the other one;
+              CUDA-event time) of the executor that dominates the step vs the
+              measured HBM peak; roofline_other: the other one;
   spmv_fp64   the FP64 CRS SpMV on the 2048^2 cotangent Laplacian (4.2M
               rows, 29.3M nonzeros) vs the measured HBM peak;
+  parity      statuses and true residuals of the completed requests, and
+              each checked result's relative error against the FP64 direct
+              oracle (SuperLU on the system built on the host);
   cpu_baseline  the CPU oracle (C, OpenMP, FP64 Jacobi-PCG on all host
-              cores) on the same sample: every request assembled and timed;
-              systems over 250k unknowns timed on 200 iterations and scaled
-              to the oracle's own iteration count for them (committed
-              fixture oracle/serving_sample_iterations.json);
-              cpu_baseline_1thread: the same with one thread;
-  hbm         peak device footprint admitted by the server vs its budget.
+              cores; host row builder + assembly) on the same stream window,
+              first come first served, bounded by the same window + drain:
+              completions / (window + drain); cpu_baseline_1thread likewise;
+  hbm         peak and mean device footprint admitted by the server.
 `--impl reference` runs only the CPU reference arm (the oracle port: the
 reference's own OpenNL source is not in the checkout) and prints its line.
 """
@@ -58,12 +63,11 @@ os.environ.setdefault("NLGB_QUIET", "1")
 import numpy as np  # noqa: E402
 
 METRIC = "solves/s & p99 latency at rel-residual 1e-10: batched mixed vs plain FP64 GPU"
-# DRAM bytes (read + write) per algorithmic byte of the persistent kernel,
-# from one ncu capture (profiles/k_batch_lscm808.md: 63.75 GB over 200 FP64
-# iterations of the 1.3M-unknown LSCM system, 72.2 GB algorithmic)
-KBATCH_DRAM_PER_ALGO_BYTE = 0.88
-# the same for the PCG iteration graph: its SpMV read 252.9 MB for 245.2 MB
-# algorithmic on that system (profiles/k_spmv_pq_lscm808_fairing2048.md)
+# DRAM bytes (read + write) per algorithmic byte of the PCG iteration
+# kernels, from one ncu capture on the 1.3M-unknown LSCM system (808^2
+# grid): its SpMV read 252.9 MB for 245.2 MB algorithmic; the serving
+# workload is too large to capture whole, and its traffic grows in
+# proportion to the iterations run.
 GRAPH_DRAM_PER_ALGO_BYTE = 1.03
 HBM_FALLBACK_GBS = 6800.0
 
@@ -74,18 +78,25 @@ def parse_args():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--requests", type=int, default=12)
     p.add_argument("--seed", type=int, default=20261203)
-    p.add_argument("--rate", type=float, default=1000.0)
+    p.add_argument("--rate", type=float, default=100.0, help="Poisson arrival rate (requests/s)")
+    p.add_argument("--window", type=float, default=4.0, help="arrival window of one step (s)")
+    p.add_argument("--drain", type=float, default=2.0, help="time after the window before the step ends (s)")
+    p.add_argument("--lead", type=float, default=1.5,
+                   help="submission lead time before the window opens (s; not timed)")
     p.add_argument("--eps", type=float, default=1e-10)
     p.add_argument("--budget-gb", type=float, default=150.0)
+    p.add_argument("--plain-steps", type=int, default=2, help="steps of the serial plain-FP64 arm")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-spmv", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-parity", action="store_true")
+    p.add_argument("--parity-max-unknowns", type=int, default=300_000,
+                   help="largest completed request checked against the direct oracle")
     p.add_argument("--profile-case", choices=["spmv", "batch", "batch_small", "batch_lscm", "plain", "mixed",
                                               "plain_lscm", "mixed_lscm", "df_lscm", "kernels"], default=None,
                    help="run one small case for an ncu capture and exit")
-    p.add_argument("--workload", choices=["serving", "configs"], default="serving",
+    p.add_argument("--workload", choices=["stream", "configs"], default="stream",
                    help="configs: measure the other benchmark configurations and exit")
     return p.parse_args()
 
@@ -292,23 +303,6 @@ def measured_peak():
     return HBM_FALLBACK_GBS, "fallback 6.8 TB/s (of fallback)"
 
 
-def build_sample(R, seed, rate):
-    from graphitethree_gb300 import systems
-    return systems.serving_sample(R, seed, rate, 1_000, 1_000_000)
-
-
-def io_bytes(objs):
-    h2d = d2h = 0
-    for kind, o in objs:
-        if kind == "rows":
-            h2d += o.row_ptr.nbytes + o.var.nbytes + o.val.nbytes + o.rhs.nbytes + o.values.nbytes
-            d2h += int((o.locked == 0).sum()) * 8 * o.n_systems
-        else:
-            h2d += o.rp.nbytes + o.ci.nbytes + o.va.nbytes + o.rhs.nbytes
-            d2h += o.rhs.nbytes
-    return int(h2d), int(d2h)
-
-
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons during the timed region."""
 
@@ -359,24 +353,6 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def serve(objs, reqs, precision, mode, eps, budget, rate_scale=1.0):
-    """Submit the sample with its Poisson arrival offsets and drain."""
-    from graphitethree_gb300 import solver
-    srv = solver.Server(budget_bytes=budget, precision=precision, mode=mode, eps=eps)
-    srv.reset_clock()
-    tickets = []
-    for r, (kind, o) in zip(reqs, objs):
-        arr = r.arrival * rate_scale
-        tickets.append(srv.submit_rows(o, arr) if kind == "rows" else srv.submit_square(o, arr))
-    results = []
-    for t in tickets:
-        x, infos, lat = srv.wait(t)
-        results.append((infos, lat))
-    st = srv.stats()
-    srv.close()
-    return st, results
-
-
 def spmv_roofline(peak):
     import ctypes
     from graphitethree_gb300 import _lib, solver, systems
@@ -400,105 +376,203 @@ def spmv_roofline(peak):
     return out
 
 
-CPU_FULL_LIMIT = 250_000   # unknowns: systems up to this size are solved to completion
-CPU_PROBE_ITERS = 200       # timed iterations of a larger system
 
 
-def sample_iterations_fixture(args):
-    """Per-system iteration counts of the oracle's PCG on this exact sample
-    (oracle/make_sample_iterations.py), or None for another sample."""
-    path = ROOT / "oracle" / "serving_sample_iterations.json"
-    try:
-        fx = json.loads(path.read_text())
-    except (OSError, ValueError):
-        return None
-    if (fx.get("requests"), fx.get("seed"), fx.get("rate"), fx.get("eps")) != \
-            (args.requests, args.seed, args.rate, args.eps):
-        return None
-    return {r["request"]: r for r in fx["systems"]}
+# ---------------------------------------------------------------------------
+# Serving stream
+# ---------------------------------------------------------------------------
+def make_stream(args, rank=0):
+    from graphitethree_gb300 import systems
+    return systems.stream_window(args.rate, args.window, args.seed + 7919 * rank)
 
 
-def cpu_arm(objs, args, threads: int | None = None):
-    """The oracle (C, OpenMP on all host cores): row assembly + FP64
-    Jacobi-PCG for every request of the sample, in arrival order.  Systems up
-    to CPU_FULL_LIMIT unknowns are solved to completion; a larger one runs
-    CPU_PROBE_ITERS timed iterations and its solve time is that per-iteration
-    time x the iteration count the same oracle needs to converge on it
-    (committed fixture).  Without the fixture the larger requests are left
-    out and the sample says so."""
-    from oracle import oracle
-    threads = threads or oracle.max_threads()
-    fx = sample_iterations_fixture(args)
-    total, done, full, scaled, skipped = 0.0, 0, [], [], []
-    for i, (kind, o) in enumerate(objs):
-        t0 = time.perf_counter()
-        rp, ci, va, rhs = oracle.assemble_rowstream(o if kind == "rows" else o.to_rows())
-        t_req = time.perf_counter() - t0
-        n = int(rp.shape[0] - 1)
-        if n <= CPU_FULL_LIMIT:
-            t0 = time.perf_counter()
-            for s in range(rhs.shape[0]):
-                oracle.pcg(rp, ci, va, rhs[s], eps=args.eps, nthreads=threads)
-            t_req += time.perf_counter() - t0
-            full.append(n)
-        elif fx is not None and i in fx and fx[i]["unknowns"] == n:
-            for s in range(rhs.shape[0]):
-                t0 = time.perf_counter()
-                _, _, it, _ = oracle.pcg(rp, ci, va, rhs[s], eps=1e-300, max_iter=CPU_PROBE_ITERS,
-                                         nthreads=threads)
-                per_iter = (time.perf_counter() - t0) / max(1, it)
-                t_req += per_iter * fx[i]["iterations"][s]
-            scaled.append((n, fx[i]["iterations"]))
+def run_stream(stream, args, mode: str, precision: str, keep_x: bool = False):
+    """One step: replay the window in real time through the C ABI, end it
+    `drain` seconds after the window, abort what is left.  Returns a dict."""
+    from graphitethree_gb300 import solver
+    srv = solver.Server(budget_bytes=args.budget_gb * 1e9, precision=precision, mode=mode, eps=args.eps)
+    srv.reset_clock()
+    T0 = args.lead
+    tickets = [srv.submit_mesh(r.kind, r.V, r.F, b=r.b, lam=r.lam, arrival=T0 + r.arrival) for r in stream]
+    t_submitted = srv.now()
+    t_end = T0 + args.window + args.drain
+    while srv.now() < t_end:
+        time.sleep(min(0.01, max(0.0, t_end - srv.now())))
+    srv.abort()
+    lat_all, lat_done, done, xs, infos = [], [], [], {}, {}
+    for r, t in zip(stream, tickets):
+        arr = T0 + r.arrival
+        try:
+            x, inf, lat = srv.wait(t)
+            ok = arr + lat <= t_end
+        except solver.SolverError:
+            ok, lat, x, inf = False, None, None, None
+        if ok:
+            done.append(r.rid)
+            lat_all.append(lat)
+            lat_done.append(lat)
+            infos[r.rid] = inf
+            if keep_x:
+                xs[r.rid] = x.copy()
         else:
-            skipped.append(n)
-            continue
-        total += t_req
-        done += 1
-    desc = (f"all {len(objs)} requests of the sample: CPU assembly + FP64 Jacobi-PCG to "
-            f"{args.eps:g}; systems solved to completion: {full}")
-    if scaled:
-        desc += (f"; larger systems (unknowns, iterations to converge): {scaled} -- "
-                 f"{CPU_PROBE_ITERS} iterations timed, scaled to the oracle's own iteration "
-                 f"count (oracle/serving_sample_iterations.json)")
-    if skipped:
-        desc += f"; left out (no iteration-count fixture for this sample): {skipped}"
-    desc += f"; {total:.1f} s of host time"
-    return {"value": done / total if total > 0 else 0.0, "unit": "solves/s", "cores": threads,
-            "kind": "port", "sample": desc}
+            lat_all.append(t_end - arr)   # censored
+    st = srv.stats()
+    srv.close()
+    span = args.window + args.drain
+    return {"completed": len(done), "done_ids": done, "e2e": len(done) / span,
+            "kernel_s": st["kernel_s"], "value": len(done) / st["kernel_s"] if st["kernel_s"] > 0 else 0.0,
+            "lat_all": lat_all, "lat_done": lat_done, "stats": st, "infos": infos, "xs": xs,
+            "submit_s": t_submitted, "t_end": t_end}
+
+
+def pct(v, q):
+    return float(np.percentile(v, q)) if len(v) else None
+
+
+def _oracle_error(job):
+    """One GPU result against the oracles, on the system built on the host
+    from the same mesh: relative error against the FP64 direct solution
+    (SuperLU), and relative difference from the oracle's own FP64 Jacobi-PCG
+    (the restated OpenNL CPU solve, one thread) run to the same threshold,
+    when pcg_max >= n.  Runs in a worker process."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    from graphitethree_gb300.systems import StreamRequest
+    from oracle import oracle
+    kind, V, F, b, lam, xs, eps, pcg_max = job
+    r = StreamRequest(rid=0, kind=kind, nx=0, ny=0, seed=0, arrival=0.0, V=V, F=F, b=b, lam=lam)
+    rp, ci, va, rhs = r.host_system()
+    n = len(rp) - 1
+    lu = spla.splu(sp.csr_matrix((va, ci, rp), shape=(n, n)).tocsc())
+    direct, pcg = [], []
+    for k in range(xs.shape[0]):
+        ref = lu.solve(np.asarray(rhs[k], np.float64))
+        direct.append(float(np.linalg.norm(xs[k] - ref) / max(np.linalg.norm(ref), 1e-300)))
+        if n <= pcg_max:
+            xo = oracle.pcg(rp, ci, va, rhs[k], eps=eps, nthreads=1)[0]
+            pcg.append(float(np.linalg.norm(xs[k] - xo) / max(np.linalg.norm(xo), 1e-300)))
+    return kind, n, direct, pcg
+
+
+def oracle_errors(stream, res, args):
+    """Every completed request up to --parity-max-unknowns against the
+    direct oracle, and up to a third of that against the oracle's PCG
+    (process pool started with spawn)."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    by_id = {r.rid: r for r in stream}
+    pcg_max = args.parity_max_unknowns // 3
+    jobs = []
+    for rid in res["done_ids"]:
+        r = by_id[rid]
+        if r.unknowns <= args.parity_max_unknowns and rid in res["xs"]:
+            jobs.append((r.unknowns, (r.kind, r.V, r.F, r.b, r.lam, res["xs"][rid], args.eps, pcg_max)))
+    jobs.sort(key=lambda j: -j[0])
+    workers = max(1, min(16, (os.cpu_count() or 2) - 1))
+    t0 = time.perf_counter()
+    out = {"lscm": {"direct": [], "pcg": []}, "fairing": {"direct": [], "pcg": []}}
+    if jobs:
+        with ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+            for kind, n, d, p in ex.map(_oracle_error, [j[1] for j in jobs]):
+                out[kind]["direct"].extend(d)
+                out[kind]["pcg"].extend(p)
+    summary = {"method": "each completed request's system rebuilt on the host from its mesh; "
+                         "direct = relative error against scipy SuperLU (FP64 direct), pcg = relative "
+                         "difference from the oracle's FP64 Jacobi-PCG (the restated OpenNL CPU solve) "
+                         f"run to the same threshold (systems up to {pcg_max} unknowns)",
+               "requests_checked": len(jobs), "requests_completed": len(res["done_ids"]),
+               "max_unknowns_checked": max([j[0] for j in jobs], default=0),
+               "seconds": time.perf_counter() - t0}
+    for kind in ("lscm", "fairing"):
+        for what in ("direct", "pcg"):
+            v = out[kind][what]
+            summary[f"{kind}_{what}"] = {"systems": len(v), "max": max(v, default=None),
+                                        "above_1e-8": int(sum(e > 1e-8 for e in v))}
+    return summary
+
+
+def cpu_stream(stream, args, threads):
+    """The CPU oracle on the same stream window, first come first served:
+    host row builder + C assembly (LSCM) or host CRS (fairing), then FP64
+    Jacobi-PCG with OpenMP on `threads` cores, bounded by window + drain."""
+    from oracle import oracle
+    span = args.window + args.drain
+    t0 = time.perf_counter()
+    done = 0
+    lat = []
+    for r in stream:
+        now = time.perf_counter() - t0
+        if now >= span:
+            break
+        if now < r.arrival:
+            time.sleep(r.arrival - now)
+        rp, ci, va, rhs = r.host_system()
+        ok = True
+        for k in range(rhs.shape[0]):
+            left = span - (time.perf_counter() - t0)
+            if left <= 0:
+                ok = False
+                break
+            _, status, _, _ = oracle.pcg(rp, ci, va, rhs[k], eps=args.eps, nthreads=threads, max_seconds=left)
+            if status != 1:
+                ok = False
+                break
+        t_done = time.perf_counter() - t0
+        if ok and t_done <= span:
+            done += 1
+            lat.append(t_done - r.arrival)
+    return {"value": done / span, "unit": "solves/s", "cores": threads, "kind": "port",
+            "completed": done, "p50_latency_s": pct(lat, 50),
+            "sample": f"the same stream window ({len(stream)} requests arriving in {args.window:g} s, "
+                      f"+{args.drain:g} s drain): host LSCM rows + C normal-equation assembly or host "
+                      f"cotangent CRS, FP64 Jacobi-PCG to {args.eps:g} (C, OpenMP), first come first "
+                      f"served, each step bounded by window + drain ({span:g} s); completions / {span:g} s"}
+
+
+def config(args, stream):
+    n_l = sum(r.kind == "lscm" for r in stream)
+    return {"workload": f"serving stream (Poisson arrivals {args.rate:g}/s during a {args.window:g} s window "
+                        f"+ {args.drain:g} s drain; LSCM / cotangent fairing with 3 RHS 50/50; vertices "
+                        f"log-uniform [1e3,1e6]; seed {args.seed}): {len(stream)} requests "
+                        f"({n_l} LSCM, {len(stream) - n_l} fairing), "
+                        f"{sum(r.unknowns for r in stream)} unknowns",
+            "requests": len(stream), "rate_per_s": args.rate, "window_s": args.window, "drain_s": args.drain,
+            "rel_residual": args.eps, "hbm_budget_gb": args.budget_gb,
+            "precision": "auto: mixed FP32/FP64 (with FP64 fallback) for the square fairing "
+                        "systems, FP64 for the least-squares LSCM normal equations",
+            "schedule": "shortest estimated remaining work first, epochs time-boxed to 10 ms",
+            "l2": "inputs larger than L2 for the large requests; every step re-uploads, rebuilds and "
+                  "re-solves every request (no cached data)"}
 
 
 def run_reference(args):
-    reqs, objs = build_sample(args.requests, args.seed, args.rate)
-    # each step: the whole sample on the host cores (large systems timed on a
-    # bounded number of iterations, see cpu_arm)
-    vals = []
-    res = None
+    from oracle import oracle
+    stream = make_stream(args)
+    vals, res = [], None
     for i in range(args.warmup + args.steps):
-        r = cpu_arm(objs, args)
+        r = cpu_stream(stream, args, threads=oracle.max_threads())
         if i >= args.warmup:
             vals.append(r["value"])
             res = r
     v = float(statistics.median(vals)) if vals else 0.0
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * (args.window + args.drain),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded serving-stream sample)",
-            "config": config(args),
+            "data": "synthetic (seeded serving stream; no public dataset)",
+            "config": config(args, stream),
             "cpu_baseline": {**res, "value": v},
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
-def config(args):
-    return {"workload": f"serving-stream sample: {args.requests} requests, LSCM / cotangent fairing "
-                        f"(3 RHS) 50/50, vertices log-uniform [1e3,1e6], Poisson arrivals "
-                        f"{args.rate:g}/s, seed {args.seed}",
-            "requests": args.requests, "rate_per_s": args.rate, "rel_residual": args.eps,
-            "hbm_budget_gb": args.budget_gb,
-            "precision": "auto: mixed FP32/FP64 (with FP64 fallback) for the square fairing "
-                         "systems, FP64 for the least-squares LSCM normal equations",
-            "l2": "inputs larger than L2 for the large requests; every step re-uploads and "
-                  "re-assembles (no cached data)"}
+def io_bytes(stream, done_ids):
+    """Host<->device bytes of one step: every mesh (and fairing right-hand
+    side) is uploaded, every completed solution downloaded."""
+    h2d = sum(r.V.nbytes + r.F.nbytes + (r.b.nbytes if r.b is not None else 0) for r in stream)
+    ids = set(done_ids)
+    d2h = sum(8 * r.unknowns * (1 if r.kind == "lscm" else 3) for r in stream if r.rid in ids)
+    return int(h2d), int(d2h)
 
 
 def main():
@@ -520,21 +594,19 @@ def main():
         raise SystemExit("bench.py: no CUDA device")
     dist = None
     if world > 1:
-        # replicas only: each rank serves its own seeded stream sample on its
-        # GPU; no data-path collective, only a barrier and max-over-ranks timing
+        # replicas only: each rank serves its own seeded stream on its GPU; no
+        # data-path collective, only a barrier and max-over-ranks timing
         import torch
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
     L = _lib.load()
     peak, peak_src = measured_peak()
-    budget = args.budget_gb * 1e9
-    reqs, objs = build_sample(args.requests, args.seed + 7919 * rank, args.rate)
-    h2d, d2h = io_bytes(objs)
-    R = len(objs)
+    stream = make_stream(args, rank)
+    span = args.window + args.drain
 
     for _ in range(args.warmup):
-        serve(objs, reqs, "auto", "batched", args.eps, budget)
+        run_stream(stream, args, "batched", "auto")
     if dist is not None:
         dist.barrier()
     clocks = ClockSampler()
@@ -542,99 +614,108 @@ def main():
     launches0 = L.nlgb_kernel_launches()
     steps = []
     t_wall0 = time.perf_counter()
-    for _ in range(args.steps):
-        st, results = serve(objs, reqs, "auto", "batched", args.eps, budget)
-        steps.append((st, results))
+    for i in range(args.steps):
+        steps.append(run_stream(stream, args, "batched", "auto", keep_x=(i == args.steps - 1)))
     t_wall = time.perf_counter() - t_wall0
     launches = L.nlgb_kernel_launches() - launches0
     clk = clocks.stop()
 
-    kern = [s["kernel_s"] for s, _ in steps]
-    walls = [s["wall_s"] for s, _ in steps]
-    k_med, w_med = statistics.median(kern), statistics.median(walls)
+    e2e = statistics.median([s["e2e"] for s in steps])
+    value = statistics.median([s["value"] for s in steps])
     if dist is not None:
         from graphitethree_gb300.replicas import max_over_ranks
-        k_med, w_med, t_wall = max_over_ranks([k_med, w_med, t_wall], dist, device="cuda")
+        # slowest replica: the smallest completion rate, as the largest time
+        inv = max_over_ranks([1.0 / max(e2e, 1e-12), 1.0 / max(value, 1e-12), t_wall], dist, device="cuda")
+        e2e, value, t_wall = world / inv[0], world / inv[1], inv[2]
         dist.barrier()
-    value = R * world / k_med
-    e2e = R * world / w_med
-    lat = [l for _, res in steps for _, l in res]
-    p50 = float(np.percentile(lat, 50))
-    p99 = float(np.percentile(lat, 99))
-    st_last, res_last = steps[-1]
-    # the persistent kernel alone: the iterations of large FP64 systems that
-    # the server continued as graph chunks are accounted separately
-    kb_bytes = st_last["algo_bytes"] - st_last["graph_algo_bytes"]
-    kb_s = st_last["kernel_s"] - st_last["graph_s"]
-    kb_launches = max(1, st_last["epochs"] - st_last["graph_epochs"])
-    achieved = kb_bytes / kb_s / 1e9 if kb_s > 0 else 0.0
-    # The step's device time splits between persistent-kernel epochs (k_batch)
-    # and graph chunks that continue large FP64 systems once only those are
-    # left (the PCG iteration kernels k_spmv_pq, k_update_xr, k_update_p);
-    # the roofline reports whichever dominates, the other beside it.
-    g_s, g_bytes, g_launches = st_last["graph_s"], st_last["graph_algo_bytes"], max(1, st_last["graph_epochs"])
-    kb = {"bound": "hbm", "kernel": "k_batch (persistent batched PCG, one launch per epoch)",
-          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-          "traffic": KBATCH_DRAM_PER_ALGO_BYTE * kb_bytes / kb_launches,
-          "algo_bytes_per_launch": kb_bytes / kb_launches, "launches_per_step": kb_launches,
-          "kernel_s_per_step": kb_s, "peak_source": peak_src,
-          "traffic_note": "dram read+write per launch, scaled from the ncu capture of k_batch on the "
-                          "1.3M-unknown LSCM system (0.88 DRAM byte per algorithmic byte, "
-                          "profiles/k_batch_lscm808.md)"}
-    g_ach = g_bytes / g_s / 1e9 if g_s > 0 else 0.0
-    gr = {"bound": "hbm", "kernel": "FP64 PCG iteration graph (k_spmv_pq + k_update_xr + k_update_p), "
-                                    "one launch per chunk of a large system",
-          "achieved": g_ach, "peak": peak, "unit": "GB/s", "frac": g_ach / peak,
-          "traffic": GRAPH_DRAM_PER_ALGO_BYTE * g_bytes / g_launches,
-          "algo_bytes_per_launch": g_bytes / g_launches, "launches_per_step": g_launches,
-          "kernel_s_per_step": g_s, "peak_source": peak_src,
-          "traffic_note": "dram read+write per launch, scaled from the ncu capture of k_spmv_pq on the "
-                          "1.3M-unknown LSCM system (1.03 DRAM byte per algorithmic byte; the vector "
-                          "kernels stream exactly their bytes), profiles/k_spmv_pq_lscm808_fairing2048.md"}
-    fp64_note = ("the FP64 phases are co-limited by GB300's FP64 pipe (65-81 % busy in the captures), "
-                 "not only by HBM")
-    roofline, other = (gr, kb) if g_s > kb_s else (kb, gr)
-    roofline = {**roofline, "fp64_note": fp64_note}
-    statuses = [i.status for infos, _ in res_last for i in infos]
-    true_res = [i.true_rel_residual for infos, _ in res_last for i in infos]
+    lat_all = [l for s in steps for l in s["lat_all"]]
+    lat_done = [l for s in steps for l in s["lat_done"]]
+    last = steps[-1]
+    st_last = last["stats"]
+    h2d, d2h = io_bytes(stream, last["done_ids"])
+
+    # Device work of the step: the server's executor runs every system as
+    # CUDA-graph chunks of the PCG iteration kernels (k_spmv_pq + k_update_xr
+    # + k_update_p, or the mixed-precision k_mx_* kernels) on 16 concurrent
+    # streams; achieved = algorithmic bytes of all iterations run (finished
+    # requests or not) / wall time during which at least one chunk was in
+    # flight.
+    busy = st_last["kernel_s"]
+    algo = st_last["epoch_algo_bytes"]
+    chunks = max(1, st_last["epochs"])
+    ach = algo / busy / 1e9 if busy > 0 else 0.0
+    roofline = {"bound": "hbm",
+                "kernel": "PCG iteration kernels in CUDA-graph chunks (k_spmv_pq, k_update_xr, k_update_p; "
+                          "k_mx_spmv_pq, k_mx_update_cr, k_mx_update_p for mixed systems), 16 concurrent "
+                          "streams",
+                "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "traffic": GRAPH_DRAM_PER_ALGO_BYTE * algo / chunks,
+                "algo_bytes_per_launch": algo / chunks, "launches_per_step": chunks,
+                "busy_s_per_step": busy, "peak_source": peak_src,
+                "traffic_note": "dram read+write per chunk: 1.03 DRAM byte per algorithmic byte, from the ncu "
+                                "capture of k_spmv_pq on the 1.3M-unknown LSCM system (the vector kernels "
+                                "stream exactly their bytes), times this workload's algorithmic bytes per chunk",
+                "fp64_note": "the FP64 phases are co-limited by GB300's FP64 pipe, not only by HBM"}
+    other = None
+
+    infos = [i for infs in last["infos"].values() for i in infs]
+    statuses = {}
+    for i in infos:
+        statuses[i.status] = statuses.get(i.status, 0) + 1
+    parity = {"completed_requests": last["completed"], "statuses": statuses,
+              "all_converged": all(i.status == "converged" for i in infos),
+              "max_true_rel_residual": max((i.true_rel_residual for i in infos), default=None),
+              "iterations_per_step": st_last["iterations"]}
+    if not args.no_parity and rank == 0:
+        parity["oracle_error"] = oracle_errors(stream, last, args)
 
     plain = None
     if not args.no_plain:
-        stp, resp = serve(objs, reqs, "double", "serial", args.eps, budget)
-        latp = [l for _, l in resp]
-        plain = {"solves_per_s_e2e": R / stp["wall_s"], "solves_per_s_device": R / stp["kernel_s"],
-                 "p50_latency_s": float(np.percentile(latp, 50)),
-                 "p99_latency_s": float(np.percentile(latp, 99)),
-                 "achieved_GBs": stp["algo_bytes"] / stp["kernel_s"] / 1e9,
-                 "speedup_e2e_batched_mixed_over_plain": e2e / (R / stp["wall_s"]),
-                 "speedup_device": value / (R / stp["kernel_s"])}
+        pr = [run_stream(stream, args, "serial", "double") for _ in range(max(1, args.plain_steps))]
+        p_e2e = statistics.median([r["e2e"] for r in pr])
+        p_val = statistics.median([r["value"] for r in pr])
+        p_all = [l for r in pr for l in r["lat_all"]]
+        plain = {"solves_per_s_e2e": p_e2e, "solves_per_s_device": p_val,
+                 "completed": [r["completed"] for r in pr],
+                 "p50_latency_s": pct(p_all, 50), "p99_latency_s": pct(p_all, 99),
+                 "achieved_GBs": (pr[-1]["stats"]["algo_bytes"] / pr[-1]["stats"]["kernel_s"] / 1e9
+                                  if pr[-1]["stats"]["kernel_s"] > 0 else 0.0),
+                 "speedup_e2e_batched_mixed_over_plain": e2e / p_e2e if p_e2e > 0 else None,
+                 "speedup_device": value / p_val if p_val > 0 else None,
+                 "note": "one request at a time, first come first served, graph-captured FP64 PCG; "
+                         "censored latencies as for the batched arm"}
     spmv = None if args.no_spmv else spmv_roofline(peak)
-    cpu = None
-    cpu1 = None
+    cpu = cpu1 = None
     if not args.no_cpu and rank == 0:
-        cpu = cpu_arm(objs, args)
-        cpu1 = cpu_arm(objs, args, threads=1)
+        from oracle import oracle
+        cpu = cpu_stream(stream, args, oracle.max_threads())
+        cpu1 = cpu_stream(stream, args, 1)
 
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_wall / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64",
-        "data": "synthetic (seeded serving-stream sample; no public dataset)",
-        "config": config(args),
+        "data": "synthetic (seeded serving stream; no public dataset)",
+        "config": config(args, stream),
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "latency": {"p50_s": p50, "p99_s": p99, "unit": "s"},
+        "completed_per_step": [s["completed"] for s in steps],
+        "latency": {"p50_s": pct(lat_all, 50), "p99_s": pct(lat_all, 99),
+                    "completed_p50_s": pct(lat_done, 50), "completed_p99_s": pct(lat_done, 99),
+                    "censored_fraction": 1.0 - len(lat_done) / max(1, len(lat_all)), "unit": "s"},
         "plain_fp64": plain,
         "roofline": roofline,
         "roofline_other": other,
         "spmv_fp64": spmv,
         "cpu_baseline": cpu,
-        "cpu_baseline_1thread": None if cpu1 is None else {k: cpu1[k] for k in ("value", "unit", "cores")},
-        "hbm": {"peak_admitted_gb": st_last["peak_bytes"] / 1e9, "budget_gb": st_last["budget_bytes"] / 1e9},
+        "cpu_baseline_1thread": None if cpu1 is None else {k: cpu1[k] for k in ("value", "unit", "cores",
+                                                                                 "completed")},
+        "hbm": {"peak_admitted_gb": st_last["peak_bytes"] / 1e9,
+                "mean_admitted_gb": st_last["byte_seconds"] / max(1e-9, last["t_end"]) / 1e9,
+                "budget_gb": st_last["budget_bytes"] / 1e9},
         "clocks": clk,
         "gpu_launches": int(launches),
-        "parity": {"all_converged": all(s == "converged" for s in statuses),
-                   "max_true_rel_residual": max(true_res) if true_res else None,
-                   "iterations_per_step": st_last["iterations"]},
+        "parity": parity,
+        "submit_s": last["submit_s"],
     }
     if rank == 0:
         print(json.dumps(line))

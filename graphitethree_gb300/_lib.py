@@ -63,7 +63,8 @@ class NlgbResult(C.Structure):
 class NlgbServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_size_t), ("mode", C.c_int), ("precision", C.c_int),
                 ("eps", C.c_double), ("max_iter", C.c_longlong), ("inner_eps", C.c_double),
-                ("epoch_iters", C.c_longlong), ("max_systems", C.c_int)]
+                ("epoch_iters", C.c_longlong), ("max_systems", C.c_int), ("schedule", C.c_int),
+                ("epoch_ms", C.c_double), ("streams", C.c_int)]
 
 
 class NlgbServerStats(C.Structure):
@@ -74,7 +75,8 @@ class NlgbServerStats(C.Structure):
                 ("kernel_s", C.c_double), ("epochs", C.c_longlong), ("iterations", C.c_longlong),
                 ("algo_bytes", C.c_double), ("peak_bytes", C.c_size_t), ("budget_bytes", C.c_size_t),
                 ("graph_s", C.c_double), ("graph_algo_bytes", C.c_double),
-                ("graph_epochs", C.c_longlong)]
+                ("graph_epochs", C.c_longlong), ("used_bytes", C.c_size_t),
+                ("byte_seconds", C.c_double), ("epoch_algo_bytes", C.c_double)]
 
 
 _SIGS = {

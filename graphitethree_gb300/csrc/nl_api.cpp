@@ -829,7 +829,12 @@ NLboolean nlSolve(void) {
     terr = std::max(terr, res.true_rel_residual);
     secs += res.seconds;
     outer += res.outer_steps;
-    if (res.status != NL_GB300_STATUS_CONVERGED) { ok = false; worst = res.status; }
+    // A stalled true residual still met OpenNL's own stopping rule (the
+    // recursive residual): nlSolve succeeds, NL_GB300_STATUS says which.
+    if (res.status != NL_GB300_STATUS_CONVERGED) {
+      worst = res.status;
+      if (res.status != NL_GB300_STATUS_TRUE_RESIDUAL_STALLED) ok = false;
+    }
   }
   c->used_iterations = iters;
   c->error = err;

@@ -315,24 +315,35 @@ NLuint nlSolveSystemIterative(NLBlas_t, NLMatrix M, NLMatrix P, const double* b,
 }
 
 // ---- NLBlas table ----
+// BLAS increments: element i of a strided n-vector sits at i * inc (inc > 0)
+// or (n - 1 - i) * |inc| (inc < 0), so a vector spans 1 + (n - 1) |inc|
+// doubles.  Host vectors are staged through device buffers of that span;
+// the arithmetic always runs on the GPU.
 static bool blas_inc_ok(int incx, int incy) {
-  if (incx != 1 || incy != 1) { report("NLBlas: only unit strides are supported"); return false; }
+  if (incx == 0 || incy == 0) { report("NLBlas: increments must be nonzero"); return false; }
   return true;
 }
 
+static size_t span(int n, int inc) { return n <= 0 ? 0 : 1 + (size_t)(n - 1) * (size_t)std::abs(inc); }
+
 static void blas_copy(NLBlas_t, int n, const double* x, int incx, double* y, int incy) {
   if (!blas_inc_ok(incx, incy) || n <= 0) return;
-  cudaMemcpyAsync(y, x, sizeof(double) * n, cudaMemcpyDefault, api_stream());
-  cudaStreamSynchronize(api_stream());
+  cudaStream_t s = api_stream();
+  Staged sx, sy;
+  // y is read too (a strided copy leaves the elements between strides alone)
+  if (!sx.in(x, span(n, incx), s) || !sy.in(y, span(n, incy), s)) return;
+  dev_copy_s(n, sx.d, incx, sy.d, incy, s);
+  sy.out(y, span(n, incy), s);
+  cudaStreamSynchronize(s);
 }
 
 static void blas_scal(NLBlas_t blas, int n, double a, double* x, int incx) {
   if (!blas_inc_ok(incx, 1) || n <= 0) return;
   cudaStream_t s = api_stream();
   Staged sx;
-  if (!sx.in(x, n, s)) return;
-  dev_scal(n, a, sx.d, s);
-  sx.out(x, n, s);
+  if (!sx.in(x, span(n, incx), s)) return;
+  dev_scal_s(n, a, sx.d, incx, s);
+  sx.out(x, span(n, incx), s);
   cudaStreamSynchronize(s);
   if (blas) blas->flops += n;
 }
@@ -341,9 +352,9 @@ static double blas_dot(NLBlas_t blas, int n, const double* x, int incx, const do
   if (!blas_inc_ok(incx, incy) || n <= 0) return 0.0;
   cudaStream_t s = api_stream();
   Staged sx, sy;
-  if (!sx.in(x, n, s) || !sy.in(y, n, s)) return 0.0;
+  if (!sx.in(x, span(n, incx), s) || !sy.in(y, span(n, incy), s)) return 0.0;
   double r = 0.0;
-  dev_dot(sx.d, sy.d, n, &r, s);
+  dev_dot_s(sx.d, incx, sy.d, incy, n, &r, s);
   if (blas) blas->flops += 2.0 * n;
   return r;
 }
@@ -357,9 +368,9 @@ static void blas_axpy(NLBlas_t blas, int n, double a, const double* x, int incx,
   if (!blas_inc_ok(incx, incy) || n <= 0) return;
   cudaStream_t s = api_stream();
   Staged sx, sy;
-  if (!sx.in(x, n, s) || !sy.in(y, n, s)) return;
-  dev_axpy(n, a, sx.d, sy.d, s);
-  sy.out(y, n, s);
+  if (!sx.in(x, span(n, incx), s) || !sy.in(y, span(n, incy), s)) return;
+  dev_axpy_s(n, a, sx.d, incx, sy.d, incy, s);
+  sy.out(y, span(n, incy), s);
   cudaStreamSynchronize(s);
   if (blas) blas->flops += 2.0 * n;
 }

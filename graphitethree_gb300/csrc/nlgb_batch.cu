@@ -26,6 +26,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 
@@ -39,11 +40,34 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
   return t;
 }
 
-constexpr unsigned long long kBarrierTimeoutNs = 4000000000ULL;   // 4 s
 
 // Barriers this CTA has completed in the current launch (set to 0 at kernel
 // start; every CTA of a team passes the same sequence of barriers).
 __shared__ unsigned long long s_bar_epoch;
+// Limit of one barrier wait (BatchArgs::barrier_timeout_ns, 4 s by default),
+// after which the CTA sets the launch's error flag and returns.
+__shared__ unsigned long long s_bar_timeout_ns;
+// Time box: the CTA's deadline on the GPU clock (0: none) and the stop
+// decision of the current iteration of its system.
+__shared__ unsigned long long s_deadline;
+__shared__ int s_stop;
+
+// Start of an iteration: the team's rank 0 decides whether the time box is
+// used up and publishes the answer before the iteration's first barrier (a
+// single CTA keeps it in shared memory).
+__device__ __forceinline__ void stop_probe(TeamBar* bar, int k, int r) {
+  if (s_deadline == 0ULL || r != 0 || threadIdx.x != 0) return;
+  const int late = globaltimer_ns() > s_deadline ? 1 : 0;
+  if (k > 1) *((volatile unsigned long long*)&bar->stop.count) = (unsigned long long)late;
+  else s_stop = late;
+}
+// Thread 0, after the iteration's first barrier: every CTA of the team reads
+// rank 0's decision (the writer passes the barrier's release before any
+// reader's acquire; the next write comes after the iteration's last barrier,
+// which every reader passes after reading).
+__device__ __forceinline__ void stop_read(TeamBar* bar, int k) {
+  if (s_deadline != 0ULL && k > 1) s_stop = (int)*((volatile unsigned long long*)&bar->stop.count);
+}
 
 __device__ __forceinline__ unsigned long long atom_add_acq_rel(unsigned long long* p, unsigned long long v) {
   unsigned long long old;
@@ -92,7 +116,7 @@ __device__ __noinline__ bool team_sync(TeamBar* bar, int k, int r, int* err) {
       while (ld_acquire(&bar->top.count) < target) {
         if ((++spins & 31u) == 0u) {
           if (*((volatile int*)err) != 0) { ok = 0; break; }
-          if (globaltimer_ns() - t0 > kBarrierTimeoutNs) {
+          if (globaltimer_ns() - t0 > s_bar_timeout_ns) {
             atomicExch(err, 1);
             ok = 0;
             break;
@@ -249,79 +273,94 @@ __device__ void run_system_once(const SysView& s, SysState* st, int r, int k, Te
                   st->stage = st->status == ST_RUNNING ? 1 : 2);
     }
   }
-  while (st->stage == 1 && (budget <= 0 || done_iters < budget)) {
-    if (!mixed) {
-      // q = A p, p.q
-      if (s.df) ph_spmv_pq<true>(s, r, k);
-      else ph_spmv_pq<false>(s, r, k);
-      if (!team_sync(bar, k, r, err)) break;
-      {
-        const Sums4 o = sums_of(s, kSlotPQ, 1);
-        NLGB_SCALAR(scalar_after_pq(st, o.v[0]));
-      }
-      if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
-      if (s.df) ph_update_xr<true>(s, r, k, st->alpha);
-      else ph_update_xr<false>(s, r, k, st->alpha);
-      if (!team_sync(bar, k, r, err)) break;
-      {
-        const Sums4 o = sums_of(s, kSlotXR, 2);
-        NLGB_SCALAR(scalar_after_xr(st, o.v[0], o.v[1]));
-      }
-      ++done_iters;
-      if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
+  for (;;) {
+    if (st->stage == 4) {
+      // continuation after a failed true-residual check (possibly left by
+      // another executor): the pending p update, then more iterations
       if (s.df) ph_update_p<true>(s, r, k, st->beta);
       else ph_update_p<false>(s, r, k, st->beta);
-      if (!team_sync(bar, k, r, err)) break;
-    } else {
-      // FP32 PCG iteration with FP64 reliable updates; same phase order as
-      // the graph solver: p update, SpMV + p.q, c/r update, [update].
-      ph_mx_update_p(s, r, k, st->beta);
-      if (!team_sync(bar, k, r, err)) break;
-      ph_mx_spmv_pq(s, r, k);
-      if (!team_sync(bar, k, r, err)) break;
-      {
-        const Sums4 o = sums_of(s, kSlotPQ, 1);
-        NLGB_SCALAR(scalar_after_pq(st, o.v[0]));
-      }
-      if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
-      ph_mx_update_cr(s, r, k, st->alpha);
-      if (!team_sync(bar, k, r, err)) break;
-      {
-        const Sums4 o = sums_of(s, kSlotXR, 2);
-        NLGB_SCALAR(scalar_after_mx_cr(st, o.v[0], o.v[1]));
-      }
-      ++done_iters;
-      if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
-      if (st->mode == 0) {
-        // reliable update: x += c, r = b - A x in FP64, FP32 residual replaced
-        ph_mx_apply(s, r, k);
+      if (!team_sync(bar, k, r, err)) { NLGB_SCALAR(st->status = ST_DEVICE_ERR; st->stage = 3); return; }
+      NLGB_SCALAR(st->stage = 1);
+    }
+    while (st->stage == 1 && (budget <= 0 || done_iters < budget)) {
+      stop_probe(bar, k, r);
+      if (!mixed) {
+        // q = A p, p.q
+        if (s.df) ph_spmv_pq<true>(s, r, k);
+        else ph_spmv_pq<false>(s, r, k);
         if (!team_sync(bar, k, r, err)) break;
-        ph_mx_outer(s, r, k);
-        if (!team_sync(bar, k, r, err)) break;
-        const Sums4 o = sums_of(s, kSlotInit, 4);
-        NLGB_SCALAR(scalar_after_outer(st, o.v[0], o.v[1], o.v[2], o.v[3]);
-                    // FP32 cannot track this system: continue it in FP64
-                    // from the current x (same rule as the graph solver).
-                    if (st->status == ST_STAGNATION && !st->fell_back) {
-                      st->status = ST_RUNNING; st->precision = 0; st->fell_back = 1;
-                      st->stage = 0; st->mode = 0; st->iter_at_fallback = st->iter;
-                    });
-        if (st->stage == 0) break;
+        {
+          const Sums4 o = sums_of(s, kSlotPQ, 1);
+          NLGB_SCALAR(scalar_after_pq(st, o.v[0]); stop_read(bar, k));
+        }
         if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
+        if (s.df) ph_update_xr<true>(s, r, k, st->alpha);
+        else ph_update_xr<false>(s, r, k, st->alpha);
+        if (!team_sync(bar, k, r, err)) break;
+        {
+          const Sums4 o = sums_of(s, kSlotXR, 2);
+          NLGB_SCALAR(scalar_after_xr(st, o.v[0], o.v[1]));
+        }
+        ++done_iters;
+        if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
+        if (s.df) ph_update_p<true>(s, r, k, st->beta);
+        else ph_update_p<false>(s, r, k, st->beta);
+        if (!team_sync(bar, k, r, err)) break;
+        if (s_stop) break;   // time box used up: the system resumes next epoch
+      } else {
+        // FP32 PCG iteration with FP64 reliable updates; same phase order as
+        // the graph solver: p update, SpMV + p.q, c/r update, [update].
+        ph_mx_update_p(s, r, k, st->beta);
+        if (!team_sync(bar, k, r, err)) break;
+        ph_mx_spmv_pq(s, r, k);
+        if (!team_sync(bar, k, r, err)) break;
+        {
+          const Sums4 o = sums_of(s, kSlotPQ, 1);
+          NLGB_SCALAR(scalar_after_pq(st, o.v[0]); stop_read(bar, k));
+        }
+        if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
+        ph_mx_update_cr(s, r, k, st->alpha);
+        if (!team_sync(bar, k, r, err)) break;
+        {
+          const Sums4 o = sums_of(s, kSlotXR, 2);
+          NLGB_SCALAR(scalar_after_mx_cr(st, o.v[0], o.v[1]));
+        }
+        ++done_iters;
+        if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
+        if (st->mode == 0) {
+          // reliable update: x += c, r = b - A x in FP64, FP32 residual replaced
+          ph_mx_apply(s, r, k);
+          if (!team_sync(bar, k, r, err)) break;
+          ph_mx_outer(s, r, k);
+          if (!team_sync(bar, k, r, err)) break;
+          const Sums4 o = sums_of(s, kSlotInit, 4);
+          NLGB_SCALAR(scalar_after_outer(st, o.v[0], o.v[1], o.v[2], o.v[3]);
+                      // FP32 cannot track this system: continue it in FP64
+                      // from the current x (same rule as the graph solver).
+                      if (st->status == ST_STAGNATION && !st->fell_back) {
+                        st->status = ST_RUNNING; st->precision = 0; st->fell_back = 1;
+                        st->stage = 0; st->mode = 0; st->iter_at_fallback = st->iter;
+                      });
+          if (st->stage == 0) break;
+          if (st->status != ST_RUNNING) { NLGB_SCALAR(st->stage = 2); break; }
+        }
+        if (s_stop) break;   // time box used up: the system resumes next epoch
       }
     }
-  }
-  if (*((volatile int*)err) != 0 && st->stage != 3) {
-    NLGB_SCALAR(st->status = ST_DEVICE_ERR; st->stage = 3);
+    if (*((volatile int*)err) != 0 && st->stage != 3) {
+      NLGB_SCALAR(st->status = ST_DEVICE_ERR; st->stage = 3);
+      return;
+    }
+    if (st->stage == 2) {
+      // final true residual (FP64) of the returned x; x = 0 when b == 0
+      if (s.df) ph_final<true>(s, r, k, st->zero_rhs != 0);
+      else ph_final<false>(s, r, k, st->zero_rhs != 0);
+      if (!team_sync(bar, k, r, err)) { NLGB_SCALAR(st->status = ST_DEVICE_ERR; st->stage = 3); return; }
+      const Sums4 o = sums_of(s, kSlotFinal, 1);
+      NLGB_SCALAR(st->rr_true = o.v[0]; st->stage = scalar_after_check(st) ? 4 : 3);
+      if (st->stage == 4) continue;
+    }
     return;
-  }
-  if (st->stage == 2) {
-    // final true residual (FP64) of the returned x; x = 0 when b == 0
-    if (s.df) ph_final<true>(s, r, k, st->zero_rhs != 0);
-    else ph_final<false>(s, r, k, st->zero_rhs != 0);
-    if (!team_sync(bar, k, r, err)) { NLGB_SCALAR(st->status = ST_DEVICE_ERR; st->stage = 3); return; }
-    const Sums4 o = sums_of(s, kSlotFinal, 1);
-    NLGB_SCALAR(st->rr_true = o.v[0]; st->stage = 3);
   }
 }
 
@@ -341,15 +380,23 @@ __global__ void __launch_bounds__(kCTA, 4) k_batch(BatchArgs a) {
   __shared__ SysState sst;
   __shared__ int pick;
   const int cta = blockIdx.x;
-  if (threadIdx.x == 0) s_bar_epoch = 0ULL;
+  if (threadIdx.x == 0) {
+    s_bar_epoch = 0ULL;
+    s_bar_timeout_ns = a.barrier_timeout_ns;
+    s_deadline = a.epoch_ns > 0ULL ? globaltimer_ns() + a.epoch_ns : 0ULL;
+    s_stop = 0;
+  }
+  if (a.times && cta == 0 && threadIdx.x == 0) a.times[0] = globaltimer_ns();
   __syncthreads();
   auto load = [&](int sys) {
     if (threadIdx.x == 0) {
       sv = a.views[sys];
       sst = *sv.st;
+      s_stop = 0;
     }
     __syncthreads();
   };
+  auto past_deadline = [&]() { return s_deadline != 0ULL && globaltimer_ns() > s_deadline; };
   auto store = [&](bool rank0) {
     __syncthreads();
     if (rank0 && threadIdx.x == 0) {
@@ -365,15 +412,17 @@ __global__ void __launch_bounds__(kCTA, 4) k_batch(BatchArgs a) {
     TeamBar* bar = a.bars + team;
     for (int j = td.sys_begin; j < td.sys_end; ++j) {
       load(a.team_sys[j]);
-      if (sst.stage != 3) run_system(sv, &sst, r, td.k, bar, a.err, a.budget);
+      if (sst.stage != 3) run_system(sv, &sst, r, td.k, bar, a.err, sv.budget > 0 ? sv.budget : a.budget);
       store(r == 0);
     }
     // Then the shared team queue: rank 0 draws the next system and publishes
     // it through the team barrier; a second barrier keeps the next draw from
     // overwriting `pick` before every CTA of the team has read it.
     while (a.n_tqueue > 0) {
+      // past the time box, rank 0 draws nothing (publishes the end of the queue)
       if (r == 0 && threadIdx.x == 0)
-        *((volatile unsigned long long*)&bar->pick.count) = atomicAdd(a.tqueue_head, 1u);
+        *((volatile unsigned long long*)&bar->pick.count) =
+            past_deadline() ? (unsigned long long)a.n_tqueue : atomicAdd(a.tqueue_head, 1u);
       if (!team_sync(bar, td.k, r, a.err)) break;
       if (threadIdx.x == 0) pick = (int)*((volatile unsigned long long*)&bar->pick.count);
       __syncthreads();
@@ -381,20 +430,22 @@ __global__ void __launch_bounds__(kCTA, 4) k_batch(BatchArgs a) {
       if (!team_sync(bar, td.k, r, a.err)) break;
       if (q >= a.n_tqueue) break;
       load(a.tqueue[q]);
-      if (sst.stage != 3) run_system(sv, &sst, r, td.k, bar, a.err, a.budget);
+      if (sst.stage != 3) run_system(sv, &sst, r, td.k, bar, a.err, sv.budget > 0 ? sv.budget : a.budget);
       store(r == 0);
     }
+    if (a.times && r == 0 && threadIdx.x == 0) a.times[2 + team] = globaltimer_ns();
   } else {
     while (true) {
-      if (threadIdx.x == 0) pick = (int)atomicAdd(a.queue_head, 1u);
+      if (threadIdx.x == 0) pick = past_deadline() ? a.n_queue : (int)atomicAdd(a.queue_head, 1u);
       __syncthreads();
       const int q = pick;
       __syncthreads();
       if (q >= a.n_queue) break;
       load(a.queue[q]);
-      if (sst.stage != 3) run_system(sv, &sst, 0, 1, nullptr, a.err, a.budget);
+      if (sst.stage != 3) run_system(sv, &sst, 0, 1, nullptr, a.err, sv.budget > 0 ? sv.budget : a.budget);
       store(true);
     }
+    if (a.times && threadIdx.x == 0) atomicMax(&a.times[1], globaltimer_ns());
   }
 }
 
@@ -410,7 +461,7 @@ __global__ void k_gather_states(const SysView* views, int n, SysState* out) {
 // ---------------------------------------------------------------------------
 BatchRunner::~BatchRunner() {
   cudaFree(d_views_); cudaFree(d_teams_); cudaFree(d_cta_team_); cudaFree(d_team_sys_);
-  cudaFree(d_queue_); cudaFree(d_tqueue_); cudaFree(d_bars_); cudaFree(d_ctl_);
+  cudaFree(d_queue_); cudaFree(d_tqueue_); cudaFree(d_bars_); cudaFree(d_ctl_); cudaFree(d_times_);
   if (h_err_) cudaFreeHost(h_err_);
   cudaFree(d_states_);
   if (ev0_) cudaEventDestroy(ev0_);
@@ -431,6 +482,15 @@ cudaError_t BatchRunner::init(cudaStream_t s) {
   *h_err_ = 0;
   NLGB_CUDA_TRY(cudaEventCreate(&ev0_));
   NLGB_CUDA_TRY(cudaEventCreate(&ev1_));
+  // Test hooks for the barrier's failure path (read once per runner): a
+  // shorter wait limit, and a first team told to wait for one CTA more than
+  // it is given, so that its first barrier runs out -- the kernel must then
+  // flag the error, return, and leave the GPU usable.
+  if (const char* e = std::getenv("NLGB_BARRIER_TIMEOUT_MS")) {
+    const double ms = std::atof(e);
+    if (ms > 0.0) barrier_timeout_ns_ = (unsigned long long)(ms * 1e6);
+  }
+  if (const char* e = std::getenv("NLGB_TEST_TEAM_SHORTFALL")) test_shortfall_ = e[0] == '1';
   return cudaSuccess;
 }
 
@@ -470,7 +530,7 @@ void BatchRunner::plan(const std::vector<SysView>& views, const std::vector<long
     reserve = (int)std::ceil((double)grid_ * w_small / (w_small + w_large));
     reserve = std::max(1, std::min(reserve, std::min((int)queue_.size(), grid_ / 2)));
   }
-  const int avail = grid_ - reserve;
+  const int avail = grid_ - reserve_ - reserve;
   if (avail < 2) {   // no room for a team: everything goes to the queue workers
     queue_.insert(queue_.begin(), large.begin(), large.end());
     return;
@@ -500,6 +560,48 @@ void BatchRunner::plan(const std::vector<SysView>& views, const std::vector<long
   }
 }
 
+constexpr int kPrioTilesPerCta = 4;
+
+void BatchRunner::plan_priority(const std::vector<SysView>& views) {
+  teams_.clear(); cta_team_.clear(); team_sys_.clear(); queue_.clear(); tqueue_.clear();
+  const int n = (int)views.size();
+  const int avail_all = std::max(1, grid_ - reserve_);
+  int n_small = 0;
+  for (int i = 0; i < n; ++i) n_small += views[i].n_tiles < kLargeTiles ? 1 : 0;
+  // queue workers: one per small system, at most half the grid
+  const int workers = n_small == 0 ? 0 : std::max(1, std::min(n_small, avail_all / 2));
+  const int avail = avail_all - workers;
+  int cta = 0;
+  for (int i = 0; i < n; ++i) {
+    if (views[i].n_tiles < kLargeTiles) { queue_.push_back(i); continue; }
+    const int room = avail - cta;
+    if (room < 2) { tqueue_.push_back(i); continue; }
+    // about kPrioTilesPerCta tiles per CTA: enough CTAs to finish the
+    // system soon, few enough that each CTA's tile work outweighs the
+    // team's barriers and that the next systems get teams too
+    int k = std::min({(views[i].n_tiles + kPrioTilesPerCta - 1) / kPrioTilesPerCta, kBarGroup * kBarMaxGroups,
+                      room});
+    k = std::max(2, k);
+    // balanced: the fewest CTAs with the same tiles on the busiest CTA
+    const int per = (views[i].n_tiles + k - 1) / k;
+    k = std::max(2, (views[i].n_tiles + per - 1) / per);
+    TeamDesc td;
+    td.cta_begin = cta;
+    td.k = k;
+    td.sys_begin = (int)team_sys_.size();
+    team_sys_.push_back(i);
+    td.sys_end = (int)team_sys_.size();
+    for (int c = 0; c < k; ++c) cta_team_.push_back((int)teams_.size());
+    teams_.push_back(td);
+    cta += k;
+  }
+  // without any team, large systems left over go to the queue workers too
+  if (teams_.empty() && !tqueue_.empty()) {
+    queue_.insert(queue_.end(), tqueue_.begin(), tqueue_.end());
+    tqueue_.clear();
+  }
+}
+
 cudaError_t BatchRunner::run(const std::vector<SysView>& views, const std::vector<long long>& work,
                              long long budget, BatchLaunchStats* stats) {
   NLGB_CUDA_TRY(launch(views, work, budget));
@@ -510,7 +612,8 @@ cudaError_t BatchRunner::launch(const std::vector<SysView>& views, const std::ve
                                 long long budget) {
   pending_ = false;
   if (views.empty()) return cudaSuccess;
-  plan(views, work);
+  if (priority_plan_) plan_priority(views);
+  else plan(views, work);
   NLGB_CUDA_TRY(ensure(d_views_, cap_views_, views.size()));
   NLGB_CUDA_TRY(ensure(d_teams_, cap_teams_, teams_.size()));
   NLGB_CUDA_TRY(ensure(d_cta_team_, cap_cta_team_, cta_team_.size()));
@@ -521,7 +624,14 @@ cudaError_t BatchRunner::launch(const std::vector<SysView>& views, const std::ve
   cudaStream_t s = stream_;
   NLGB_CUDA_TRY(cudaMemcpyAsync(d_views_, views.data(), views.size() * sizeof(SysView), cudaMemcpyHostToDevice, s));
   if (!teams_.empty()) {
-    NLGB_CUDA_TRY(cudaMemcpyAsync(d_teams_, teams_.data(), teams_.size() * sizeof(TeamDesc), cudaMemcpyHostToDevice, s));
+    if (test_shortfall_ && teams_[0].k < kBarFlat) {
+      std::vector<TeamDesc> t = teams_;
+      t[0].k += 1;   // no CTA is mapped to the extra rank: the team's barrier cannot complete
+      NLGB_CUDA_TRY(cudaMemcpy(d_teams_, t.data(), t.size() * sizeof(TeamDesc), cudaMemcpyHostToDevice));
+    } else {
+      NLGB_CUDA_TRY(cudaMemcpyAsync(d_teams_, teams_.data(), teams_.size() * sizeof(TeamDesc),
+                                    cudaMemcpyHostToDevice, s));
+    }
     NLGB_CUDA_TRY(cudaMemcpyAsync(d_cta_team_, cta_team_.data(), cta_team_.size() * sizeof(int), cudaMemcpyHostToDevice, s));
     NLGB_CUDA_TRY(cudaMemcpyAsync(d_team_sys_, team_sys_.data(), team_sys_.size() * sizeof(int), cudaMemcpyHostToDevice, s));
     NLGB_CUDA_TRY(cudaMemsetAsync(d_bars_, 0, teams_.size() * sizeof(TeamBar), s));
@@ -547,8 +657,18 @@ cudaError_t BatchRunner::launch(const std::vector<SysView>& views, const std::ve
   a.n_queue = (int)queue_.size();
   a.n_tqueue = teams_.empty() ? 0 : (int)tqueue_.size();
   a.budget = budget;
-  // Grid: every team CTA plus queue workers, never more than can be resident.
-  const int workers = queue_.empty() ? 0 : std::min(grid_ - a.team_ctas, (int)queue_.size());
+  a.times = nullptr;
+  a.barrier_timeout_ns = barrier_timeout_ns_;
+  a.epoch_ns = epoch_ns_;
+  if (timing_) {
+    NLGB_CUDA_TRY(ensure(d_times_, cap_times_, teams_.size() + 2));
+    NLGB_CUDA_TRY(cudaMemsetAsync(d_times_, 0, (teams_.size() + 2) * sizeof(unsigned long long), s));
+    a.times = d_times_;
+  }
+  // Grid: every team CTA plus queue workers, never more than can be resident
+  // (less the reserve).
+  const int workers = queue_.empty() ? 0 : std::max(1, std::min(std::max(1, grid_ - reserve_) - a.team_ctas,
+                                                                (int)queue_.size()));
   const int grid = a.team_ctas + std::max(0, workers);
   void* args[] = {&a};
   NLGB_CUDA_TRY(cudaEventRecord(ev0_, s));
@@ -570,6 +690,11 @@ cudaError_t BatchRunner::finish(BatchLaunchStats* stats) {
   NLGB_CUDA_TRY(cudaStreamSynchronize(stream_));
   float ms = 0.f;
   cudaEventElapsedTime(&ms, ev0_, ev1_);
+  if (timing_) {
+    h_times_.assign(teams_.size() + 2, 0ULL);
+    NLGB_CUDA_TRY(cudaMemcpy(h_times_.data(), d_times_, h_times_.size() * sizeof(unsigned long long),
+                             cudaMemcpyDeviceToHost));
+  }
   const int err = *h_err_;
   if (stats) {
     stats->ms = ms;

@@ -36,6 +36,7 @@ struct TeamBar {
   BarLine top;
   BarLine grp[kBarMaxGroups];
   BarLine pick;   // .count: team-queue entry drawn by the team's rank 0
+  BarLine stop;   // .count: 1 when rank 0 found the epoch's time box used up
 };
 
 struct TeamDesc {
@@ -60,6 +61,15 @@ struct BatchArgs {
   int n_queue;
   int n_tqueue;
   long long budget;          // iterations per system in this launch (<= 0: no limit)
+  // Optional timing (null: off), %globaltimer ns: [0] kernel start, [1] last
+  // queue worker done, [2 + t] team t done.
+  unsigned long long* times;
+  unsigned long long barrier_timeout_ns;   // limit of one team-barrier wait
+  // Time box of the launch (0: none): a system stops at the first iteration
+  // boundary after it (its team's rank 0 reads the clock at the start of
+  // each iteration and tells the team through the iteration's first
+  // barrier), and no further system is started.
+  unsigned long long epoch_ns;
 };
 
 struct BatchLaunchStats {
@@ -93,29 +103,42 @@ struct SystemSlot {
   void release(cudaStream_t s);
 };
 
-// Resumable FP64 PCG continuation, as CUDA graph chunks, of a system whose
-// buffers and device state belong to a SystemSlot (see nlgb_solver.cu).
+// Resumable PCG chunks (FP64, double-float or mixed precision) of a system
+// whose buffers and device state belong to a SystemSlot, as CUDA graphs (see
+// nlgb_solver.cu).
 class ViewGraph {
  public:
   ViewGraph() = default;
   ~ViewGraph();
   ViewGraph(const ViewGraph&) = delete;
   ViewGraph& operator=(const ViewGraph&) = delete;
+  // Build (or keep) the chunk graph of this system (mixed: the
+  // mixed-precision iteration); run() does it too, prepare() lets a caller
+  // pay the instantiation ahead of time.
+  cudaError_t prepare(const SysView& v, bool mixed);
   // Queue a chunk of at most `iters` iterations (whole passes of 4) of the
-  // system on stream s; finish() waits for it and stores its time in *ms.
-  cudaError_t run(const SysView& v, long long iters, cudaStream_t s, float* ms);
+  // system on stream s; finish() waits for it and stores its time in *ms;
+  // done() tells, without blocking, whether it has finished.
+  cudaError_t run(const SysView& v, long long iters, cudaStream_t s, float* ms, bool mixed = false);
+  bool done() const;
   cudaError_t finish(long long iters_before, long long iters_after);
 
  private:
-  cudaError_t build(const SysView& v);
+  cudaError_t build(const SysView& v, bool mixed);
   cudaError_t run_eager(cudaStream_t s, long long iters);
   SysView view_{};
+  bool mixed_ = false;
   cudaGraphExec_t exec_ = nullptr;
   cudaEvent_t e0_ = nullptr, e1_ = nullptr;
   float* ms_ = nullptr;
   bool pending_ = false;
   bool eager_counted_ = false;
 };
+
+// A mixed system whose state says STAGNATION (FP32 cannot track it) is
+// switched to FP64 PCG from its current x (stage 0, iteration count kept);
+// stream-ordered, before the system's next chunk.
+cudaError_t chunk_fallback_fp64(SysState* st, cudaStream_t s);
 
 // Launches the persistent kernel over a set of resident systems.  Each
 // system's SysState (device) must be initialised by the caller (status
@@ -143,9 +166,26 @@ class BatchRunner {
   // (host, pinned or pageable; views.size() entries), one transfer.
   cudaError_t gather_states(SysState* out, int n);
   int max_grid() const { return grid_; }
+  // Per-team completion times of the next launches (tracing): after
+  // finish(), last_times() holds [kernel start, queue workers done, team
+  // 0 done, ...] in ns of the GPU clock.
+  void set_timing(bool on) { timing_ = on; }
+  // Time box of the next launches (0: none, every system runs its budget).
+  void set_epoch_ns(unsigned long long ns) { epoch_ns_ = ns; }
+  // Priority plan: the views are given in priority order; teams (one CTA
+  // per tile at most) go to the large systems in that order until the grid
+  // is used, the rest wait in the team queue in that order, small systems go
+  // to the queue workers in that order.  Otherwise: the work-proportional
+  // plan (plan()).
+  void set_priority_plan(bool on) { priority_plan_ = on; }
+  // CTAs of the co-resident capacity left unused (room for kernels of other
+  // streams, e.g. system builds, while an epoch runs).
+  void set_reserve(int ctas) { reserve_ = ctas; }
+  const std::vector<unsigned long long>& last_times() const { return h_times_; }
 
  private:
   void plan(const std::vector<SysView>& views, const std::vector<long long>& work);
+  void plan_priority(const std::vector<SysView>& views);
 
   cudaStream_t stream_ = nullptr;
   int n_sm_ = 0, per_sm_ = 0, grid_ = 0;
@@ -164,6 +204,15 @@ class BatchRunner {
   size_t cap_states_ = 0;
   int last_grid_ = 0, last_workers_ = 0;
   bool pending_ = false;
+  bool timing_ = false;
+  bool priority_plan_ = false;
+  int reserve_ = 0;
+  unsigned long long epoch_ns_ = 0;
+  unsigned long long barrier_timeout_ns_ = 4000000000ULL;
+  bool test_shortfall_ = false;
+  unsigned long long* d_times_ = nullptr;
+  size_t cap_times_ = 0;
+  std::vector<unsigned long long> h_times_;
 };
 
 }  // namespace nlgb

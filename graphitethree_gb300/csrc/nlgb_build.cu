@@ -144,11 +144,18 @@ __global__ void k_set_locked(double* xl, int4 vars, double4 values) {
 
 int grid_of(long long n, int block) { return (int)std::max(1LL, std::min<long long>((n + block - 1) / block, 1LL << 30)); }
 
+// Stream-ordered scratch (cudaMallocAsync / cudaFreeAsync): no device-wide
+// synchronisation, so a build can run while a solver kernel occupies the
+// GPU (the solve server admits requests during an epoch).
 struct DevBuf {
   void* p = nullptr;
-  ~DevBuf() { cudaFree(p); }
+  cudaStream_t st = nullptr;
+  ~DevBuf() { if (p) cudaFreeAsync(p, st); }
   template <typename T>
-  cudaError_t alloc(size_t count) { return cudaMalloc(&p, std::max<size_t>(1, count) * sizeof(T)); }
+  cudaError_t alloc(size_t count, cudaStream_t s) {
+    st = s;
+    return cudaMallocAsync(&p, std::max<size_t>(1, count) * sizeof(T), s);
+  }
   template <typename T>
   T* as() const { return static_cast<T*>(p); }
 };
@@ -157,14 +164,14 @@ struct DevBuf {
 // the triangle-index check.
 cudaError_t mesh_to_device(int n_verts, const double* xyz, int n_tris, const int* tris, DevBuf& dx,
                            DevBuf& dt, cudaStream_t s, bool* bad_index) {
-  NLGB_CUDA_TRY(dx.alloc<double>(3 * (size_t)n_verts));
-  NLGB_CUDA_TRY(dt.alloc<int>(3 * (size_t)n_tris));
+  NLGB_CUDA_TRY(dx.alloc<double>(3 * (size_t)n_verts, s));
+  NLGB_CUDA_TRY(dt.alloc<int>(3 * (size_t)n_tris, s));
   if (n_verts > 0)
     NLGB_CUDA_TRY(cudaMemcpyAsync(dx.p, xyz, sizeof(double) * 3 * (size_t)n_verts, cudaMemcpyDefault, s));
   if (n_tris > 0)
     NLGB_CUDA_TRY(cudaMemcpyAsync(dt.p, tris, sizeof(int) * 3 * (size_t)n_tris, cudaMemcpyDefault, s));
   DevBuf flag;
-  NLGB_CUDA_TRY(flag.alloc<int>(1));
+  NLGB_CUDA_TRY(flag.alloc<int>(1, s));
   NLGB_CUDA_TRY(cudaMemsetAsync(flag.p, 0, sizeof(int), s));
   if (n_tris > 0) {
     k_check_tris<<<grid_of(3LL * n_tris, 256), 256, 0, s>>>(3LL * n_tris, dt.as<int>(), n_verts, flag.as<int>());
@@ -194,10 +201,10 @@ cudaError_t build_lscm_system(int n_verts, const double* xyz, int n_tris, const 
   const int n_vars = 2 * n_verts, n_free = n_vars - 4;
   const long long n_rows = 2LL * n_tris, n_coefs = 6 * n_rows;
   DevBuf rp, col, val, xl;
-  NLGB_CUDA_TRY(rp.alloc<long long>((size_t)n_rows + 1));
-  NLGB_CUDA_TRY(col.alloc<int>((size_t)n_coefs));
-  NLGB_CUDA_TRY(val.alloc<double>((size_t)n_coefs));
-  NLGB_CUDA_TRY(xl.alloc<double>((size_t)n_vars));
+  NLGB_CUDA_TRY(rp.alloc<long long>((size_t)n_rows + 1, s));
+  NLGB_CUDA_TRY(col.alloc<int>((size_t)n_coefs, s));
+  NLGB_CUDA_TRY(val.alloc<double>((size_t)n_coefs, s));
+  NLGB_CUDA_TRY(xl.alloc<double>((size_t)n_vars, s));
   NLGB_CUDA_TRY(cudaMemsetAsync(xl.p, 0, sizeof(double) * (size_t)n_vars, s));
   k_set_locked<<<1, 1, 0, s>>>(xl.as<double>(), locked, make_double4(uv0[0], uv0[1], uv1[0], uv1[1]));
   k_row_ptr<<<grid_of(n_rows + 1, 256), 256, 0, s>>>(n_rows, n_rows, 6, rp.as<long long>());
@@ -225,12 +232,12 @@ cudaError_t build_fairing_system(int n_verts, const double* xyz, int n_tris, con
   const long long n_edge_rows = 3LL * n_tris, n_rows = n_edge_rows + n_verts;
   const long long n_coefs = 2 * n_edge_rows + n_verts;
   DevBuf rp, col, val, w, xl, rhs;
-  NLGB_CUDA_TRY(rp.alloc<long long>((size_t)n_rows + 1));
-  NLGB_CUDA_TRY(col.alloc<int>((size_t)n_coefs));
-  NLGB_CUDA_TRY(val.alloc<double>((size_t)n_coefs));
-  NLGB_CUDA_TRY(w.alloc<double>((size_t)n_rows));
-  NLGB_CUDA_TRY(xl.alloc<double>(1));
-  NLGB_CUDA_TRY(rhs.alloc<double>((size_t)n_verts));
+  NLGB_CUDA_TRY(rp.alloc<long long>((size_t)n_rows + 1, s));
+  NLGB_CUDA_TRY(col.alloc<int>((size_t)n_coefs, s));
+  NLGB_CUDA_TRY(val.alloc<double>((size_t)n_coefs, s));
+  NLGB_CUDA_TRY(w.alloc<double>((size_t)n_rows, s));
+  NLGB_CUDA_TRY(xl.alloc<double>(1, s));
+  NLGB_CUDA_TRY(rhs.alloc<double>((size_t)n_verts, s));
   NLGB_CUDA_TRY(cudaMemsetAsync(xl.p, 0, sizeof(double), s));
   k_row_ptr<<<grid_of(n_rows + 1, 256), 256, 0, s>>>(n_rows, n_edge_rows, 2, rp.as<long long>());
   count_launches(1);

@@ -41,7 +41,13 @@ enum : int {
   ST_DEVICE_ERR = 5,
   ST_BAD_INPUT = 6,
   ST_ABORTED = 7,
+  ST_TRUE_STALLED = 8,   // recursive residual met eps, the true one did not after kMaxTrueChecks continuations
 };
+
+// FP64 / double-float solves stop on the recursive residual (OpenNL's rule)
+// and then recompute the true one: at most this many times the iteration is
+// continued with a lower recursive threshold before ST_TRUE_STALLED.
+constexpr int kMaxTrueChecks = 4;
 
 // Device-resident scalar state of one system (one per system, in HBM).
 struct __align__(16) SysState {
@@ -64,13 +70,24 @@ struct __align__(16) SysState {
   int zero_rhs;                // b == 0: the solution is x = 0
   int stall;                   // mixed: outer steps in a row without progress
   unsigned int cnt[4];         // last-CTA counters of the phase kernels
-  int stage;                   // batched: 0 start, 1 iterating, 2 final residual due, 3 done
+  int stage;                   // 0 start, 1 iterating, 2 final residual due, 3 done, 4 continuation
+                               // due (the p update after a failed true-residual check is pending)
   int precision;               // batched: 0 FP64, 1 mixed
   int fell_back;               // mixed system continued in FP64 (FP32 could not track it)
-  int pad_;
+  int checks;                  // FP64 / double-float: continuations after a failed true-residual check
   long long iter_at_fallback;  // FP32 iterations done before the FP64 fallback
   long long iter_stop;         // > 0: a graph chunk pauses (status unchanged) at this iteration
   long long coop_epoch;        // single-kernel iterations run in this solve (grid-barrier targets)
+  double rthresh2;             // FP64 / double-float: threshold^2 of the recursive residual (starts at thresh2)
+  int cont_ok;                 // beta / rho of the last iteration are valid (the iteration can be continued)
+  int pad_;
+  // Two-level election of the graph solver's p.q (0) and x/r (1) phase
+  // kernels: arrivals per group of tiles, groups done, and each group's
+  // warp-level sums (canonical order, see elect2 in nlgb_solver.cu).
+  unsigned int gcnt[2][8];
+  unsigned int tcnt[2];
+  unsigned int pad2_[2];
+  double wsum[2][8][2];
 };
 
 // Algorithmic HBM bytes of one solve (n rows, z nonzeros), from its final
@@ -87,6 +104,9 @@ inline __host__ __device__ double algo_bytes(long long n, long long z, const Sys
   b += it64 * (12.0 * Z + 108.0 * N) + it32 * (8.0 * Z + 56.0 * N);
   b += double(h.outer) * (12.0 * Z + 52.0 * N);
   if (h.fell_back) b += 12.0 * Z + 36.0 * N;   // FP64 restart residual
+  // each failed true-residual check: that residual pass and the p update
+  // that resumes the iteration
+  b += double(h.checks) * (12.0 * Z + 48.0 * N);
   return b;
 }
 
@@ -123,6 +143,7 @@ struct SysView {
   double* part;          // n_tiles * kParts tile partials
   SysState* st;
   const volatile int* abort_flag;   // host-mapped; nonzero -> stop
+  long long budget;      // persistent kernel: iterations in this launch (> 0; else the launch's own)
 };
 
 // ---------------------------------------------------------------------------
@@ -743,6 +764,9 @@ __device__ __forceinline__ bool finite_pos(double v) { return v > 0.0 && v < 1.0
 // After the initial residual: decide whether any iteration is needed.
 __device__ __forceinline__ void scalar_after_init(SysState* st, double bb, double rz, double rr) {
   st->bnorm2 = bb;
+  st->rthresh2 = st->thresh2;
+  st->checks = 0;
+  st->cont_ok = 0;
   st->rho = rz;
   st->rr = rr;
   if (!st->fell_back) st->iter = 0;   // a fallback keeps counting the FP32 iterations
@@ -762,15 +786,48 @@ __device__ __forceinline__ void scalar_after_pq(SysState* st, double pq) {
   st->alpha = st->rho / pq;
 }
 
+// beta and rho are advanced before the stopping test, so that an iteration
+// stopped on the recursive residual can be continued (scalar_after_check).
 __device__ __forceinline__ void scalar_after_xr(SysState* st, double rz, double rr) {
   st->iter += 1;
   st->rr = rr;
   if (!(rr <= 1.0e300)) { st->status = ST_BREAKDOWN; return; }
-  if (rr <= st->thresh2 * st->bnorm2) { st->status = ST_CONVERGED; return; }
+  const bool rz_ok = finite_pos(rz);
+  st->cont_ok = rz_ok ? 1 : 0;
+  if (rz_ok) {
+    st->beta = rz / st->rho;
+    st->rho = rz;
+  }
+  if (rr <= st->rthresh2 * st->bnorm2) { st->status = ST_CONVERGED; return; }
   if (st->iter >= st->max_iter) { st->status = ST_MAX_ITER; return; }
-  if (!finite_pos(rz)) { st->status = ST_BREAKDOWN; return; }
-  st->beta = rz / st->rho;
-  st->rho = rz;
+  if (!rz_ok) { st->status = ST_BREAKDOWN; return; }
+}
+
+// After the final true residual ||b - A x||^2 (rr_true) of an FP64 or
+// double-float solve.  The iteration stopped when its recursively updated
+// residual met eps (OpenNL's rule); in finite precision that residual drifts
+// away from the true one, so the true one may still miss eps.  Then the
+// recursive threshold is lowered by the observed ratio (with a 0.9 margin in
+// norm) and the same recurrence continues (status back to ST_RUNNING,
+// returns true; the caller applies the pending p update first).  After
+// kMaxTrueChecks continuations, or when the gap is too large to close by
+// iterating (the recursive residual would have to go 1e4x below eps: the
+// attainable accuracy of the recurrence is reached), the solve ends with
+// ST_TRUE_STALLED.  Mixed-precision systems stop on the true residual
+// already and are left alone.
+__host__ __device__ __forceinline__ bool scalar_after_check(SysState* st) {
+  if (st->status != ST_CONVERGED || st->zero_rhs || st->precision == 1) return false;
+  if (st->rr_true <= st->thresh2 * st->bnorm2) return false;
+  const double next = st->thresh2 * (st->rr / st->rr_true) * 0.81;
+  if (!st->cont_ok || st->checks >= kMaxTrueChecks || st->iter >= st->max_iter || !(st->rr > 0.0) ||
+      !(next >= st->thresh2 * 1.0e-8)) {
+    st->status = ST_TRUE_STALLED;
+    return false;
+  }
+  st->rthresh2 = next;
+  st->checks += 1;
+  st->status = ST_RUNNING;
+  return true;
 }
 
 // Mixed precision = FP32 PCG with FP64 reliable updates (defect correction

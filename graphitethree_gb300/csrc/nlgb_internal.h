@@ -9,6 +9,7 @@
 namespace nlgb {
 
 struct SysState;
+struct SysView;
 
 // Thread-local error text reported by nlGetErrorString()/nlgb_last_error().
 void set_error(const std::string& msg);
@@ -115,8 +116,12 @@ class PcgSolver {
   cudaError_t alloc(bool mixed);
   cudaError_t run_graph(bool mixed, bool df, const SolveParams& prm, long long max_iter,
                         long long done, int outer, float* ms);
-  cudaError_t run_eager(bool mixed, bool df, SysState* h);
-  cudaError_t build_plain_graph(bool df);
+  cudaError_t run_eager(bool mixed, bool df, SysState* h, bool cont = false);
+  // continuation after a failed true-residual check (state: running, stage 4)
+  cudaError_t run_cont(bool df, float* ms);
+  cudaError_t add_plain_loop(cudaGraph_t g, cudaGraphNode_t dep, SysView* v, bool df,
+                             cudaGraphNode_t* loop_out);
+  cudaError_t build_plain_graph(bool df, bool cont = false);
   cudaError_t build_mixed_graph();
   void release();
 
@@ -130,6 +135,7 @@ class PcgSolver {
   void* st_host_ = nullptr;     // pinned staging
   const volatile int* abort_flag_ = nullptr;
   cudaGraphExec_t plain_exec_ = nullptr, mixed_exec_ = nullptr, df_exec_ = nullptr;
+  cudaGraphExec_t cont_exec_ = nullptr, cont_df_exec_ = nullptr;
   // single-kernel cooperative iterations (small and mid-size systems)
   bool use_coop_ = false;
   int coop_grid_ = 0;
@@ -195,6 +201,12 @@ cudaError_t dev_dot(const double* x, const double* y, long long n, double* out_h
 cudaError_t dev_axpy(long long n, double a, const double* x, double* y, cudaStream_t s);
 cudaError_t dev_scal(long long n, double a, double* x, cudaStream_t s);
 cudaError_t dev_mul(long long n, const double* x, double* y, cudaStream_t s);
+// Strided BLAS-1 (increments as in BLAS, negative ones walk backwards).
+cudaError_t dev_dot_s(const double* x, int incx, const double* y, int incy, long long n, double* out_host,
+                      cudaStream_t s);
+cudaError_t dev_axpy_s(long long n, double a, const double* x, int incx, double* y, int incy, cudaStream_t s);
+cudaError_t dev_scal_s(long long n, double a, double* x, int incx, cudaStream_t s);
+cudaError_t dev_copy_s(long long n, const double* x, int incx, double* y, int incy, cudaStream_t s);
 
 // Process-wide default stream of the OpenNL API (created on first use).
 cudaStream_t api_stream();

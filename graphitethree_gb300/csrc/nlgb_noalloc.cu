@@ -22,6 +22,7 @@
 #include "nlgb_internal.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -140,6 +141,22 @@ __global__ void __launch_bounds__(kCTA) na_final(SysView s) {
   }
 }
 
+// The true-residual check after na_final and the continuation it may ask
+// for (the same steps as the other executors: the pending p update, then
+// more iterations).
+__global__ void na_check(SysState* st) {
+  if (scalar_after_check(st)) st->stage = 4;
+}
+
+__global__ void __launch_bounds__(kCTA) na_resume_p(SysView s) {
+  if (!na_running(s) || __ldcg(&s.st->stage) != 4) return;
+  tile_update_p(s, blockIdx.x, __ldcg(&s.st->beta));
+}
+
+__global__ void na_resume_mark(SysState* st) {
+  if (st->stage == 4) st->stage = 1;
+}
+
 // dinv[i] = 1 / a_ii (1 when the diagonal is missing or zero).
 __global__ void na_jacobi(int n, const int* __restrict__ rp, const int* __restrict__ ci,
                           const double* __restrict__ va, double* dinv) {
@@ -189,21 +206,32 @@ cudaError_t run_pcg(const SysView& v, long long max_iter, cudaStream_t s, SysSta
   NLGB_CUDA_TRY(cudaGetLastError());
   // Host loop: 32 iterations per check of the status word.  The kernels do
   // nothing once the status leaves RUNNING, and the loop is capped by
-  // max_iter independently of the device logic.
+  // max_iter independently of the device logic.  After the final residual,
+  // a failed true-residual check continues the recurrence (at most
+  // kMaxTrueChecks times).
   constexpr int kChunk = 32;
-  const long long max_chunks = max_iter / kChunk + 2;
-  for (long long c = 0; c < max_chunks; ++c) {
-    int status = ST_RUNNING;
-    NLGB_CUDA_TRY(cudaMemcpyAsync(&status, &v.st->status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  const long long max_chunks = max_iter / kChunk + 2 + 2LL * (kMaxTrueChecks + 1);
+  long long chunks = 0;
+  for (int pass = 0; pass <= kMaxTrueChecks; ++pass) {
+    for (; chunks < max_chunks; ++chunks) {
+      int status = ST_RUNNING;
+      NLGB_CUDA_TRY(cudaMemcpyAsync(&status, &v.st->status, sizeof(int), cudaMemcpyDeviceToHost, s));
+      NLGB_CUDA_TRY(cudaStreamSynchronize(s));
+      if (status != ST_RUNNING) break;
+      NLGB_CUDA_TRY(launch_iterations<T>(v, grid, kChunk, s));
+    }
+    na_final<T><<<grid, kCTA, 0, s>>>(v);
+    na_check<<<1, 1, 0, s>>>(v.st);
+    count_launches(2);
+    NLGB_CUDA_TRY(cudaGetLastError());
+    NLGB_CUDA_TRY(cudaMemcpyAsync(h, v.st, sizeof(SysState), cudaMemcpyDeviceToHost, s));
     NLGB_CUDA_TRY(cudaStreamSynchronize(s));
-    if (status != ST_RUNNING) break;
-    NLGB_CUDA_TRY(launch_iterations<T>(v, grid, kChunk, s));
+    if (h->status != ST_RUNNING) break;
+    na_resume_p<<<grid, kCTA, 0, s>>>(v);
+    na_resume_mark<<<1, 1, 0, s>>>(v.st);
+    count_launches(2);
+    NLGB_CUDA_TRY(cudaGetLastError());
   }
-  na_final<T><<<grid, kCTA, 0, s>>>(v);
-  count_launches(1);
-  NLGB_CUDA_TRY(cudaGetLastError());
-  NLGB_CUDA_TRY(cudaMemcpyAsync(h, v.st, sizeof(SysState), cudaMemcpyDeviceToHost, s));
-  NLGB_CUDA_TRY(cudaStreamSynchronize(s));
   return cudaSuccess;
 }
 
@@ -238,9 +266,27 @@ extern "C" int nlgb_solve_noalloc(int n, const int* rp, const int* ci, const dou
     set_error("nlgb_solve_noalloc: bad tolerance");
     return NLGB_E_INVALID;
   }
+  if (n == 0) {
+    // nothing to solve (and no row pointer to read)
+    if (res) {
+      std::memset(res, 0, sizeof(*res));
+      res->status = NL_GB300_STATUS_CONVERGED;
+      res->precision = NL_GB300_PRECISION_DOUBLE;
+    }
+    return NLGB_OK;
+  }
+  const auto t_start = std::chrono::steady_clock::now();
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   double* base = nullptr;
   if (scratch_address(&base) != cudaSuccess) return NLGB_E_DEVICE;
+  auto device_error = [](const char* what, cudaError_t e) {
+    set_error(std::string("nlgb_solve_noalloc: ") + what + ": " + cudaGetErrorString(e));
+    return NLGB_E_DEVICE;
+  };
+  int dev = 0, sms = 0;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (ce != cudaSuccess) return device_error("device query", ce);
   // Carve the static array: dinv | r | p | q | partials | state | histogram.
   double* dinv = base;
   double* r = dinv + kNoAllocMaxRows;
@@ -252,18 +298,18 @@ extern "C" int nlgb_solve_noalloc(int n, const int* rp, const int* ci, const dou
 
   // Layout choice: the same autotuner as the allocating path.
   int h34[34] = {0};
-  if (cudaMemsetAsync(hist, 0, sizeof(h34), s) != cudaSuccess) return NLGB_E_DEVICE;
-  if (n > 0) {
-    na_hist<<<std::max(1, std::min(152 * 4, (n + 255) / 256)), 256, 0, s>>>(n, rp, hist);
-    count_launches(1);
-  }
+  ce = cudaMemsetAsync(hist, 0, sizeof(h34), s);
+  if (ce != cudaSuccess) return device_error("clearing the histogram", ce);
+  // four 256-thread CTAs per SM at most (grid-stride loop)
+  na_hist<<<std::max(1, std::min(4 * std::max(1, sms), (n + 255) / 256)), 256, 0, s>>>(n, rp, hist);
+  count_launches(1);
+  ce = cudaGetLastError();
+  if (ce != cudaSuccess) return device_error("histogram launch", ce);
   int nnz = 0;
-  if (cudaMemcpyAsync(h34, hist, sizeof(h34), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-      cudaMemcpyAsync(&nnz, rp + n, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-      cudaStreamSynchronize(s) != cudaSuccess) {
-    set_error(std::string("nlgb_solve_noalloc: ") + cudaGetErrorString(cudaGetLastError()));
-    return NLGB_E_DEVICE;
-  }
+  if ((ce = cudaMemcpyAsync(h34, hist, sizeof(h34), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (ce = cudaMemcpyAsync(&nnz, rp + n, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (ce = cudaStreamSynchronize(s)) != cudaSuccess)
+    return device_error("reading the row-length histogram", ce);
   const TuneChoice tc = autotune(n, nnz, h34[33], h34);
   const int tile = std::max(kNoAllocMinTile, tc.tile_rows);
   SysView v;
@@ -276,10 +322,10 @@ extern "C" int nlgb_solve_noalloc(int n, const int* rp, const int* ci, const dou
   v.b = b; v.x = x; v.r = r; v.p = pv; v.q = q;
   v.part = part;
   v.st = st;
-  if (n > 0) {
-    na_jacobi<<<(n + 255) / 256, 256, 0, s>>>(n, rp, ci, va, dinv);
-    count_launches(1);
-  }
+  na_jacobi<<<(n + 255) / 256, 256, 0, s>>>(n, rp, ci, va, dinv);
+  count_launches(1);
+  ce = cudaGetLastError();
+  if (ce != cudaSuccess) return device_error("Jacobi launch", ce);
   // Fresh state (the array keeps the previous call's contents).
   SysState h;
   std::memset(&h, 0, sizeof(h));
@@ -287,7 +333,8 @@ extern "C" int nlgb_solve_noalloc(int n, const int* rp, const int* ci, const dou
   h.thresh2 = p.eps * p.eps;
   h.max_iter = max_iter;
   h.status = ST_RUNNING;
-  if (cudaMemcpyAsync(st, &h, sizeof(h), cudaMemcpyHostToDevice, s) != cudaSuccess) return NLGB_E_DEVICE;
+  ce = cudaMemcpyAsync(st, &h, sizeof(h), cudaMemcpyHostToDevice, s);
+  if (ce != cudaSuccess) return device_error("state upload", ce);
   cudaError_t e;
   switch (v.tpr) {
     case 1: e = run_pcg<1>(v, max_iter, s, &h); break;
@@ -297,14 +344,15 @@ extern "C" int nlgb_solve_noalloc(int n, const int* rp, const int* ci, const dou
     case 16: e = run_pcg<16>(v, max_iter, s, &h); break;
     default: e = run_pcg<32>(v, max_iter, s, &h); break;
   }
-  if (e != cudaSuccess) return NLGB_E_DEVICE;
+  if (e != cudaSuccess) return NLGB_E_DEVICE;   // message set by NLGB_CUDA_TRY
   if (res) {
     res->status = h.status == ST_RUNNING ? ST_MAX_ITER : h.status;
     res->iterations = h.iter;
     res->refinement_steps = 0;
     res->rel_residual = h.bnorm2 > 0 ? std::sqrt(h.rr / h.bnorm2) : 0.0;
     res->true_rel_residual = h.bnorm2 > 0 ? std::sqrt(h.rr_true / h.bnorm2) : 0.0;
-    res->seconds = 0.0;
+    // host clock of the whole call (it returns when the solve is finished)
+    res->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
     res->algo_bytes = algo_bytes(n, nnz, h);
     res->precision = NL_GB300_PRECISION_DOUBLE;
   }

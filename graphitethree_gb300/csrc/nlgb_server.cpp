@@ -27,6 +27,8 @@
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -76,6 +78,17 @@ struct Req {
   std::vector<int> sys_done;
   std::vector<int> sys_stage;   // SysState::stage after the last epoch
   std::vector<long long> sys_iter;
+  // SRPT bookkeeping per system: residual at the first and at the previous
+  // epoch boundary, and the estimated iterations left (< 0: not estimated)
+  std::vector<double> rr_first, rr_prev, est_left;
+  std::vector<long long> it_prev;
+  double iter_cost = 0.0;            // bytes-equivalent of one iteration of one system
+  // SRPT stream executor: per system, its chunk graphs, whether a chunk is
+  // in flight, whether it runs the mixed iteration now, a pending switch to
+  // FP64, and the measured time per iteration (ms; < 0 unknown)
+  std::vector<std::unique_ptr<ViewGraph>> graphs;
+  std::vector<int> running, mixed_now, need_fallback;
+  std::vector<double> ms_per_iter;
   std::vector<nlgb_result> res;
   double t_done = 0.0;
   int status = NL_GB300_STATUS_NONE;
@@ -135,14 +148,30 @@ struct nlgb_server_s {
   long long next_id = 0;
   std::map<long long, std::unique_ptr<Req>> reqs;
   std::deque<Req*> incoming;
-  // owned by the worker thread
+  // BATCHED: future / pending belong to the admission thread, active to the
+  // worker; admitted requests pass from one to the other through `admitted`
+  // (guarded by mu).  SERIAL: one thread owns them all.
   std::vector<Req*> future, pending, active;
+  std::deque<Req*> admitted;
+  std::condition_variable cv_admit;   // wakes the admission thread
+  std::thread adm_th;
+  bool admitter_done = false;
+  long long sys_in_flight = 0;        // systems admitted or being admitted (guarded by mu)
   size_t used = 0;
   // statistics (guarded by mu)
   nlgb_server_stats st{};
   std::vector<double> latencies;
   double first_arrival = -1.0, last_done = 0.0;
+  double t_used = 0.0;           // server time of the last change of `used`
   std::string fatal;
+  int device = 0;                // the creator's current device (the worker uses it too)
+  // Abort flag in pinned, mapped host memory: the guard kernel of a graph
+  // executor polls it once per while-loop pass.
+  volatile int* abort_host = nullptr;
+  int* abort_dev = nullptr;
+  // Tracing (environment NLGB_SERVER_TRACE = path): one CSV line per epoch
+  // ("E", ...) and per admission ("A", ...), written by the worker thread.
+  FILE* trace = nullptr;
 
   double now() const { return std::chrono::duration<double>(Clock::now() - origin).count(); }
 };
@@ -165,6 +194,37 @@ int req_precision(const nlgb_server_s* S, const Req& r) {
 }
 bool req_mixed(const nlgb_server_s* S, const Req& r) {
   return req_precision(S, r) == NL_GB300_PRECISION_MIXED;
+}
+
+// Device footprint admitted by the server: every change goes through here,
+// so that the peak and the time integral stay exact.  add_used_locked: with
+// S->mu held.
+void add_used_locked(nlgb_server_s* S, long long delta) {
+  const double t = S->now();
+  S->st.byte_seconds += double(S->used) * std::max(0.0, t - S->t_used);
+  S->t_used = t;
+  if (delta < 0) S->used -= std::min<size_t>(S->used, (size_t)(-delta));
+  else S->used += (size_t)delta;
+  S->st.used_bytes = S->used;
+  S->st.peak_bytes = std::max(S->st.peak_bytes, S->used);
+}
+void add_used(nlgb_server_s* S, long long delta) {
+  std::lock_guard<std::mutex> lk(S->mu);
+  add_used_locked(S, delta);
+}
+
+// Cost of one iteration of one system of r (bytes-equivalent): its
+// algorithmic bytes, at least what a latency-bound iteration occupies (one
+// CTA slot of the persistent kernel for ~15 us, at the HBM rate shared by
+// ~608 slots: ~160 kB).
+constexpr double kServiceFloorBytes = 1.6e5;
+constexpr long long kProbeIters = 16;      // SRPT: first epoch of a new system
+constexpr int kReserveCtas = 16;           // persistent-kernel slots left to system builds
+constexpr long long kUnrollPlainIters = 4;  // a chunk pauses on whole passes of 4 iterations
+double iteration_cost(const Req& r, bool mixed) {
+  const double n = double(r.A.n), z = double(r.A.nnz);
+  const double b = mixed ? 8.0 * z + 56.0 * n : 12.0 * z + 108.0 * n;
+  return std::max(b, kServiceFloorBytes);
 }
 
 SolveParams params_of(const nlgb_server_s* S, int precision) {
@@ -240,13 +300,15 @@ bool admit(nlgb_server_s* S, Req* r, cudaStream_t s, bool df_slots) {
   if (e == cudaSuccess) {
     // true footprint now known
     const size_t actual = (size_t)device_bytes(r->A) + (size_t)r->n_rhs * SystemSlot::bytes_for(r->n, r->A.tile_rows, mixed);
-    S->used = S->used - std::min(S->used, r->bytes) + actual;
+    add_used(S, (long long)actual - (long long)r->bytes);
     r->bytes = actual;
+    r->iter_cost = iteration_cost(*r, mixed);
     r->slots.resize((size_t)r->n_rhs);
     const SolveParams prm = params_of(S, prec);
     for (int k = 0; k < r->n_rhs && e == cudaSuccess; ++k) {
       e = r->slots[k].alloc(&r->A, mixed, s, dfl && df_slots);
       if (e != cudaSuccess) break;
+      r->slots[k].view.abort_flag = S->abort_dev;
       const double* bk = r->kind == 0 ? r->b.data() + (size_t)k * r->n : r->d_rhs + (size_t)k * r->n;
       const double* xk = r->x0.empty() ? nullptr : r->x0.data() + (size_t)k * r->n;
       e = r->slots[k].start(bk, xk, prm, s);
@@ -267,6 +329,15 @@ bool admit(nlgb_server_s* S, Req* r, cudaStream_t s, bool df_slots) {
   r->sys_done.assign((size_t)r->n_rhs, 0);
   r->sys_stage.assign((size_t)r->n_rhs, 0);
   r->sys_iter.assign((size_t)r->n_rhs, 0);
+  r->rr_first.assign((size_t)r->n_rhs, 0.0);
+  r->rr_prev.assign((size_t)r->n_rhs, 0.0);
+  r->est_left.assign((size_t)r->n_rhs, -1.0);
+  r->it_prev.assign((size_t)r->n_rhs, 0);
+  r->running.assign((size_t)r->n_rhs, 0);
+  r->need_fallback.assign((size_t)r->n_rhs, 0);
+  r->ms_per_iter.assign((size_t)r->n_rhs, -1.0);
+  r->mixed_now.assign((size_t)r->n_rhs, 0);
+  for (int k = 0; k < r->n_rhs; ++k) r->mixed_now[k] = r->slots[k].mixed ? 1 : 0;
   r->res.assign((size_t)r->n_rhs, nlgb_result{});
   return true;
 }
@@ -278,10 +349,15 @@ void release(nlgb_server_s* S, Req* r, cudaStream_t s) {
   crs_free(r->A);
   cudaFree(r->d_rhs);
   r->d_rhs = nullptr;
-  S->used -= std::min(S->used, r->bytes);
+  add_used(S, -(long long)r->bytes);
+  r->bytes = 0;
 }
 
 void finish_request(nlgb_server_s* S, Req* r, bool ok) {
+  if (r->status == NL_GB300_STATUS_ABORTED) {
+    ok = false;
+    if (r->error.empty()) r->error = "aborted by nlgb_server_abort";
+  }
   std::lock_guard<std::mutex> lk(S->mu);
   r->t_done = S->now();
   r->state = ok ? R_DONE : R_FAILED;
@@ -362,71 +438,243 @@ void fail_all_waiting(nlgb_server_s* S, const char* why) {
   }
 }
 
+// Copy a finished request's solutions to the caller's buffer, release its
+// device memory and report it.
+void complete_request(nlgb_server_s* S, Req* r, cudaStream_t su) {
+  bool ok = true;
+  for (int k = 0; k < r->n_rhs; ++k) {
+    if (r->res[k].status == NL_GB300_STATUS_ABORTED) continue;   // nothing to return
+    if (r->slots[k].df && df_unpack(r->slots[k].view.x, r->n, su) != cudaSuccess) ok = false;
+    if (cudaMemcpyAsync(r->x_out + (size_t)k * r->n, r->slots[k].view.x, sizeof(double) * r->n,
+                        cudaMemcpyDeviceToHost, su) != cudaSuccess) ok = false;
+  }
+  for (int k = 0; k < r->n_rhs; ++k)
+    if (r->res[k].status != NL_GB300_STATUS_CONVERGED && r->status != NL_GB300_STATUS_ABORTED)
+      r->status = r->res[k].status;
+  cudaStreamSynchronize(su);
+  if (r->status == NL_GB300_STATUS_NONE) r->status = NL_GB300_STATUS_CONVERGED;
+  release(S, r, su);
+  finish_request(S, r, ok);
+}
+
+// Iterations a system still needs, from its residual history: the slower
+// of the average reduction rate since the start and the rate over the last
+// epoch, extrapolated to the threshold (CG's residual is not monotone; the
+// slower rate errs on the side of more work).
+double estimate_left(Req* r, int k, const SysState& h) {
+  if (h.bnorm2 <= 0.0 || h.iter <= 0) return -1.0;
+  if (r->rr_first[k] <= 0.0) r->rr_first[k] = h.bnorm2;   // zero initial guess: ||r0|| = ||b||
+  const double rr = std::max(h.rr, 1e-300);
+  const double target = std::max((h.precision == 1 ? h.thresh2 : h.rthresh2) * h.bnorm2, 1e-300);
+  const double left_max = double(std::max(1LL, h.max_iter - h.iter));
+  double rate = std::log(rr / r->rr_first[k]) / double(h.iter);
+  const long long dk = h.iter - r->it_prev[k];
+  if (r->it_prev[k] > 0 && dk >= 8 && r->rr_prev[k] > 0.0)
+    rate = std::max(rate, std::log(rr / r->rr_prev[k]) / double(dk));
+  r->it_prev[k] = h.iter;
+  r->rr_prev[k] = rr;
+  if (rr <= target) return 1.0;
+  if (!(rate < -1e-9)) return left_max;
+  return std::min(left_max, std::max(1.0, std::log(target / rr) / rate));
+}
+
+// Admission thread of the BATCHED server: arrived requests are admitted in
+// arrival order, first fit against the HBM budget, each uploaded and built
+// (or assembled) on this thread's stream while the worker's epochs run (the
+// persistent kernel leaves kReserveCtas slots for these kernels); admitted
+// requests join the next epoch.
+void admitter(nlgb_server_s* S) {
+  cudaSetDevice(S->device);
+  cudaStream_t su = nullptr;
+  cudaStreamCreateWithFlags(&su, cudaStreamNonBlocking);
+  std::unique_lock<std::mutex> lk(S->mu);
+  for (;;) {
+    while (!S->incoming.empty()) {
+      S->future.push_back(S->incoming.front());
+      S->incoming.pop_front();
+    }
+    if (S->aborting || !S->fatal.empty()) {
+      std::vector<Req*> drop(S->pending.begin(), S->pending.end());
+      drop.insert(drop.end(), S->future.begin(), S->future.end());
+      S->pending.clear();
+      S->future.clear();
+      lk.unlock();
+      for (Req* r : drop) {
+        r->error = S->fatal.empty() ? "server aborted" : S->fatal;
+        r->status = NL_GB300_STATUS_ABORTED;
+        finish_request(S, r, false);
+      }
+      lk.lock();
+      if (S->stop) break;
+      S->cv_admit.wait_for(lk, std::chrono::milliseconds(50));
+      continue;
+    }
+    const double t = S->now();
+    std::stable_sort(S->future.begin(), S->future.end(),
+                     [](const Req* a, const Req* b) { return a->arrival < b->arrival; });
+    size_t j = 0;
+    while (j < S->future.size() && S->future[j]->arrival <= t) {
+      S->future[j]->state = R_PENDING;
+      S->pending.push_back(S->future[j]);
+      ++j;
+    }
+    S->future.erase(S->future.begin(), S->future.begin() + (long)j);
+    // first fit in arrival order
+    Req* pick = nullptr;
+    for (size_t i = 0; i < S->pending.size(); ++i) {
+      Req* r = S->pending[i];
+      if (S->used + r->bytes <= S->cfg.hbm_budget_bytes && S->sys_in_flight + r->n_rhs <= S->cfg.max_systems) {
+        pick = r;
+        S->pending.erase(S->pending.begin() + (long)i);
+        break;
+      }
+    }
+    if (pick) {
+      add_used_locked(S, (long long)pick->bytes);
+      S->sys_in_flight += pick->n_rhs;
+      lk.unlock();
+      const double ta = S->now();
+      bool ok = admit(S, pick, su, true);
+      if (ok && S->cfg.schedule == NLGB_SCHEDULE_SRPT) {
+        // instantiate the chunk graphs here, off the worker's path
+        pick->graphs.resize((size_t)pick->n_rhs);
+        for (int k = 0; k < pick->n_rhs && ok; ++k) {
+          pick->graphs[k].reset(new ViewGraph());
+          ok = pick->graphs[k]->prepare(pick->slots[k].view, pick->slots[k].mixed) == cudaSuccess;
+        }
+        if (!ok) pick->error = std::string("admission failed: ") + last_error();
+      }
+      const double tb = S->now();
+      if (S->trace)
+        std::fprintf(S->trace, "A,%.6f,%lld,%d,%d,%.6f,%zu,%.6f\n", ta, pick->id,
+                     pick->kind == 2 ? pick->mesh_kind : -1, pick->n, tb - ta, pick->bytes, pick->arrival);
+      if (!ok) {
+        release(S, pick, su);
+        {
+          std::lock_guard<std::mutex> g(S->mu);
+          S->sys_in_flight -= pick->n_rhs;
+        }
+        finish_request(S, pick, false);
+      }
+      lk.lock();
+      if (ok) {
+        pick->state = R_ACTIVE;
+        S->admitted.push_back(pick);
+        S->cv_work.notify_all();
+      }
+      continue;
+    }
+    if (S->stop && S->future.empty() && S->pending.empty() && S->incoming.empty()) break;
+    // nothing admissible: wait for a submission, an arrival, freed memory or shutdown
+    double wait_s = 0.05;
+    if (!S->future.empty()) wait_s = std::min(wait_s, std::max(0.0, S->future.front()->arrival - S->now()));
+    S->cv_admit.wait_for(lk, std::chrono::duration<double>(wait_s));
+  }
+  S->admitter_done = true;
+  S->cv_work.notify_all();
+  lk.unlock();
+  cudaStreamSynchronize(su);
+  cudaStreamDestroy(su);
+}
+
 void worker_batched(nlgb_server_s* S) {
+  cudaSetDevice(S->device);
   cudaStream_t sc = nullptr, su = nullptr;
   cudaStreamCreateWithFlags(&sc, cudaStreamNonBlocking);
   cudaStreamCreateWithFlags(&su, cudaStreamNonBlocking);
   BatchRunner runner;
   if (runner.init(sc) != cudaSuccess) {
+    std::lock_guard<std::mutex> lk(S->mu);
     S->fatal = last_error();
-    fail_all_waiting(S, "server could not start on the GPU");
+    S->cv_admit.notify_all();
   }
+  const bool srpt = S->cfg.schedule == NLGB_SCHEDULE_SRPT;
+  const unsigned long long epoch_ns = S->cfg.epoch_ms > 0.0 ? (unsigned long long)(S->cfg.epoch_ms * 1e6) : 0ULL;
+  runner.set_priority_plan(srpt);
+  runner.set_epoch_ns(srpt ? epoch_ns : 0ULL);
+  runner.set_reserve(kReserveCtas);
+  if (S->trace) runner.set_timing(true);
   std::vector<SysState> states;
   std::vector<std::pair<Req*, int>> owner;   // system index -> (request, rhs)
-  int active_systems = 0;
   std::vector<std::unique_ptr<ViewGraph>> solos;   // graph executors of large systems
-  auto admit_pending = [&]() {
-    // first fit in arrival order
-    for (size_t i = 0; i < S->pending.size();) {
-      Req* r = S->pending[i];
-      if (S->aborting) break;
-      const bool fits = S->used + r->bytes <= S->cfg.hbm_budget_bytes &&
-                        active_systems + r->n_rhs <= S->cfg.max_systems;
-      if (!fits) { ++i; continue; }
-      S->used += r->bytes;
-      {
-        std::lock_guard<std::mutex> lk(S->mu);
-        S->st.peak_bytes = std::max(S->st.peak_bytes, S->used);
-      }
-      S->pending.erase(S->pending.begin() + (long)i);
-      if (admit(S, r, su, true)) {
-        r->state = R_ACTIVE;
-        S->active.push_back(r);
-        active_systems += r->n_rhs;
-        std::lock_guard<std::mutex> lk(S->mu);
-        S->st.peak_bytes = std::max(S->st.peak_bytes, S->used);
-      } else {
-        release(S, r, su);
-        finish_request(S, r, false);
-      }
+  auto finish_abort_all = [&]() {
+    for (Req* r : S->active) {
+      for (int k = 0; k < r->n_rhs; ++k)
+        if (!r->sys_done[k]) {
+          r->sys_done[k] = 1;
+          r->res[k].status = NL_GB300_STATUS_ABORTED;
+          r->res[k].iterations = r->sys_iter[k];   // as of the last epoch boundary
+        }
+      r->status = NL_GB300_STATUS_ABORTED;
+      complete_request(S, r, su);
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->sys_in_flight -= r->n_rhs;
     }
+    S->active.clear();
   };
   while (S->fatal.empty()) {
-    if (!intake(S, true)) break;
-    if (S->aborting) fail_all_waiting(S, "server aborted");
-    admit_pending();
-    if (S->active.empty()) continue;
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      while (!S->admitted.empty()) {
+        S->active.push_back(S->admitted.front());
+        S->admitted.pop_front();
+      }
+      if (S->active.empty()) {
+        if (S->admitter_done) break;
+        S->cv_work.wait_for(lk, std::chrono::milliseconds(50),
+                            [&] { return !S->admitted.empty() || S->admitter_done || S->aborting; });
+        if (!S->aborting) continue;
+      }
+    }
+    if (S->aborting) {
+      // active requests stop here (between epochs); the admission thread
+      // fails the queued ones
+      finish_abort_all();
+      S->cv_admit.notify_all();
+      std::unique_lock<std::mutex> lk(S->mu);
+      if (S->admitter_done && S->admitted.empty()) break;
+      S->cv_work.wait_for(lk, std::chrono::milliseconds(20));
+      continue;
+    }
+    // The systems of this epoch.  SRPT: every active system, in order of
+    // estimated remaining work (iterations left x bytes per iteration); a
+    // system without an estimate yet comes first with a probe budget of
+    // kProbeIters iterations; the launch is time-boxed to epoch_ms and the
+    // plan gives teams in that order.  ALL: every system, epoch_iters
+    // iterations, work-proportional teams.
+    struct Cand { Req* r; int k; double key; };
+    std::vector<Cand> cands;
+    for (Req* r : S->active)
+      for (int k = 0; k < r->n_rhs; ++k)
+        if (!r->sys_done[k])
+          cands.push_back({r, k, r->est_left[k] < 0.0 ? -1.0 : r->est_left[k] * r->iter_cost});
+    if (srpt)
+      std::stable_sort(cands.begin(), cands.end(), [](const Cand& a, const Cand& b) {
+        return a.key != b.key ? a.key < b.key : a.r->id < b.r->id;
+      });
     std::vector<SysView> views;
     std::vector<long long> work;
     owner.clear();
-    for (Req* r : S->active)
-      for (int k = 0; k < r->n_rhs; ++k) {
-        if (r->sys_done[k]) continue;
-        views.push_back(r->slots[k].view);
-        work.push_back((r->A.nnz + 8LL * r->A.n));
-        owner.push_back({r, k});
-      }
+    for (const Cand& c : cands) {
+      SysView v = c.r->slots[c.k].view;
+      v.budget = srpt ? (c.key < 0.0 ? kProbeIters : (epoch_ns ? 0 : S->cfg.epoch_iters)) : S->cfg.epoch_iters;
+      views.push_back(v);
+      work.push_back((long long)std::min(9.0e18, c.r->iter_cost * double(S->cfg.epoch_iters)));
+      owner.push_back({c.r, c.k});
+    }
     BatchLaunchStats bst;
-    // When every active system is a large FP64 one (at most kMaxGraphSystems,
-    // everything small finished), each continues on its own graph executor,
-    // one after the other in the epoch: faster per iteration than sharing the
+    const double t_epoch0 = S->now();
+    // When the epoch's systems are all large FP64 ones (at most
+    // kMaxGraphSystems), each continues on its own graph executor, one after
+    // the other in the epoch: faster per iteration than sharing the
     // persistent kernel once each fills the GPU alone (same iterates, see
     // ViewGraph).
-    bool graph_epoch = !views.empty() && views.size() <= kMaxGraphSystems && !S->aborting;
+    bool graph_epoch = !views.empty() && views.size() <= kMaxGraphSystems;
     for (size_t i = 0; graph_epoch && i < views.size(); ++i) {
       const Req* r = owner[i].first;
       const int k = owner[i].second;
-      graph_epoch = !req_mixed(S, *r) && views[i].n_tiles >= kGraphMinTiles && r->sys_stage[k] == 1;
+      graph_epoch = !req_mixed(S, *r) && views[i].n_tiles >= kGraphMinTiles && r->sys_stage[k] == 1 &&
+                    r->est_left[k] >= 0.0;
     }
     cudaError_t e = cudaSuccess;
     if (graph_epoch) {
@@ -435,11 +683,15 @@ void worker_batched(nlgb_server_s* S) {
       std::vector<long long> before(views.size());
       for (size_t i = 0; i < views.size() && e == cudaSuccess; ++i) {
         before[i] = owner[i].first->sys_iter[owner[i].second];
-        e = solos[i]->run(views[i], S->cfg.epoch_iters, sc, &gms[i]);
+        // a chunk of about epoch_ms at ~2.8 TB/s, in whole passes of 4
+        long long it = S->cfg.epoch_iters;
+        if (srpt && epoch_ns) {
+          const double per = owner[i].first->iter_cost / 2.8e12;
+          it = std::max<long long>(16, std::min<long long>(4096, (long long)(double(epoch_ns) * 1e-9 / per)));
+        }
+        e = solos[i]->run(views[i], it, sc, &gms[i]);
       }
       if (e == cudaSuccess) {
-        intake(S, false);
-        admit_pending();
         states.resize(views.size());
         for (size_t i = 0; i < views.size() && e == cudaSuccess; ++i)
           e = cudaMemcpyAsync(&states[i], views[i].st, sizeof(SysState), cudaMemcpyDeviceToHost, sc);
@@ -460,73 +712,348 @@ void worker_batched(nlgb_server_s* S) {
         S->st.graph_algo_bytes += bytes;
       }
     } else {
-      e = runner.launch(views, work, S->aborting ? 1 : S->cfg.epoch_iters);
-      if (e == cudaSuccess) {
-        // overlap: admit what arrived meanwhile while the epoch runs
-        intake(S, false);
-        admit_pending();
-        e = runner.finish(&bst);
-      }
+      e = runner.launch(views, work, srpt && epoch_ns ? 0 : S->cfg.epoch_iters);
+      if (e == cudaSuccess) e = runner.finish(&bst);
       if (e == cudaSuccess) {
         states.resize(views.size());
         e = runner.gather_states(states.data(), (int)views.size());
       }
     }
     if (e != cudaSuccess) {
+      std::lock_guard<std::mutex> lk(S->mu);
       S->fatal = last_error();
+      S->cv_admit.notify_all();
       break;
+    }
+    double done_bytes = 0.0, done_algo = 0.0;
+    for (size_t i = 0; i < views.size(); ++i) {
+      const Req* r = owner[i].first;
+      const long long di = states[i].iter - r->sys_iter[owner[i].second];
+      done_bytes += double(di) * r->iter_cost;
+      done_algo += double(di) * (r->slots[owner[i].second].mixed ? 8.0 * double(r->A.nnz) + 56.0 * double(r->A.n)
+                                                                  : 12.0 * double(r->A.nnz) + 108.0 * double(r->A.n));
     }
     {
       std::lock_guard<std::mutex> lk(S->mu);
       S->st.kernel_s += bst.ms * 1e-3;
       S->st.epochs += 1;
+      S->st.epoch_algo_bytes += done_algo;
+    }
+    if (S->trace) {
+      double tmin = 0.0, tmed = 0.0, tmax = 0.0, tq = 0.0;
+      const std::vector<unsigned long long>& tt = runner.last_times();
+      if (!graph_epoch && tt.size() >= 2 && tt[0] > 0) {
+        std::vector<double> te;
+        for (size_t t = 2; t < tt.size(); ++t)
+          if (tt[t] > 0) te.push_back(1e-6 * double(tt[t] - tt[0]));
+        std::sort(te.begin(), te.end());
+        if (!te.empty()) { tmin = te.front(); tmed = te[te.size() / 2]; tmax = te.back(); }
+        if (tt[1] > 0) tq = 1e-6 * double(tt[1] - tt[0]);
+      }
+      std::fprintf(S->trace, "E,%.6f,%.6f,%s,%zu,%d,%d,%d,%d,%.3f,%.3f,%.3f,%.3f,%.3f,%.3f,%.3f,%d,%.6f,%zu\n",
+                   t_epoch0, S->now(), graph_epoch ? "graph" : "batch", views.size(), bst.n_teams, bst.team_ctas,
+                   bst.queue_ctas, bst.grid, done_algo * 1e-9, done_bytes * 1e-9, bst.ms, tmin, tmed, tmax, tq,
+                   0, 0.0, S->active.size());
     }
     for (size_t i = 0; i < views.size(); ++i) {
       Req* r = owner[i].first;
       const int k = owner[i].second;
+      r->est_left[k] = estimate_left(r, k, states[i]);
       r->sys_stage[k] = states[i].stage;
       r->sys_iter[k] = states[i].iter;
-      if (states[i].stage == 3 || S->aborting) {
-        SysState h = states[i];
-        if (h.stage != 3) h.status = ST_ABORTED;
+      if (states[i].stage == 3) {
         r->sys_done[k] = 1;
-        fill_result(r->res[k], h, bst.ms * 1e-3, r->A.n, r->A.nnz,
+        fill_result(r->res[k], states[i], bst.ms * 1e-3, r->A.n, r->A.nnz,
                     r->slots[k].mixed ? NL_GB300_PRECISION_MIXED
                                       : (r->slots[k].df ? NL_GB300_PRECISION_DOUBLE_FLOAT
                                                         : NL_GB300_PRECISION_DOUBLE));
       }
     }
+    bool freed = false;
     for (size_t i = 0; i < S->active.size();) {
       Req* r = S->active[i];
       bool all = true;
       for (int d : r->sys_done) all = all && d;
       if (!all) { ++i; continue; }
-      bool ok = true;
-      for (int k = 0; k < r->n_rhs; ++k) {
-        if (r->slots[k].df && df_unpack(r->slots[k].view.x, r->n, su) != cudaSuccess) ok = false;
-        if (cudaMemcpyAsync(r->x_out + (size_t)k * r->n, r->slots[k].view.x, sizeof(double) * r->n,
-                            cudaMemcpyDeviceToHost, su) != cudaSuccess) ok = false;
-        if (r->res[k].status != NL_GB300_STATUS_CONVERGED) r->status = r->res[k].status;
-      }
-      cudaStreamSynchronize(su);
-      if (r->status == NL_GB300_STATUS_NONE) r->status = NL_GB300_STATUS_CONVERGED;
-      release(S, r, su);
-      active_systems -= r->n_rhs;
       S->active.erase(S->active.begin() + (long)i);
-      finish_request(S, r, ok);
+      complete_request(S, r, su);
+      {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->sys_in_flight -= r->n_rhs;
+      }
+      freed = true;
     }
+    if (freed) S->cv_admit.notify_all();
   }
   if (!S->fatal.empty()) {
-    for (Req* r : S->active) { r->error = S->fatal; finish_request(S, r, false); }
+    for (Req* r : S->active) { r->error = S->fatal; release(S, r, su); finish_request(S, r, false); }
     S->active.clear();
-    fail_all_waiting(S, S->fatal.c_str());
+    std::unique_lock<std::mutex> lk(S->mu);
+    S->cv_admit.notify_all();
+    // requests the admission thread hands over from now on fail too
+    while (!S->admitter_done || !S->admitted.empty()) {
+      while (!S->admitted.empty()) {
+        Req* r = S->admitted.front();
+        S->admitted.pop_front();
+        lk.unlock();
+        r->error = S->fatal;
+        release(S, r, su);
+        finish_request(S, r, false);
+        lk.lock();
+      }
+      if (!S->admitter_done) S->cv_work.wait_for(lk, std::chrono::milliseconds(20));
+    }
   }
   cudaStreamSynchronize(sc);
   cudaStreamDestroy(sc);
   cudaStreamDestroy(su);
 }
 
+// SRPT executor of the BATCHED server: `streams` CUDA streams, each running
+// one system at a time as a chunk of CUDA-graph iterations (ViewGraph) of
+// about epoch_ms.  Whenever a stream is free it takes the system with the
+// least estimated remaining work that is not running already (a new system
+// first, for a probe of kProbeIters iterations).  A system's chunks run one
+// after the other (the next one is queued only after the previous one was
+// seen to finish), so its iterates are those of the single-system solver.
+void worker_streams(nlgb_server_s* S) {
+  cudaSetDevice(S->device);
+  const int ns = std::max(1, S->cfg.streams > 0 ? S->cfg.streams : 16);
+  struct Lane {
+    cudaStream_t s = nullptr;
+    SysState* h = nullptr;      // pinned copy of the system's state after the chunk
+    Req* r = nullptr;
+    int k = -1;
+    long long iter_before = 0;
+    float ms = 0.f;
+  };
+  std::vector<Lane> lanes((size_t)ns);
+  cudaStream_t su = nullptr;
+  cudaStreamCreateWithFlags(&su, cudaStreamNonBlocking);
+  bool init_ok = true;
+  for (Lane& l : lanes)
+    init_ok = init_ok && cudaStreamCreateWithFlags(&l.s, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaMallocHost(&l.h, sizeof(SysState)) == cudaSuccess;
+  if (!init_ok) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->fatal = std::string("server streams: ") + cudaGetErrorString(cudaGetLastError());
+    S->cv_admit.notify_all();
+  }
+  const double target_ms = S->cfg.epoch_ms > 0.0 ? S->cfg.epoch_ms : 10.0;
+  int n_busy = 0;
+  double t_busy0 = 0.0;
+  auto busy_change = [&](int delta) {
+    const double t = S->now();
+    if (n_busy > 0 && delta != 0) {
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->st.kernel_s += t - t_busy0;
+    }
+    t_busy0 = t;
+    n_busy += delta;
+  };
+  auto finish_abort_all = [&]() {
+    for (Req* r : S->active) {
+      for (int k = 0; k < r->n_rhs; ++k)
+        if (!r->sys_done[k]) {
+          r->sys_done[k] = 1;
+          r->res[k].status = NL_GB300_STATUS_ABORTED;
+          r->res[k].iterations = r->sys_iter[k];
+        }
+      r->status = NL_GB300_STATUS_ABORTED;
+      complete_request(S, r, su);
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->sys_in_flight -= r->n_rhs;
+    }
+    S->active.clear();
+  };
+  // one finished chunk: results, estimates, completion
+  auto retire = [&](Lane& l) -> cudaError_t {
+    Req* r = l.r;
+    const int k = l.k;
+    const SysState h = *l.h;
+    cudaError_t e = r->graphs[k]->finish(l.iter_before, h.iter);
+    const long long di = h.iter - l.iter_before;
+    const bool mixed_chunk = r->mixed_now[k] != 0;
+    const double bytes_it = mixed_chunk ? 8.0 * double(r->A.nnz) + 56.0 * double(r->A.n)
+                                        : 12.0 * double(r->A.nnz) + 108.0 * double(r->A.n);
+    {
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->st.epochs += 1;
+      S->st.graph_epochs += 1;
+      S->st.graph_s += l.ms * 1e-3;
+      S->st.epoch_algo_bytes += double(di) * bytes_it;
+      if (!mixed_chunk) S->st.graph_algo_bytes += double(di) * bytes_it;
+    }
+    if (S->trace)
+      std::fprintf(S->trace, "C,%.6f,%lld,%d,%d,%lld,%lld,%.3f,%d,%d\n", S->now(), r->id, k, mixed_chunk ? 1 : 0,
+                   l.iter_before, h.iter, l.ms, h.status, h.stage);
+    if (di > 0) r->ms_per_iter[k] = double(l.ms) / double(di);
+    r->est_left[k] = estimate_left(r, k, h);
+    r->sys_stage[k] = h.stage;
+    r->sys_iter[k] = h.iter;
+    r->running[k] = 0;
+    if (mixed_chunk && h.status == ST_STAGNATION && !h.fell_back && h.precision == 1) {
+      // FP32 cannot track this system: it continues in FP64 from its x
+      r->need_fallback[k] = 1;
+      r->mixed_now[k] = 0;
+      r->sys_stage[k] = 0;
+    } else if (h.stage == 3) {
+      r->sys_done[k] = 1;
+      fill_result(r->res[k], h, l.ms * 1e-3, r->A.n, r->A.nnz,
+                  r->slots[k].mixed ? NL_GB300_PRECISION_MIXED
+                                    : (r->slots[k].df ? NL_GB300_PRECISION_DOUBLE_FLOAT
+                                                      : NL_GB300_PRECISION_DOUBLE));
+    }
+    l.r = nullptr;
+    l.k = -1;
+    busy_change(-1);
+    return e;
+  };
+  auto complete_finished = [&]() {
+    bool freed = false;
+    for (size_t i = 0; i < S->active.size();) {
+      Req* r = S->active[i];
+      bool all = true;
+      for (int k = 0; k < r->n_rhs; ++k) all = all && r->sys_done[k] && !r->running[k];
+      if (!all) { ++i; continue; }
+      S->active.erase(S->active.begin() + (long)i);
+      complete_request(S, r, su);
+      {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->sys_in_flight -= r->n_rhs;
+      }
+      freed = true;
+    }
+    if (freed) S->cv_admit.notify_all();
+  };
+  while (S->fatal.empty()) {
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      while (!S->admitted.empty()) {
+        S->active.push_back(S->admitted.front());
+        S->admitted.pop_front();
+      }
+      if (S->active.empty() && n_busy == 0) {
+        if (S->admitter_done) break;
+        S->cv_work.wait_for(lk, std::chrono::milliseconds(50),
+                            [&] { return !S->admitted.empty() || S->admitter_done || S->aborting; });
+        if (!S->aborting) continue;
+      }
+    }
+    // retire finished chunks
+    cudaError_t e = cudaSuccess;
+    bool progress = false;
+    for (Lane& l : lanes) {
+      if (!l.r) continue;
+      const cudaError_t q = cudaStreamQuery(l.s);
+      if (q == cudaErrorNotReady) continue;
+      if (q != cudaSuccess) { e = q; set_error(std::string("server chunk: ") + cudaGetErrorString(q)); break; }
+      e = retire(l);
+      if (e != cudaSuccess) break;
+      progress = true;
+    }
+    if (e != cudaSuccess) {
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->fatal = last_error();
+      S->cv_admit.notify_all();
+      break;
+    }
+    complete_finished();
+    if (S->aborting) {
+      // running chunks see the abort flag within one loop pass; when they
+      // are all back, the active requests end as aborted
+      if (n_busy == 0) {
+        finish_abort_all();
+        S->cv_admit.notify_all();
+        std::unique_lock<std::mutex> lk(S->mu);
+        if (S->admitter_done && S->admitted.empty()) break;
+        S->cv_work.wait_for(lk, std::chrono::milliseconds(20));
+      } else {
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+      }
+      continue;
+    }
+    // give every free lane the least-work system that is not running
+    for (Lane& l : lanes) {
+      if (l.r) continue;
+      Req* best = nullptr;
+      int bk = -1;
+      double bkey = 0.0;
+      for (Req* r : S->active)
+        for (int k = 0; k < r->n_rhs; ++k) {
+          if (r->sys_done[k] || r->running[k]) continue;
+          const double key = r->est_left[k] < 0.0 ? -1.0 : r->est_left[k] * r->iter_cost;
+          if (!best || key < bkey || (key == bkey && r->id < best->id)) { best = r; bk = k; bkey = key; }
+        }
+      if (!best) break;
+      long long iters = kProbeIters;
+      if (best->est_left[bk] >= 0.0) {
+        const double mpi = best->ms_per_iter[bk] > 0.0 ? best->ms_per_iter[bk] : best->iter_cost / 2e8;
+        iters = (long long)std::ceil(target_ms / std::max(1e-4, mpi));
+        iters = std::max<long long>(kProbeIters, std::min<long long>(iters, 1LL << 22));
+      }
+      iters = (iters + kUnrollPlainIters - 1) / kUnrollPlainIters * kUnrollPlainIters;
+      if (best->need_fallback[bk]) {
+        e = chunk_fallback_fp64(best->slots[bk].view.st, l.s);
+        best->need_fallback[bk] = 0;
+      }
+      l.r = best;
+      l.k = bk;
+      l.iter_before = best->sys_iter[bk];
+      l.ms = 0.f;
+      best->running[bk] = 1;
+      if (e == cudaSuccess)
+        e = best->graphs[bk]->run(best->slots[bk].view, iters, l.s, &l.ms, best->mixed_now[bk] != 0);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(l.h, best->slots[bk].view.st, sizeof(SysState), cudaMemcpyDeviceToHost, l.s);
+      busy_change(+1);
+      progress = true;
+      if (e != cudaSuccess) break;
+    }
+    if (e != cudaSuccess) {
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->fatal = last_error();
+      S->cv_admit.notify_all();
+      break;
+    }
+    if (!progress) {
+      if (n_busy > 0) {
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
+      } else {
+        std::unique_lock<std::mutex> lk(S->mu);
+        S->cv_work.wait_for(lk, std::chrono::milliseconds(20),
+                            [&] { return !S->admitted.empty() || S->admitter_done || S->aborting; });
+      }
+    }
+  }
+  for (Lane& l : lanes) if (l.s) cudaStreamSynchronize(l.s);
+  if (!S->fatal.empty()) {
+    for (Req* r : S->active) { r->error = S->fatal; release(S, r, su); finish_request(S, r, false); }
+    S->active.clear();
+    std::unique_lock<std::mutex> lk(S->mu);
+    S->cv_admit.notify_all();
+    while (!S->admitter_done || !S->admitted.empty()) {
+      while (!S->admitted.empty()) {
+        Req* r = S->admitted.front();
+        S->admitted.pop_front();
+        lk.unlock();
+        r->error = S->fatal;
+        release(S, r, su);
+        finish_request(S, r, false);
+        lk.lock();
+      }
+      if (!S->admitter_done) S->cv_work.wait_for(lk, std::chrono::milliseconds(20));
+    }
+  }
+  for (Lane& l : lanes) {
+    if (l.h) cudaFreeHost(l.h);
+    if (l.s) cudaStreamDestroy(l.s);
+  }
+  cudaStreamDestroy(su);
+}
+
 void worker_serial(nlgb_server_s* S) {
+  cudaSetDevice(S->device);
   cudaStream_t s = nullptr;
   cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
   while (true) {
@@ -536,18 +1063,16 @@ void worker_serial(nlgb_server_s* S) {
     Req* r = S->pending.front();
     S->pending.erase(S->pending.begin());
     r->bytes = estimate_bytes(*r, req_precision(S, *r));
-    S->used += r->bytes;
-    {
-      std::lock_guard<std::mutex> lk(S->mu);
-      S->st.peak_bytes = std::max(S->st.peak_bytes, S->used);
-    }
+    add_used(S, (long long)r->bytes);
     // Reuse the admission upload/assembly, then solve each right-hand side
-    // with the graph-captured single-system solver.
+    // with the graph-captured single-system solver (which polls the abort
+    // flag once per while-loop pass).
     bool ok = admit(S, r, s, false);
     const SolveParams prm = params_of(S, req_precision(S, *r));
     if (ok) {
       PcgSolver pcg;
       ok = pcg.bind(&r->A, s) == cudaSuccess;
+      pcg.set_abort_flag(S->abort_dev);
       for (int k = 0; ok && k < r->n_rhs; ++k) {
         SolveResult sr;
         const SysView& v = r->slots[k].view;
@@ -564,6 +1089,7 @@ void worker_serial(nlgb_server_s* S) {
         if (sr.status != NL_GB300_STATUS_CONVERGED) r->status = sr.status;
         std::lock_guard<std::mutex> lk(S->mu);
         S->st.kernel_s += sr.seconds;
+        if (r->status == NL_GB300_STATUS_ABORTED) break;
       }
       if (r->status == NL_GB300_STATUS_NONE) r->status = NL_GB300_STATUS_CONVERGED;
     }
@@ -594,6 +1120,7 @@ long long enqueue(nlgb_server_s* S, std::unique_ptr<Req> r) {
   S->reqs[id] = std::move(r);
   S->incoming.push_back(raw);
   S->cv_work.notify_all();
+  S->cv_admit.notify_all();
   return id;
 }
 
@@ -611,6 +1138,9 @@ void nlgb_server_default_config(nlgb_server_config* c) {
   c->inner_eps = 0.1;
   c->epoch_iters = 256;
   c->max_systems = 8192;
+  c->schedule = NLGB_SCHEDULE_SRPT;
+  c->epoch_ms = 10.0;
+  c->streams = 16;
 }
 
 nlgb_server nlgb_server_create(const nlgb_server_config* cfg) {
@@ -625,6 +1155,14 @@ nlgb_server nlgb_server_create(const nlgb_server_config* cfg) {
   if (cfg) S->cfg = *cfg;
   if (S->cfg.epoch_iters <= 0) S->cfg.epoch_iters = 256;
   if (S->cfg.max_systems <= 0) S->cfg.max_systems = 8192;
+  if (!(S->cfg.epoch_ms >= 0.0)) S->cfg.epoch_ms = 10.0;
+  if (S->cfg.streams <= 0) S->cfg.streams = 16;
+  S->cfg.streams = std::min(S->cfg.streams, 128);
+  if (S->cfg.schedule != NLGB_SCHEDULE_SRPT && S->cfg.schedule != NLGB_SCHEDULE_ALL) {
+    set_error("nlgb_server_create: unknown schedule");
+    delete S;
+    return nullptr;
+  }
   if (S->cfg.precision != NL_GB300_PRECISION_MIXED && S->cfg.precision != NL_GB300_PRECISION_DOUBLE &&
       S->cfg.precision != NL_GB300_PRECISION_AUTO && S->cfg.precision != NL_GB300_PRECISION_DOUBLE_FLOAT) {
     set_error("nlgb_server_create: unknown precision");
@@ -632,8 +1170,31 @@ nlgb_server nlgb_server_create(const nlgb_server_config* cfg) {
     return nullptr;
   }
   S->st.budget_bytes = S->cfg.hbm_budget_bytes;
+  cudaGetDevice(&S->device);
+  void* flag = nullptr;
+  if (cudaHostAlloc(&flag, sizeof(int), cudaHostAllocMapped) != cudaSuccess ||
+      cudaHostGetDevicePointer((void**)&S->abort_dev, flag, 0) != cudaSuccess) {
+    set_error(std::string("nlgb_server_create: abort flag: ") + cudaGetErrorString(cudaGetLastError()));
+    if (flag) cudaFreeHost(flag);
+    delete S;
+    return nullptr;
+  }
+  S->abort_host = static_cast<volatile int*>(flag);
+  *S->abort_host = 0;
+  if (const char* tp = std::getenv("NLGB_SERVER_TRACE")) {
+    S->trace = std::fopen(tp, "a");
+    if (S->trace)
+      std::fprintf(S->trace, "# E,t0,t1,kind,systems,teams,team_ctas,queue_ctas,grid,planned_GB,done_GB,ms,"
+                             "team_ms_min,team_ms_med,team_ms_max,queue_ms,admits,admit_s,active_requests\n"
+                             "# C,t,request,rhs,mixed,iter_before,iter_after,ms,status,stage\n"
+                             "# A,t,request,mesh_kind,n,seconds,bytes,arrival\n");
+  }
   S->origin = Clock::now();
-  S->th = std::thread(S->cfg.mode == NLGB_SERVER_SERIAL ? worker_serial : worker_batched, S);
+  S->th = std::thread(S->cfg.mode == NLGB_SERVER_SERIAL
+                          ? worker_serial
+                          : (S->cfg.schedule == NLGB_SCHEDULE_SRPT ? worker_streams : worker_batched),
+                      S);
+  if (S->cfg.mode != NLGB_SERVER_SERIAL) S->adm_th = std::thread(admitter, S);
   return S;
 }
 
@@ -641,6 +1202,8 @@ void nlgb_server_reset_clock(nlgb_server S) {
   if (!S) return;
   std::lock_guard<std::mutex> lk(S->mu);
   S->origin = Clock::now();
+  S->t_used = 0.0;
+  S->st.byte_seconds = 0.0;
 }
 
 double nlgb_server_now(nlgb_server S) { return S ? S->now() : 0.0; }
@@ -787,6 +1350,7 @@ int nlgb_server_get_stats(nlgb_server S, nlgb_server_stats* out) {
   if (!S || !out) return NLGB_E_INVALID;
   std::lock_guard<std::mutex> lk(S->mu);
   nlgb_server_stats st = S->st;
+  st.byte_seconds += double(S->used) * std::max(0.0, S->now() - S->t_used);
   st.p50_latency_s = percentile(S->latencies, 0.50);
   st.p99_latency_s = percentile(S->latencies, 0.99);
   double sum = 0.0, mx = 0.0;
@@ -803,7 +1367,9 @@ void nlgb_server_abort(nlgb_server S) {
   if (!S) return;
   std::lock_guard<std::mutex> lk(S->mu);
   S->aborting = true;
+  if (S->abort_host) *S->abort_host = 1;
   S->cv_work.notify_all();
+  S->cv_admit.notify_all();
 }
 
 void nlgb_server_destroy(nlgb_server S) {
@@ -814,8 +1380,12 @@ void nlgb_server_destroy(nlgb_server S) {
     S->stop = true;
     S->aborting = true;
     S->cv_work.notify_all();
+    S->cv_admit.notify_all();
   }
   if (S->th.joinable()) S->th.join();
+  if (S->adm_th.joinable()) S->adm_th.join();
+  if (S->abort_host) cudaFreeHost(const_cast<int*>(S->abort_host));
+  if (S->trace) std::fclose(S->trace);
   delete S;
 }
 

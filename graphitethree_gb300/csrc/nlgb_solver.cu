@@ -44,6 +44,77 @@ __device__ __forceinline__ bool publish_elect(const SysView& s, int tile, const 
   return am_last != 0;
 }
 
+// ---------------------------------------------------------------------------
+// Two-level last-CTA election with the canonical reduction.  The canonical
+// order (canon_reduce) sums tile t into thread (t mod 256)'s running sum,
+// then each warp's 32 running sums by a butterfly, then the 8 warp totals in
+// order.  Here the tiles of warp g's running sums -- those with (t mod 256)
+// / 32 == g -- form group g: the CTAs of a group arrive on the group's
+// counter, the last one computes the group's warp total (one warp, the same
+// loads, adds and butterfly), and the last of the groups adds the 8 totals
+// in order.  Same result bit for bit as one CTA reducing every partial, but
+// the partials are read by eight CTAs in parallel as their groups complete,
+// and no counter takes more than 1/8 of the arrivals.  Each CTA covers vec
+// consecutive tiles starting at tile0 (vec divides 32, so they lie in one
+// group).  Returns true in every thread of the CTA that finishes; thread 0
+// then holds the K sums in out.
+// ---------------------------------------------------------------------------
+template <int K>
+__device__ __forceinline__ bool elect2(const SysView& s, int tile0, int vec, int slot, int phase,
+                                       double (&out)[K]) {
+  __shared__ int flag;
+  SysState* st = s.st;
+  const int g = (tile0 & 255) >> 5;
+  const int ngroups = min(8, (s.n_tiles + 31) >> 5);
+  if (threadIdx.x == 0) {
+    const int per_grp = 32 / vec, per_cyc = 256 / vec;
+    const int G = (int)gridDim.x;
+    const int size = (G / per_cyc) * per_grp + min(max(G % per_cyc - g * per_grp, 0), per_grp);
+    __threadfence();
+    const unsigned int prev = atomicAdd(&st->gcnt[phase][g], 1u);
+    flag = (prev == (unsigned int)size - 1u);
+    if (flag) st->gcnt[phase][g] = 0u;   // next use is in a later kernel
+  }
+  __syncthreads();
+  if (!flag) return false;
+  __threadfence();
+  if (threadIdx.x < 32) {
+    double v[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = 0.0;
+#pragma unroll 8
+    for (int t = (g << 5) + (int)threadIdx.x; t < s.n_tiles; t += kCTA) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) v[k] += __ldcg(s.part + (size_t)t * kParts + slot + k);
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) __stcg(&st->wsum[phase][g][k], v[k]);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned int prev = atomicAdd(&st->tcnt[phase], 1u);
+    flag = (prev == (unsigned int)ngroups - 1u);
+    if (flag) st->tcnt[phase] = 0u;
+  }
+  __syncthreads();
+  if (!flag) return false;
+  __threadfence();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      double sum = 0.0;
+      for (int w = 0; w < 8; ++w) sum += (w < ngroups) ? __ldcg(&st->wsum[phase][w][k]) : 0.0;
+      out[k] = sum;
+    }
+  }
+  return true;
+}
+
 __device__ __forceinline__ int ld_status(const SysState* st) { return __ldcg(&st->status); }
 __device__ __forceinline__ int ld_mode(const SysState* st) { return __ldcg(&st->mode); }
 
@@ -69,12 +140,9 @@ template <int T, bool D>
 __global__ void __launch_bounds__(kCTA, 8) k_spmv_pq(SysView s) {
   if (ld_status(s.st) != ST_RUNNING) return;
   double v[1] = {phase_spmv_pq<D, T>(s, blockIdx.x)};
-  if (publish_elect<1>(s, blockIdx.x, v, kSlotPQ, &s.st->cnt[1])) {
-    const int comp[1] = {kSlotPQ};
-    double o[1];
-    canon_reduce<1>(s.part, s.n_tiles, comp, o);
-    if (threadIdx.x == 0) scalar_after_pq(s.st, o[0]);
-  }
+  if (threadIdx.x == 0) __stcg(s.part + (size_t)blockIdx.x * kParts + kSlotPQ, v[0]);
+  double o[1];
+  if (elect2<1>(s, blockIdx.x, 1, kSlotPQ, 0, o) && threadIdx.x == 0) scalar_after_pq(s.st, o[0]);
 }
 
 // Vector phases: each CTA handles vec_tiles_for(tile_rows) consecutive tiles
@@ -116,12 +184,9 @@ __global__ void __launch_bounds__(kCTA) k_update_xr(SysView s) {
     phase_update_xr<D>(s, t, alpha, v);
     store_parts<2>(s, t, v, kSlotXR);
   }
-  if (elect_last(&s.st->cnt[2])) {
-    const int comp[2] = {kSlotXR, kSlotXR + 1};
-    double o[2];
-    canon_reduce<2>(s.part, s.n_tiles, comp, o);
-    if (threadIdx.x == 0) scalar_after_xr(s.st, o[0], o[1]);
-  }
+  double o[2];
+  if (elect2<2>(s, vec_t0(s), vec_tiles_for(s.tile_rows), kSlotXR, 1, o) && threadIdx.x == 0)
+    scalar_after_xr(s.st, o[0], o[1]);
 }
 
 template <bool D>
@@ -256,9 +321,30 @@ __global__ void k_chunk_start(SysState* st, long long iters, int unroll) {
 }
 
 // After a chunk: a system that stopped (converged or failed) is done; its
-// true residual was computed by the final kernel of the graph.
+// true residual was computed by the final kernel of the graph.  A system
+// whose true-residual check asked for more iterations keeps stage 4.
 __global__ void k_chunk_end(SysState* st) {
   if (st->status != ST_RUNNING) st->stage = 3;
+}
+
+// After the final residual: the true-residual check (single thread).  A
+// continuation sets the status back to running and stage 4.
+__global__ void k_check(SysState* st) {
+  if (scalar_after_check(st)) st->stage = 4;
+}
+
+// Start of a continuation (stage 4): the p update the stopped iteration did
+// not do, p = D^-1 r + beta p (vector-phase grid); no-op otherwise.
+template <bool D>
+__global__ void __launch_bounds__(kCTA) k_resume_p(SysView s) {
+  if (ld_status(s.st) != ST_RUNNING || __ldcg(&s.st->stage) != 4) return;
+  const double beta = __ldcg(&s.st->beta);
+  for (int t = vec_t0(s), t1 = vec_t1(s); t < t1; ++t) phase_update_p<D>(s, t, beta);
+}
+
+// After k_resume_p: iterating again (single thread).
+__global__ void k_resume_mark(SysState* st) {
+  if (st->stage == 4) st->stage = 1;
 }
 
 // ||b - A x||^2 of the final iterate; zeroes x when b == 0.
@@ -276,6 +362,64 @@ __global__ void __launch_bounds__(kCTA) k_final(SysView s) {
     canon_reduce<1>(s.part, s.n_tiles, comp, o);
     if (threadIdx.x == 0) s.st->rr_true = o[0];
   }
+}
+
+// Chunk forms (resumable executor, ViewGraph): the initial residual only for
+// a fresh system (stage 0; the last CTA moves it to stage 1, or 2 when no
+// iteration is needed), and the final residual only for a system that
+// stopped (a paused chunk leaves it running).  Every CTA reads stage /
+// status before it arrives on the election, so all of them take the same
+// branch.
+template <int T, bool D>
+__global__ void __launch_bounds__(kCTA) k_init_chunk(SysView s) {
+  if (__ldcg(&s.st->stage) != 0 || ld_status(s.st) != ST_RUNNING) return;
+  double v[3];
+  phase_residual<D, T>(s, blockIdx.x, v);
+  if (publish_elect<3>(s, blockIdx.x, v, kSlotInit, &s.st->cnt[0])) {
+    const int comp[3] = {kSlotInit, kSlotInit + 1, kSlotInit + 2};
+    double o[3];
+    canon_reduce<3>(s.part, s.n_tiles, comp, o);
+    if (threadIdx.x == 0) {
+      scalar_after_init(s.st, o[0], o[1], o[2]);
+      s.st->stage = s.st->status == ST_RUNNING ? 1 : 2;
+    }
+  }
+}
+
+template <int T, bool D>
+__global__ void __launch_bounds__(kCTA) k_final_if(SysView s) {
+  if (ld_status(s.st) == ST_RUNNING) return;
+  double v[1] = {0.0};
+  if (__ldcg(&s.st->zero_rhs)) {
+    tile_zero_x(s, blockIdx.x);
+  } else {
+    v[0] = phase_true_rr<D, T>(s, blockIdx.x);
+  }
+  if (publish_elect<1>(s, blockIdx.x, v, kSlotFinal, &s.st->cnt[3])) {
+    const int comp[1] = {kSlotFinal};
+    double o[1];
+    canon_reduce<1>(s.part, s.n_tiles, comp, o);
+    if (threadIdx.x == 0) s.st->rr_true = o[0];
+  }
+}
+
+// Mixed chunk, after its (possibly skipped) initial FP64 residual.
+__global__ void k_mark_started(SysState* st) {
+  if (st->stage == 0) st->stage = st->status == ST_RUNNING ? 1 : 2;
+}
+
+// A mixed system whose FP32 iteration cannot track it (STAGNATION before any
+// fallback) continues as FP64 PCG from its current x, keeping its iteration
+// count -- the same transition as the persistent kernel's and the graph
+// solver's.
+__global__ void k_fallback_fp64(SysState* st) {
+  if (st->status != ST_STAGNATION || st->fell_back || st->precision != 1) return;
+  st->status = ST_RUNNING;
+  st->precision = 0;
+  st->fell_back = 1;
+  st->stage = 0;
+  st->mode = 0;
+  st->iter_at_fallback = st->iter;
 }
 
 // ---------------------------------------------------------------------------
@@ -305,12 +449,9 @@ template <int T>
 __global__ void __launch_bounds__(kCTA) k_mx_spmv_pq(SysView s) {
   if (ld_status(s.st) != ST_RUNNING || ld_mode(s.st) != 1) return;
   double v[1] = {tile_mx_spmv_pq<T>(s, blockIdx.x)};
-  if (publish_elect<1>(s, blockIdx.x, v, kSlotPQ, &s.st->cnt[1])) {
-    const int comp[1] = {kSlotPQ};
-    double o[1];
-    canon_reduce<1>(s.part, s.n_tiles, comp, o);
-    if (threadIdx.x == 0) scalar_after_pq(s.st, o[0]);
-  }
+  if (threadIdx.x == 0) __stcg(s.part + (size_t)blockIdx.x * kParts + kSlotPQ, v[0]);
+  double o[1];
+  if (elect2<1>(s, blockIdx.x, 1, kSlotPQ, 0, o) && threadIdx.x == 0) scalar_after_pq(s.st, o[0]);
 }
 
 // c += a p, r -= a q; the last CTA decides whether a reliable update is due
@@ -325,15 +466,11 @@ __global__ void __launch_bounds__(kCTA) k_mx_update_cr(SysView s, cudaGraphCondi
     tile_mx_update_cr(s, t, alpha, v);
     store_parts<2>(s, t, v, kSlotXR);
   }
-  if (elect_last(&s.st->cnt[2])) {
-    const int comp[2] = {kSlotXR, kSlotXR + 1};
-    double o[2];
-    canon_reduce<2>(s.part, s.n_tiles, comp, o);
-    if (threadIdx.x == 0) {
-      scalar_after_mx_cr(s.st, o[0], o[1]);
-      const bool upd = s.st->status == ST_RUNNING && s.st->mode == 0;
-      if (use_handle) cudaGraphSetConditional(h_upd, upd ? 1u : 0u);
-    }
+  double o[2];
+  if (elect2<2>(s, vec_t0(s), vec_tiles_for(s.tile_rows), kSlotXR, 1, o) && threadIdx.x == 0) {
+    scalar_after_mx_cr(s.st, o[0], o[1]);
+    const bool upd = s.st->status == ST_RUNNING && s.st->mode == 0;
+    if (use_handle) cudaGraphSetConditional(h_upd, upd ? 1u : 0u);
   }
 }
 
@@ -766,12 +903,16 @@ static cudaError_t add_while(cudaGraph_t g, cudaGraphNode_t* node, cudaGraphNode
 
 // The kernels of one threads-per-row variant; df selects the double-float
 // form of the plain iteration (init, SpMV, vector updates, final residual).
-struct KernelSet { const void *init, *spmv, *fin, *mx_outer, *mx_spmv, *iter, *update_xr, *update_p; };
+struct KernelSet {
+  const void *init, *spmv, *fin, *mx_outer, *mx_spmv, *iter, *update_xr, *update_p, *resume_p,
+      *init_chunk, *fin_if;
+};
 template <int T, bool D>
 static KernelSet kernel_set() {
   return {(const void*)k_init<T, D>, (const void*)k_spmv_pq<T, D>, (const void*)k_final<T, D>,
           (const void*)k_mx_outer<T>, (const void*)k_mx_spmv_pq<T>, (const void*)k_iter<T, D>,
-          (const void*)k_update_xr<D>, (const void*)k_update_p<D>};
+          (const void*)k_update_xr<D>, (const void*)k_update_p<D>, (const void*)k_resume_p<D>,
+          (const void*)k_init_chunk<T, D>, (const void*)k_final_if<T, D>};
 }
 template <bool D>
 static KernelSet kernels_for_t(int tpr) {
@@ -799,7 +940,9 @@ void PcgSolver::release() {
   if (plain_exec_) cudaGraphExecDestroy(plain_exec_);
   if (mixed_exec_) cudaGraphExecDestroy(mixed_exec_);
   if (df_exec_) cudaGraphExecDestroy(df_exec_);
-  plain_exec_ = mixed_exec_ = df_exec_ = nullptr;
+  if (cont_exec_) cudaGraphExecDestroy(cont_exec_);
+  if (cont_df_exec_) cudaGraphExecDestroy(cont_df_exec_);
+  plain_exec_ = mixed_exec_ = df_exec_ = cont_exec_ = cont_df_exec_ = nullptr;
   cudaFree(b_); cudaFree(x_); cudaFree(r_); cudaFree(p_); cudaFree(q_); cudaFree(part_);
   cudaFree(coop_bar_);
   coop_bar_ = nullptr;
@@ -879,22 +1022,20 @@ static SysView make_view(DeviceCRS* A, int tile_rows, int n_tiles, double* b, do
   return v;
 }
 
-cudaError_t PcgSolver::build_plain_graph(bool df) {
-  SysView v = make_view(A_, tile_rows_, n_tiles_, b_, x_, r_, p_, q_, nullptr, nullptr, nullptr,
-                        nullptr, part_, st_, abort_flag_, df);
+// The while loop of the plain (FP64 or double-float) iteration, after
+// `dep`: kUnrollPlain iterations per pass (one cooperative kernel each, or
+// three phase kernels), then the guard.
+cudaError_t PcgSolver::add_plain_loop(cudaGraph_t g, cudaGraphNode_t dep, SysView* v, bool df,
+                                      cudaGraphNode_t* loop_out) {
   const KernelSet ks = kernels_for(tpr_, df);
-  cudaGraph_t g;
-  NLGB_CUDA_TRY(cudaGraphCreate(&g, 0));
   cudaGraphConditionalHandle h;
   NLGB_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault));
-  void* a1[] = {&v};
-  cudaGraphNode_t n_init, n_loop, n_fin, prev;
-  NLGB_CUDA_TRY(add_kernel(g, &n_init, nullptr, ks.init, n_tiles_, kCTA, a1));
+  void* a1[] = {v};
   cudaGraph_t body;
-  NLGB_CUDA_TRY(add_while(g, &n_loop, n_init, h, &body));
-  prev = nullptr;
+  NLGB_CUDA_TRY(add_while(g, loop_out, dep, h, &body));
+  cudaGraphNode_t prev = nullptr;
   unsigned long long* bar = coop_bar_;
-  void* a_it[] = {&v, &bar};
+  void* a_it[] = {v, &bar};
   for (int u = 0; u < kUnrollPlain; ++u) {
     if (use_coop_) {
       cudaGraphNode_t n1;
@@ -914,11 +1055,38 @@ cudaError_t PcgSolver::build_plain_graph(bool df) {
     prev = n3;
   }
   int need_mode = -1, use_handle = 1;
-  void* ag[] = {&v, &h, &need_mode, &use_handle};
+  void* ag[] = {v, &h, &need_mode, &use_handle};
   cudaGraphNode_t n_g;
   NLGB_CUDA_TRY(add_kernel(body, &n_g, prev, (const void*)k_guard, 1, 1, ag));
-  NLGB_CUDA_TRY(add_kernel(g, &n_fin, n_loop, ks.fin, n_tiles_, kCTA, a1));
-  cudaError_t e = cudaGraphInstantiate(df ? &df_exec_ : &plain_exec_, g, 0);
+  return cudaSuccess;
+}
+
+// init -> while { iterations ; guard } -> final residual -> true-residual
+// check.  cont == true: the continuation after a failed check instead,
+// resume p update -> mark -> while { ... } -> final residual -> check.
+cudaError_t PcgSolver::build_plain_graph(bool df, bool cont) {
+  SysView v = make_view(A_, tile_rows_, n_tiles_, b_, x_, r_, p_, q_, nullptr, nullptr, nullptr,
+                        nullptr, part_, st_, abort_flag_, df);
+  const KernelSet ks = kernels_for(tpr_, df);
+  cudaGraph_t g;
+  NLGB_CUDA_TRY(cudaGraphCreate(&g, 0));
+  void* a1[] = {&v};
+  SysState* st = (SysState*)st_;
+  void* ast[] = {&st};
+  const int vg = (n_tiles_ + vec_tiles_for(tile_rows_) - 1) / vec_tiles_for(tile_rows_);
+  cudaGraphNode_t n_first, n_loop, n_fin, n_chk;
+  if (cont) {
+    cudaGraphNode_t n_res;
+    NLGB_CUDA_TRY(add_kernel(g, &n_res, nullptr, ks.resume_p, vg, kCTA, a1));
+    NLGB_CUDA_TRY(add_kernel(g, &n_first, n_res, (const void*)k_resume_mark, 1, 1, ast));
+  } else {
+    NLGB_CUDA_TRY(add_kernel(g, &n_first, nullptr, ks.init, n_tiles_, kCTA, a1));
+  }
+  cudaError_t e = add_plain_loop(g, n_first, &v, df, &n_loop);
+  if (e == cudaSuccess) e = add_kernel(g, &n_fin, n_loop, ks.fin, n_tiles_, kCTA, a1);
+  if (e == cudaSuccess) e = add_kernel(g, &n_chk, n_fin, (const void*)k_check, 1, 1, ast);
+  cudaGraphExec_t* out = cont ? (df ? &cont_df_exec_ : &cont_exec_) : (df ? &df_exec_ : &plain_exec_);
+  if (e == cudaSuccess) e = cudaGraphInstantiate(out, g, 0);
   cudaGraphDestroy(g);
   NLGB_CUDA_TRY(e);
   return cudaSuccess;
@@ -971,14 +1139,20 @@ cudaError_t PcgSolver::build_mixed_graph() {
 static bool eager_mode();
 
 // ---------------------------------------------------------------------------
-// ViewGraph: resumable FP64 PCG continuation of a system whose buffers and
-// state live elsewhere (a SystemSlot of the persistent solver).  Same kernels
-// and order as the plain graph, without the initial residual:
-//   chunk start -> while { (q = A p, p.q ; x, r ; p) x 4 ; guard } -> final
-//   residual -> chunk end.
-// The iterates are those of the persistent kernel (same tile procedures and
-// canonical reductions), so a system may switch between the two executors
-// at any iteration boundary (the graph pauses on whole passes of 4).
+// ViewGraph: resumable PCG chunks of a system whose buffers and state live
+// elsewhere (a SystemSlot of the server or of the persistent solver).  The
+// kernels and their order are those of the single-system graphs, so a
+// system's iterates do not depend on where a chunk ends, on other systems
+// running concurrently on other streams, or on switching between this
+// executor and the persistent kernel:
+//   FP64 / double-float:  initial residual (stage 0 only) -> resume p update
+//     (stage 4 only) -> while { (q = A p, p.q ; x, r ; p) x 4 ; guard } ->
+//     final residual (if the system stopped) -> true-residual check -> end;
+//   mixed:  initial FP64 residual (fresh system only) -> mark started ->
+//     while { (p ; q = A32 p, p.q ; c, r -> IF(update due) { x += c ; FP64
+//     residual }) x 4 ; guard } -> final residual (if stopped) -> end.
+// A chunk pauses on whole passes of 4 iterations (guard), the system stays
+// running; the server continues it with another chunk later.
 // ---------------------------------------------------------------------------
 ViewGraph::~ViewGraph() {
   if (exec_) cudaGraphExecDestroy(exec_);
@@ -986,36 +1160,68 @@ ViewGraph::~ViewGraph() {
   if (e1_) cudaEventDestroy(e1_);
 }
 
-cudaError_t ViewGraph::build(const SysView& v) {
+cudaError_t ViewGraph::build(const SysView& v, bool mixed) {
   if (exec_) cudaGraphExecDestroy(exec_);
   exec_ = nullptr;
   if (!e0_) NLGB_CUDA_TRY(cudaEventCreate(&e0_));
   if (!e1_) NLGB_CUDA_TRY(cudaEventCreate(&e1_));
   view_ = v;
-  const KernelSet ks = kernels_for(v.tpr, v.df != 0);
+  mixed_ = mixed;
+  const KernelSet ks = kernels_for(v.tpr, !mixed && v.df != 0);
   cudaGraph_t g;
   NLGB_CUDA_TRY(cudaGraphCreate(&g, 0));
   cudaGraphConditionalHandle h;
   NLGB_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault));
   void* a1[] = {&view_};
-  cudaGraphNode_t n_loop, n_fin, prev = nullptr;
-  cudaGraph_t body;
-  NLGB_CUDA_TRY(add_while(g, &n_loop, nullptr, h, &body));
+  SysState* st = v.st;
+  void* ae[] = {&st};
   const int vg = (v.n_tiles + vec_tiles_for(v.tile_rows) - 1) / vec_tiles_for(v.tile_rows);
-  for (int u = 0; u < kUnrollPlain; ++u) {
-    cudaGraphNode_t n1, n2, n3;
-    NLGB_CUDA_TRY(add_kernel(body, &n1, prev, ks.spmv, v.n_tiles, kCTA, a1));
-    NLGB_CUDA_TRY(add_kernel(body, &n2, n1, ks.update_xr, vg, kCTA, a1));
-    NLGB_CUDA_TRY(add_kernel(body, &n3, n2, ks.update_p, vg, kCTA, a1));
-    prev = n3;
+  cudaGraphNode_t n_start, n_loop, n_fin, n_end, prev = nullptr;
+  cudaGraph_t body;
+  if (!mixed) {
+    cudaGraphNode_t n_init, n_res;
+    NLGB_CUDA_TRY(add_kernel(g, &n_init, nullptr, ks.init_chunk, v.n_tiles, kCTA, a1));
+    NLGB_CUDA_TRY(add_kernel(g, &n_res, n_init, ks.resume_p, vg, kCTA, a1));
+    NLGB_CUDA_TRY(add_kernel(g, &n_start, n_res, (const void*)k_resume_mark, 1, 1, ae));
+    NLGB_CUDA_TRY(add_while(g, &n_loop, n_start, h, &body));
+    for (int u = 0; u < kUnrollPlain; ++u) {
+      cudaGraphNode_t n1, n2, n3;
+      NLGB_CUDA_TRY(add_kernel(body, &n1, prev, ks.spmv, v.n_tiles, kCTA, a1));
+      NLGB_CUDA_TRY(add_kernel(body, &n2, n1, ks.update_xr, vg, kCTA, a1));
+      NLGB_CUDA_TRY(add_kernel(body, &n3, n2, ks.update_p, vg, kCTA, a1));
+      prev = n3;
+    }
+  } else {
+    cudaGraphNode_t n_outer;
+    NLGB_CUDA_TRY(add_kernel(g, &n_outer, nullptr, ks.mx_outer, v.n_tiles, kCTA, a1));
+    NLGB_CUDA_TRY(add_kernel(g, &n_start, n_outer, (const void*)k_mark_started, 1, 1, ae));
+    NLGB_CUDA_TRY(add_while(g, &n_loop, n_start, h, &body));
+    for (int u = 0; u < kUnrollInner; ++u) {
+      cudaGraphConditionalHandle h_upd;
+      NLGB_CUDA_TRY(cudaGraphConditionalHandleCreate(&h_upd, body, 0u, cudaGraphCondAssignDefault));
+      cudaGraphNode_t n1, n2, n3, n_if, n4, n5;
+      NLGB_CUDA_TRY(add_kernel(body, &n1, prev, (const void*)k_mx_update_p, vg, kCTA, a1));
+      NLGB_CUDA_TRY(add_kernel(body, &n2, n1, ks.mx_spmv, v.n_tiles, kCTA, a1));
+      int use_handle = 1;
+      void* acr[] = {&view_, &h_upd, &use_handle};
+      NLGB_CUDA_TRY(add_kernel(body, &n3, n2, (const void*)k_mx_update_cr, vg, kCTA, acr));
+      cudaGraph_t ubody;
+      NLGB_CUDA_TRY(add_cond(body, &n_if, n3, h_upd, cudaGraphCondTypeIf, &ubody));
+      NLGB_CUDA_TRY(add_kernel(ubody, &n4, nullptr, (const void*)k_mx_apply, vg, kCTA, a1));
+      NLGB_CUDA_TRY(add_kernel(ubody, &n5, n4, ks.mx_outer, v.n_tiles, kCTA, a1));
+      prev = n_if;
+    }
   }
   int need_mode = -1, use_handle = 1;
   void* ag[] = {&view_, &h, &need_mode, &use_handle};
-  cudaGraphNode_t n_g, n_end;
+  cudaGraphNode_t n_g;
   NLGB_CUDA_TRY(add_kernel(body, &n_g, prev, (const void*)k_guard, 1, 1, ag));
-  NLGB_CUDA_TRY(add_kernel(g, &n_fin, n_loop, ks.fin, v.n_tiles, kCTA, a1));
-  SysState* st = v.st;
-  void* ae[] = {&st};
+  NLGB_CUDA_TRY(add_kernel(g, &n_fin, n_loop, ks.fin_if, v.n_tiles, kCTA, a1));
+  if (!mixed) {
+    cudaGraphNode_t n_chk;
+    NLGB_CUDA_TRY(add_kernel(g, &n_chk, n_fin, (const void*)k_check, 1, 1, ae));
+    n_fin = n_chk;
+  }
   NLGB_CUDA_TRY(add_kernel(g, &n_end, n_fin, (const void*)k_chunk_end, 1, 1, ae));
   cudaError_t e = cudaGraphInstantiate(&exec_, g, 0);
   cudaGraphDestroy(g);
@@ -1031,11 +1237,20 @@ static bool same_view(const SysView& a, const SysView& b) {
          a.df == b.df && a.vadf == b.vadf && a.dinvdf == b.dinvdf &&
          a.rp == b.rp && a.ci == b.ci && a.va == b.va && a.dinv == b.dinv && a.b == b.b &&
          a.x == b.x && a.r == b.r && a.p == b.p && a.q == b.q && a.part == b.part && a.st == b.st &&
-         a.abort_flag == b.abort_flag;
+         a.va32 == b.va32 && a.dinv32 == b.dinv32 && a.r32 == b.r32 && a.p32 == b.p32 &&
+         a.q32 == b.q32 && a.c32 == b.c32 && a.abort_flag == b.abort_flag;
 }
 
-cudaError_t ViewGraph::run(const SysView& v, long long iters, cudaStream_t s, float* ms) {
-  if (!exec_ || !same_view(v, view_)) NLGB_CUDA_TRY(build(v));
+cudaError_t ViewGraph::prepare(const SysView& v, bool mixed) {
+  if (!exec_ || mixed != mixed_ || !same_view(v, view_)) NLGB_CUDA_TRY(build(v, mixed));
+  return cudaSuccess;
+}
+
+cudaError_t ViewGraph::run(const SysView& v, long long iters, cudaStream_t s, float* ms, bool mixed) {
+  if (!eager_mode()) NLGB_CUDA_TRY(prepare(v, mixed));
+  else { view_ = v; mixed_ = mixed; }
+  if (!e0_) NLGB_CUDA_TRY(cudaEventCreate(&e0_));
+  if (!e1_) NLGB_CUDA_TRY(cudaEventCreate(&e1_));
   NLGB_CUDA_TRY(cudaEventRecord(e0_, s));
   k_chunk_start<<<1, 1, 0, s>>>(v.st, std::max(1LL, iters), kUnrollPlain);
   NLGB_CUDA_TRY(cudaGetLastError());
@@ -1050,34 +1265,67 @@ cudaError_t ViewGraph::run(const SysView& v, long long iters, cudaStream_t s, fl
   return cudaSuccess;
 }
 
+cudaError_t chunk_fallback_fp64(SysState* st, cudaStream_t s) {
+  k_fallback_fp64<<<1, 1, 0, s>>>(st);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+bool ViewGraph::done() const {
+  if (!pending_) return true;
+  return cudaEventQuery(e1_) != cudaErrorNotReady;
+}
+
 // Eager mode: the chunk's kernels launched one by one (profiling only).
 cudaError_t ViewGraph::run_eager(cudaStream_t s, long long iters) {
-  const KernelSet ks = kernels_for(view_.tpr, view_.df != 0);
+  const KernelSet ks = kernels_for(view_.tpr, !mixed_ && view_.df != 0);
   const int vg = (view_.n_tiles + vec_tiles_for(view_.tile_rows) - 1) / vec_tiles_for(view_.tile_rows);
   const cudaGraphConditionalHandle none = 0;
   const int need = -1, no_handle = 0;
   void* a1[] = {&view_};
   void* ag[] = {&view_, const_cast<cudaGraphConditionalHandle*>(&none), const_cast<int*>(&need),
                 const_cast<int*>(&no_handle)};
+  void* acr[] = {&view_, const_cast<cudaGraphConditionalHandle*>(&none), const_cast<int*>(&no_handle)};
   SysState* st = view_.st;
   void* ae[] = {&st};
   int status = ST_RUNNING;
   long long launched = 0;
+  auto go = [&](const void* fn, int grid, int block, void** args) {
+    ++launched;
+    return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, 0, s);
+  };
+  if (!mixed_) {
+    NLGB_CUDA_TRY(go(ks.init_chunk, view_.n_tiles, kCTA, a1));
+    NLGB_CUDA_TRY(go(ks.resume_p, vg, kCTA, a1));
+    NLGB_CUDA_TRY(go((const void*)k_resume_mark, 1, 1, ae));
+  } else {
+    NLGB_CUDA_TRY(go(ks.mx_outer, view_.n_tiles, kCTA, a1));
+    NLGB_CUDA_TRY(go((const void*)k_mark_started, 1, 1, ae));
+  }
+  NLGB_CUDA_TRY(cudaMemcpyAsync(&status, &st->status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  NLGB_CUDA_TRY(cudaStreamSynchronize(s));
   for (long long pass = 0; pass * kUnrollPlain < std::max(1LL, iters) && status == ST_RUNNING; ++pass) {
     for (int u = 0; u < kUnrollPlain; ++u) {
-      NLGB_CUDA_TRY(cudaLaunchKernel(ks.spmv, dim3(view_.n_tiles), dim3(kCTA), a1, 0, s));
-      NLGB_CUDA_TRY(cudaLaunchKernel(ks.update_xr, dim3(vg), dim3(kCTA), a1, 0, s));
-      NLGB_CUDA_TRY(cudaLaunchKernel(ks.update_p, dim3(vg), dim3(kCTA), a1, 0, s));
-      launched += 3;
+      if (!mixed_) {
+        NLGB_CUDA_TRY(go(ks.spmv, view_.n_tiles, kCTA, a1));
+        NLGB_CUDA_TRY(go(ks.update_xr, vg, kCTA, a1));
+        NLGB_CUDA_TRY(go(ks.update_p, vg, kCTA, a1));
+      } else {
+        NLGB_CUDA_TRY(go((const void*)k_mx_update_p, vg, kCTA, a1));
+        NLGB_CUDA_TRY(go(ks.mx_spmv, view_.n_tiles, kCTA, a1));
+        NLGB_CUDA_TRY(go((const void*)k_mx_update_cr, vg, kCTA, acr));
+        NLGB_CUDA_TRY(go((const void*)k_mx_apply, vg, kCTA, a1));   // return unless an update is due
+        NLGB_CUDA_TRY(go(ks.mx_outer, view_.n_tiles, kCTA, a1));
+      }
     }
-    NLGB_CUDA_TRY(cudaLaunchKernel((const void*)k_guard, dim3(1), dim3(1), ag, 0, s));
-    ++launched;
+    NLGB_CUDA_TRY(go((const void*)k_guard, 1, 1, ag));
     NLGB_CUDA_TRY(cudaMemcpyAsync(&status, &st->status, sizeof(int), cudaMemcpyDeviceToHost, s));
     NLGB_CUDA_TRY(cudaStreamSynchronize(s));
   }
-  NLGB_CUDA_TRY(cudaLaunchKernel(ks.fin, dim3(view_.n_tiles), dim3(kCTA), a1, 0, s));
-  NLGB_CUDA_TRY(cudaLaunchKernel((const void*)k_chunk_end, dim3(1), dim3(1), ae, 0, s));
-  count_launches(launched + 2);
+  NLGB_CUDA_TRY(go(ks.fin_if, view_.n_tiles, kCTA, a1));
+  if (!mixed_) NLGB_CUDA_TRY(go((const void*)k_check, 1, 1, ae));
+  NLGB_CUDA_TRY(go((const void*)k_chunk_end, 1, 1, ae));
+  count_launches(launched);
   eager_counted_ = true;
   return cudaSuccess;
 }
@@ -1087,32 +1335,30 @@ cudaError_t ViewGraph::finish(long long iters_before, long long iters_after) {
   pending_ = false;
   NLGB_CUDA_TRY(cudaEventSynchronize(e1_));
   if (ms_) NLGB_CUDA_TRY(cudaEventElapsedTime(ms_, e0_, e1_));
-  // kernels executed: chunk start/end, final residual, and per while-body
-  // pass 3 kernels per unrolled iteration + the guard
   if (eager_counted_) {   // run_eager counted its launches (plus the chunk start)
     eager_counted_ = false;
     count_launches(1);
     return cudaSuccess;
   }
+  // kernels executed: chunk start and end, the fixed nodes before and after
+  // the loop, and per while-body pass 3 kernels per unrolled iteration + the
+  // guard (mixed: + 2 per reliable update, counted as passes x 1 here)
   const long long passes = (std::max(0LL, iters_after - iters_before) + kUnrollPlain - 1) / kUnrollPlain;
-  count_launches(3 + std::max(1LL, passes) * (3LL * kUnrollPlain + 1));
+  count_launches((mixed_ ? 5 : 7) + std::max(1LL, passes) * (3LL * kUnrollPlain + 1));
   return cudaSuccess;
 }
 
-// Eager mode (environment NLGB_EAGER_SOLVE=1): the same kernels as the
-// graphs, launched one by one from a host loop that reads the status after
-// every unrolled pass.  Slower (one host round trip per pass); it exists so
-// that profilers which do not descend into conditional graph nodes see
-// every kernel of an iteration.
+// Eager mode (environment NLGB_EAGER_SOLVE=1, read at every solve): the
+// same kernels as the graphs, launched one by one from a host loop that
+// reads the status after every unrolled pass.  Slower (one host round trip
+// per pass); it exists so that profilers and launch lists, which do not
+// descend into conditional graph nodes, see every kernel of an iteration.
 static bool eager_mode() {
-  static const bool on = [] {
-    const char* e = std::getenv("NLGB_EAGER_SOLVE");
-    return e != nullptr && e[0] == '1';
-  }();
-  return on;
+  const char* e = std::getenv("NLGB_EAGER_SOLVE");
+  return e != nullptr && e[0] == '1';
 }
 
-cudaError_t PcgSolver::run_eager(bool mixed, bool df, SysState* h) {
+cudaError_t PcgSolver::run_eager(bool mixed, bool df, SysState* h, bool cont) {
   SysView v = make_view(A_, tile_rows_, n_tiles_, b_, x_, r_, p_, q_, r32_, p32_, q32_, c32_,
                         part_, st_, abort_flag_, df && !mixed);
   const KernelSet ks = kernels_for(tpr_, df && !mixed);
@@ -1128,7 +1374,14 @@ cudaError_t PcgSolver::run_eager(bool mixed, bool df, SysState* h) {
   void* ag[] = {&v, const_cast<cudaGraphConditionalHandle*>(&none), const_cast<int*>(&need),
                 const_cast<int*>(&no_handle)};
   void* acr[] = {&v, const_cast<cudaGraphConditionalHandle*>(&none), const_cast<int*>(&no_handle)};
-  NLGB_CUDA_TRY(go(mixed ? ks.mx_outer : ks.init, n_tiles_, kCTA, a1));
+  SysState* st = (SysState*)st_;
+  void* ast[] = {&st};
+  if (cont) {
+    NLGB_CUDA_TRY(go(ks.resume_p, vg, kCTA, a1));
+    NLGB_CUDA_TRY(go((const void*)k_resume_mark, 1, 1, ast));
+  } else {
+    NLGB_CUDA_TRY(go(mixed ? ks.mx_outer : ks.init, n_tiles_, kCTA, a1));
+  }
   while (true) {
     for (int u = 0; u < (mixed ? kUnrollInner : kUnrollPlain); ++u) {
       if (mixed) {
@@ -1149,7 +1402,31 @@ cudaError_t PcgSolver::run_eager(bool mixed, bool df, SysState* h) {
     if (h->status != ST_RUNNING) break;
   }
   NLGB_CUDA_TRY(go(ks.fin, n_tiles_, kCTA, a1));
+  if (!mixed) NLGB_CUDA_TRY(go((const void*)k_check, 1, 1, ast));
   count_launches(launched);
+  return cudaSuccess;
+}
+
+cudaError_t PcgSolver::run_cont(bool df, float* ms) {
+  cudaGraphExec_t* ex = df ? &cont_df_exec_ : &cont_exec_;
+  if (!eager_mode() && !*ex) NLGB_CUDA_TRY(build_plain_graph(df, true));
+  SysState* h = (SysState*)st_host_;
+  const long long guard0 = h->guard;
+  NLGB_CUDA_TRY(cudaEventRecord(ev0_, stream_));
+  if (eager_mode()) {
+    NLGB_CUDA_TRY(run_eager(false, df, h, true));
+  } else {
+    NLGB_CUDA_TRY(cudaGraphLaunch(*ex, stream_));
+  }
+  NLGB_CUDA_TRY(cudaEventRecord(ev1_, stream_));
+  NLGB_CUDA_TRY(cudaMemcpyAsync(h, st_, sizeof(SysState), cudaMemcpyDeviceToHost, stream_));
+  NLGB_CUDA_TRY(cudaStreamSynchronize(stream_));
+  NLGB_CUDA_TRY(cudaEventElapsedTime(ms, ev0_, ev1_));
+  if (eager_mode()) return cudaSuccess;   // run_eager counted its launches
+  ++graph_launches_;
+  // resume p update, mark, final residual, check + every while-body pass
+  const long long per_iter = use_coop_ ? 1 : 3;
+  count_launches(4 + (h->guard - guard0) * (per_iter * kUnrollPlain + 1));
   return cudaSuccess;
 }
 
@@ -1171,7 +1448,9 @@ cudaError_t PcgSolver::run_graph(bool mixed, bool df, const SolveParams& prm, lo
       use_coop_ = false;
       if (plain_exec_) cudaGraphExecDestroy(plain_exec_);
       if (df_exec_) cudaGraphExecDestroy(df_exec_);
-      plain_exec_ = df_exec_ = nullptr;
+      if (cont_exec_) cudaGraphExecDestroy(cont_exec_);
+      if (cont_df_exec_) cudaGraphExecDestroy(cont_df_exec_);
+      plain_exec_ = df_exec_ = cont_exec_ = cont_df_exec_ = nullptr;
       e = build_plain_graph(df);
     }
     NLGB_CUDA_TRY(e);
@@ -1215,10 +1494,11 @@ cudaError_t PcgSolver::run_graph(bool mixed, bool df, const SolveParams& prm, lo
   ++graph_launches_;
   // Kernel nodes executed: every while-body pass runs all of its kernels
   // (3 per unrolled iteration + the guard); the mixed graph adds 2 kernels
-  // per reliable update after the first; plus the first and final kernels.
+  // per reliable update after the first; plus the first and final kernels
+  // (and the true-residual check of the plain graph).
   const long long passes = h->guard;
   const long long per_iter = (!mixed && use_coop_) ? 1 : 3;
-  long long k = 2 + passes * (per_iter * unroll + 1);
+  long long k = (mixed ? 2 : 3) + passes * (per_iter * unroll + 1);
   if (mixed) k += 2LL * std::max(0, h->outer - outer - 1);
   count_launches(k);
   return cudaSuccess;
@@ -1238,9 +1518,21 @@ cudaError_t PcgSolver::solve(const double* b, double* x, const SolveParams& prm,
   NLGB_CUDA_TRY(cudaMemcpyAsync(x_, x, (size_t)n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
   if (df) NLGB_CUDA_TRY(df_pack(x_, n_, stream_));
   float ms = 0.f;
-  NLGB_CUDA_TRY(run_graph(mixed, df, prm, max_iter, 0, 0, &ms));
-  if (df) NLGB_CUDA_TRY(df_unpack(x_, n_, stream_));
   SysState* h = (SysState*)st_host_;
+  // An FP64 / double-float stop whose true residual missed eps leaves the
+  // state running (k_check): continue the recurrence until it passes or
+  // stalls (at most kMaxTrueChecks continuations).
+  auto continue_checks = [&](bool dfc) -> cudaError_t {
+    for (int c = 0; c <= kMaxTrueChecks && h->status == ST_RUNNING; ++c) {
+      float m = 0.f;
+      NLGB_CUDA_TRY(run_cont(dfc, &m));
+      ms += m;
+    }
+    return cudaSuccess;
+  };
+  NLGB_CUDA_TRY(run_graph(mixed, df, prm, max_iter, 0, 0, &ms));
+  if (!mixed) NLGB_CUDA_TRY(continue_checks(df));
+  if (df) NLGB_CUDA_TRY(df_unpack(x_, n_, stream_));
   if (mixed && h->status == ST_STAGNATION && !h->fell_back) {
     // FP32 cannot track this system (kappa * u32 ~ 1): continue it with the
     // FP64 PCG from the current x, keeping the iteration count.
@@ -1249,6 +1541,7 @@ cudaError_t PcgSolver::solve(const double* b, double* x, const SolveParams& prm,
     float ms2 = 0.f;
     NLGB_CUDA_TRY(run_graph(false, false, prm, max_iter, done, outer, &ms2));
     ms += ms2;
+    NLGB_CUDA_TRY(continue_checks(false));
   }
   NLGB_CUDA_TRY(cudaMemcpyAsync(x, x_, (size_t)n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
   NLGB_CUDA_TRY(cudaStreamSynchronize(stream_));

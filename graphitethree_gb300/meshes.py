@@ -37,19 +37,21 @@ def eval_bumps(bumps, x: np.ndarray, y: np.ndarray) -> np.ndarray:
 
 def grid_faces(nx: int, ny: int, rng: np.random.Generator) -> np.ndarray:
     """Triangles of an nx x ny vertex grid, one seeded diagonal per quad."""
-    i, j = np.meshgrid(np.arange(nx - 1), np.arange(ny - 1), indexing="xy")
-    v00 = (j * nx + i).ravel().astype(np.int64)
+    i, j = np.meshgrid(np.arange(nx - 1, dtype=np.int32), np.arange(ny - 1, dtype=np.int32), indexing="xy")
+    v00 = (j * np.int32(nx) + i).ravel()
     v10 = v00 + 1
-    v01 = v00 + nx
+    v01 = v00 + np.int32(nx)
     v11 = v01 + 1
     diag = rng.integers(0, 2, size=v00.shape[0]).astype(bool)
     # diag False: (v00,v10,v11), (v00,v11,v01); True: (v00,v10,v01), (v10,v11,v01)
-    t1 = np.where(diag[:, None], np.stack([v00, v10, v01], 1), np.stack([v00, v10, v11], 1))
-    t2 = np.where(diag[:, None], np.stack([v10, v11, v01], 1), np.stack([v00, v11, v01], 1))
-    faces = np.empty((2 * v00.shape[0], 3), dtype=np.int64)
-    faces[0::2] = t1
-    faces[1::2] = t2
-    return faces.astype(np.int32)
+    faces = np.empty((2 * v00.shape[0], 3), dtype=np.int32)
+    faces[0::2, 0] = v00
+    faces[0::2, 1] = v10
+    faces[0::2, 2] = np.where(diag, v01, v11)
+    faces[1::2, 0] = np.where(diag, v10, v00)
+    faces[1::2, 1] = v11
+    faces[1::2, 2] = v01
+    return faces
 
 
 def height_field(nx: int, ny: int, seed: int, n_bumps: int = 8, flat: bool = False,

@@ -197,7 +197,8 @@ class Server:
 
     def __init__(self, budget_bytes: float = 150e9, precision: str = "mixed", mode: str = "batched",
                  eps: float = 1e-10, epoch_iters: int = 256, inner_eps: float = 0.1,
-                 max_systems: int = 8192, max_iter: int = -1):
+                 max_systems: int = 8192, max_iter: int = -1, schedule: str = "srpt",
+                 epoch_ms: float = 10.0, streams: int = 16):
         L = _lib.load()
         cfg = _lib.NlgbServerConfig()
         L.nlgb_server_default_config(ctypes.byref(cfg))
@@ -209,6 +210,9 @@ class Server:
         cfg.inner_eps = inner_eps
         cfg.max_systems = max_systems
         cfg.max_iter = max_iter
+        cfg.schedule = K["NLGB_SCHEDULE_SRPT"] if schedule == "srpt" else K["NLGB_SCHEDULE_ALL"]
+        cfg.epoch_ms = epoch_ms
+        cfg.streams = streams
         h = L.nlgb_server_create(ctypes.byref(cfg))
         if not h:
             raise SolverError(f"nlgb_server_create failed: {_lib.last_error()}")
@@ -294,6 +298,16 @@ class Server:
         if rc != 0:
             raise SolverError(f"request {ticket} failed: {_lib.last_error()}")
         return out, infos, lat.value
+
+    def wait_result(self, ticket: int):
+        """Like wait, without raising: returns (ok, solutions, [SolveInfo],
+        latency_s); a failed or aborted request gives ok False and the
+        per-system statuses it ended with."""
+        out = self._out[ticket]
+        R = (_lib.NlgbResult * out.shape[0])()
+        lat = ctypes.c_double()
+        rc = _lib.load().nlgb_server_wait(self._h, ticket, R, ctypes.byref(lat))
+        return rc == 0, out, [_info(r) for r in R], lat.value
 
     def drain(self) -> int:
         return _lib.load().nlgb_server_drain(self._h)

@@ -307,3 +307,71 @@ def serving_sample(n_requests: int, seed: int, rate: float, vmin: int = 1_000,
         else:
             objs.append(("square", fairing_system(r.nx, r.ny, r.seed, lam=1e-2, n_rhs=3)))
     return reqs, objs
+
+
+@dataclass
+class StreamRequest:
+    """One request of the serving stream with its mesh: LSCM (one system
+    over the 2 nv - 4 free variables, pins at vertices 0 and nv - 1) or
+    cotangent fairing (L + lam I, right-hand sides b (3, nv))."""
+    rid: int
+    kind: str            # "lscm" or "fairing"
+    nx: int
+    ny: int
+    seed: int
+    arrival: float       # seconds after the stream starts
+    V: np.ndarray
+    F: np.ndarray
+    b: np.ndarray | None = None
+    lam: float = 1e-2
+
+    @property
+    def n_verts(self) -> int:
+        return int(self.V.shape[0])
+
+    @property
+    def unknowns(self) -> int:
+        return 2 * self.n_verts - 4 if self.kind == "lscm" else self.n_verts
+
+    def host_system(self):
+        """The same system built on the host from the published formulas
+        (rows / CRS of systems.py): (rp, ci, va, rhs (n_rhs, n)) -- the
+        oracle's input."""
+        if self.kind == "lscm":
+            from oracle import oracle   # test infrastructure, imported only by its callers
+            rp, ci, va, rhs = oracle.assemble_rowstream(lscm_rows(self.V, self.F))
+            return rp, ci, va, rhs
+        rp, ci, va = cotan_laplacian(self.V, self.F, self.lam)
+        return rp, ci, va, self.b
+
+
+def stream_window(rate: float, window: float, seed: int, vmin: int = 1_000, vmax: int = 1_000_000,
+                  lam: float = 1e-2, noise: float = 1e-3) -> list[StreamRequest]:
+    """The serving stream over [0, window): Poisson arrivals at `rate`/s;
+    each request is LSCM or cotangent-Laplacian fairing (3 right-hand sides:
+    the x, y, z positions + N(0, noise) times lam) with probability 1/2,
+    vertex count log-uniform in [vmin, vmax], a square-ish seeded grid patch
+    with the bump model of config 1.  Requests are drawn one after the
+    other from one seeded generator, so a longer window extends a shorter
+    one."""
+    rng = np.random.default_rng(seed)
+    out: list[StreamRequest] = []
+    t = 0.0
+    while True:
+        gap = float(rng.exponential(1.0 / rate))
+        t = gap if not out else t + gap
+        if t >= window:
+            break
+        nv = float(np.exp(rng.uniform(np.log(vmin), np.log(vmax))))
+        kind = "lscm" if int(rng.integers(0, 2)) == 0 else "fairing"
+        s = int(rng.integers(0, 2**31 - 1))
+        side = max(4, int(round(np.sqrt(nv))))
+        V, F = meshes.height_field(side, side, s)
+        b = None
+        if kind == "fairing":
+            r2 = np.random.default_rng(s + 7919)
+            P = V.T.copy()
+            b = np.ascontiguousarray(lam * (P + r2.normal(0.0, noise, P.shape)))
+        out.append(StreamRequest(rid=len(out), kind=kind, nx=side, ny=side, seed=s, arrival=t, V=V,
+                                 F=F, b=b, lam=lam))
+    return out

@@ -31,8 +31,10 @@
  *     number of rows must equal the number of free variables.
  *   - nlSolve runs Jacobi-preconditioned CG on the GPU from the current
  *     variable values, until ||b - A x||_2 <= NL_THRESHOLD * ||b||_2
- *     (recursively updated residual for NL_GB300_PRECISION_DOUBLE, the true
- *     FP64 residual for NL_GB300_PRECISION_MIXED) or NL_MAX_ITERATIONS.
+ *     (recursively updated residual for NL_GB300_PRECISION_DOUBLE, then the
+ *     true FP64 residual is recomputed and, if it misses the threshold, the
+ *     iteration continues with a lower recursive threshold; the true FP64
+ *     residual for NL_GB300_PRECISION_MIXED) or NL_MAX_ITERATIONS.
  *     Defaults: NL_THRESHOLD = 1e-10, NL_MAX_ITERATIONS = 5 * n_free.
  *   - Errors never abort the process: void calls report through
  *     nlGetError()/nlGetErrorString() and stderr; nlSolve returns NL_FALSE.
@@ -118,6 +120,13 @@ typedef void*          NLContext;
 #define NL_GB300_STATUS_DEVICE_ERR 5  /* CUDA error (message in nlGetErrorString) */
 #define NL_GB300_STATUS_BAD_INPUT  6  /* rejected before touching the GPU     */
 #define NL_GB300_STATUS_ABORTED    7  /* host abort flag raised              */
+/* FP64 / double-float: the recursive residual met NL_THRESHOLD, and the true
+ * FP64 residual recomputed then did not, even after the iteration was
+ * continued with a lower recursive threshold (up to 4 times) -- the
+ * attainable accuracy of the recurrence lies above NL_THRESHOLD.  The
+ * solution is returned (nlSolve returns NL_TRUE: OpenNL's own stopping
+ * rule was met); NL_GB300_TRUE_RESIDUAL gives the true residual. */
+#define NL_GB300_STATUS_TRUE_RESIDUAL_STALLED 8
 
 /* ---- solvers / preconditioners ---- */
 #define NL_SOLVER_DEFAULT 0x000
@@ -207,6 +216,10 @@ NLboolean nlSolve(void);
 
 struct NLMatrixStruct;
 typedef struct NLMatrixStruct* NLMatrix;
+/* OGF::NL::Matrix casts its matrix to NLSparseMatrix* before
+ * nlSparseMatrixAdd (matrix.cpp:163,237,257,291): here every matrix object
+ * starts with NLMatrixStruct, so the two names are one type. */
+typedef struct NLMatrixStruct NLSparseMatrix;
 typedef void (*NLDestroyMatrixFunc)(NLMatrix M);
 typedef void (*NLMultMatrixVectorFunc)(NLMatrix M, const double* x, double* y);
 
@@ -243,7 +256,10 @@ typedef void   (*FUNPTR_axpy)(NLBlas_t, int n, double a, const double* x, int in
 typedef void   (*FUNPTR_mul)(NLBlas_t, int n, const double* x, double* y); /* y <- x .* y */
 
 /* The table's vector arguments may be host or device pointers: the
- * computation always runs on the GPU (host vectors are staged). */
+ * computation always runs on the GPU (host vectors are staged through device
+ * buffers, two PCIe / C2C transfers per call).  Increments follow BLAS:
+ * element i of a vector with increment inc sits at i * inc, or at
+ * (n - 1 - i) * |inc| when inc < 0; inc == 0 is rejected. */
 struct NLBlas {
     FUNPTR_copy Dcopy;
     FUNPTR_scal Dscal;

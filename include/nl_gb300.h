@@ -149,7 +149,9 @@ int nlgb_batch_solve(int n_sys, const nlgb_matrix* A, const double* const* b, do
  * The first call on a device looks up the array's address with that device
  * current.  Every call reuses the same array: calls that overlap on the GPU
  * race and must be serialised by the caller.  stream: a cudaStream_t (NULL:
- * the default stream); the call returns when the solve is finished. */
+ * the default stream); the call returns when the solve is finished
+ * (res->seconds: host time of the call).  n == 0 returns at once
+ * (converged). */
 int nlgb_solve_noalloc(int n, const int* rp, const int* ci, const double* va, const double* b,
                        double* x, const nlgb_params* prm, nlgb_result* res, void* stream);
 
@@ -173,15 +175,28 @@ int nlgb_assemble(int least_squares, long long n_rows, const long long* row_ptr,
  * accepts solves of any size at any time, admits them while their device
  * footprint fits the HBM budget, keeps their matrices and Krylov state
  * resident until convergence and advances every admitted system together:
- * each "epoch" is one persistent-kernel launch that runs every active system
- * for up to epoch_iters iterations; requests arriving meanwhile are
- * uploaded (and least-squares rows assembled) on a second stream while the
- * epoch runs and join the next epoch.  A result does not depend on what else
+ * each "epoch" is one persistent-kernel launch over the active systems (see
+ * NLGB_SCHEDULE_*); requests arriving meanwhile are uploaded and built (or
+ * their least-squares rows assembled) by an admission thread on a second
+ * stream while the epoch runs, and join the next epoch.  A result does not depend on what else
  * is in flight (bit-identical alone and in any mix). */
 typedef struct nlgb_server_s* nlgb_server;
 
 #define NLGB_SERVER_BATCHED 0   /* continuous batching, persistent kernel     */
 #define NLGB_SERVER_SERIAL  1   /* one request at a time, graph-captured PCG  */
+
+/* Scheduling of the batched server.  SRPT (shortest remaining processing
+ * time, the default): `streams` CUDA streams each run one system at a time
+ * as a chunk of CUDA-graph PCG iterations lasting about epoch_ms; whenever a
+ * stream is free it takes the system with the least estimated remaining work
+ * (iterations left, extrapolated from the system's residual history, times
+ * its bytes per iteration); a new system first gets a short probe (16
+ * iterations).  A request that just arrived starts within about epoch_ms,
+ * light requests finish first, and work-heavy ones progress whenever a
+ * stream has nothing lighter to do.  ALL: epochs of the persistent batched
+ * kernel in which every active system runs epoch_iters iterations. */
+#define NLGB_SCHEDULE_SRPT 0
+#define NLGB_SCHEDULE_ALL  1
 
 typedef struct {
     size_t    hbm_budget_bytes;  /* admission limit (default 150e9)            */
@@ -195,6 +210,9 @@ typedef struct {
     double    inner_eps;         /* mixed reliable-update factor (0.1)         */
     long long epoch_iters;       /* iterations per system per epoch (256)      */
     int       max_systems;       /* active systems at once (default 8192)      */
+    int       schedule;          /* NLGB_SCHEDULE_SRPT (default) / _ALL         */
+    double    epoch_ms;          /* SRPT: target length of a chunk (10 ms)     */
+    int       streams;           /* SRPT: concurrent chunks (default 16)        */
 } nlgb_server_config;
 
 typedef struct {
@@ -214,6 +232,12 @@ typedef struct {
                                     such systems are left)                   */
     double    graph_algo_bytes;  /* part of algo_bytes: iterations run there   */
     long long graph_epochs;      /* part of epochs run as graph chunks         */
+    size_t    used_bytes;        /* device footprint admitted now              */
+    double    byte_seconds;      /* admitted footprint integrated over time
+                                    since the clock (re)started: the mean HBM
+                                    occupancy is byte_seconds / elapsed time  */
+    double    epoch_algo_bytes;  /* algorithmic bytes of every iteration run in
+                                    the epochs (finished or not)               */
 } nlgb_server_stats;
 
 void        nlgb_server_default_config(nlgb_server_config* cfg);
@@ -258,8 +282,11 @@ int         nlgb_server_wait(nlgb_server srv, long long ticket, nlgb_result* res
                              double* latency_s);
 int         nlgb_server_drain(nlgb_server srv);
 int         nlgb_server_get_stats(nlgb_server srv, nlgb_server_stats* st);
-/* Stop admitting and abort: active systems stop at the next epoch boundary
- * with NL_GB300_STATUS_ABORTED. */
+/* Stop admitting and abort: queued requests fail at once, active systems
+ * stop at the next epoch boundary (a solve running on a graph executor, e.g.
+ * the SERIAL mode's, within one while-loop pass of 4 iterations) with
+ * NL_GB300_STATUS_ABORTED; nlgb_server_wait reports those requests as
+ * failed. */
 void        nlgb_server_abort(nlgb_server srv);
 void        nlgb_server_destroy(nlgb_server srv);
 

@@ -26,6 +26,7 @@
  *   (no fused multiply-add: build with -ffp-contract=off).
  */
 #include <math.h>
+#include <time.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -218,11 +219,22 @@ static double dot(int n, const double* a, const double* b, int nthreads) {
     return s;
 }
 
+static double wall_seconds(void) {
+#ifdef _OPENMP
+    return omp_get_wtime();
+#else
+    return (double)clock() / CLOCKS_PER_SEC;
+#endif
+}
+
 /* Jacobi-preconditioned CG (jacobi != 0) or plain CG.  x: initial guess in,
- * solution out.  Returns the status: 1 converged, 2 max_iter, 3 breakdown. */
-int nlo_pcg(int n, const int* rp, const int* ci, const double* va, const double* b, double* x,
-            double eps, long long max_iter, int jacobi, int nthreads, long long* iters_out,
-            double* rel_res_out) {
+ * solution out.  Returns the status: 1 converged, 2 max_iter, 3 breakdown,
+ * 4 time limit (max_seconds > 0: checked every 16 iterations; used by the
+ * time-bounded CPU baseline). */
+int nlo_pcg_timed(int n, const int* rp, const int* ci, const double* va, const double* b, double* x,
+                  double eps, long long max_iter, int jacobi, int nthreads, double max_seconds,
+                  long long* iters_out, double* rel_res_out) {
+    const double t_start = max_seconds > 0.0 ? wall_seconds() : 0.0;
     double* r = (double*)malloc(sizeof(double) * (n > 0 ? n : 1));
     double* z = (double*)malloc(sizeof(double) * (n > 0 ? n : 1));
     double* p = (double*)malloc(sizeof(double) * (n > 0 ? n : 1));
@@ -275,6 +287,10 @@ int nlo_pcg(int n, const int* rp, const int* ci, const double* va, const double*
         ++it;
         if (rr <= eps * eps * bb) { status = 1; break; }
         if (it >= max_iter) { status = 2; break; }
+        if (max_seconds > 0.0 && (it & 15) == 0 && wall_seconds() - t_start > max_seconds) {
+            status = 4;
+            break;
+        }
         if (!(rho_new > 0.0)) { status = 3; break; }
         const double beta = rho_new / rho;
         rho = rho_new;
@@ -288,6 +304,13 @@ done:
     if (rel_res_out) *rel_res_out = bb > 0.0 ? sqrt(rr / bb) : 0.0;
     free(r); free(z); free(p); free(q); free(d);
     return status;
+}
+
+int nlo_pcg(int n, const int* rp, const int* ci, const double* va, const double* b, double* x,
+            double eps, long long max_iter, int jacobi, int nthreads, long long* iters_out,
+            double* rel_res_out) {
+    return nlo_pcg_timed(n, rp, ci, va, b, x, eps, max_iter, jacobi, nthreads, 0.0, iters_out,
+                         rel_res_out);
 }
 
 int nlo_max_threads(void) {

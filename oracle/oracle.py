@@ -62,6 +62,10 @@ def lib():
         L.nlo_pcg.argtypes = [ctypes.c_int, _c_int_p, _c_int_p, _c_dbl_p, _c_dbl_p, _c_dbl_p,
                               ctypes.c_double, ctypes.c_longlong, ctypes.c_int, ctypes.c_int,
                               _c_ll_p, _c_dbl_p]
+        L.nlo_pcg_timed.restype = ctypes.c_int
+        L.nlo_pcg_timed.argtypes = [ctypes.c_int, _c_int_p, _c_int_p, _c_dbl_p, _c_dbl_p, _c_dbl_p,
+                                    ctypes.c_double, ctypes.c_longlong, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_double, _c_ll_p, _c_dbl_p]
         L.nlo_max_threads.restype = ctypes.c_int
         _lib = L
     return _lib
@@ -148,17 +152,20 @@ def spmv(rp, ci, va, x, nthreads: int = 0):
 
 
 def pcg(rp, ci, va, b, x0=None, eps: float = 1e-10, max_iter: int | None = None,
-        jacobi: bool = True, nthreads: int = 0):
-    """FP64 (Jacobi-)PCG.  Returns (x, status, iterations, rel_residual)."""
+        jacobi: bool = True, nthreads: int = 0, max_seconds: float = 0.0):
+    """FP64 (Jacobi-)PCG.  Returns (x, status, iterations, rel_residual);
+    status 1 converged, 2 max_iter, 3 breakdown, 4 time limit (max_seconds
+    > 0)."""
     rp = np.ascontiguousarray(rp, np.int32); ci = np.ascontiguousarray(ci, np.int32)
     va = np.ascontiguousarray(va, np.float64); b = np.ascontiguousarray(b, np.float64)
     n = rp.shape[0] - 1
     x = np.zeros(n) if x0 is None else np.array(x0, np.float64, copy=True)
     it = ctypes.c_longlong()
     rr = ctypes.c_double()
-    st = lib().nlo_pcg(n, _p(rp, _c_int_p), _p(ci, _c_int_p), _p(va, _c_dbl_p), _p(b, _c_dbl_p),
-                       _p(x, _c_dbl_p), eps, 5 * n if max_iter is None else max_iter, int(jacobi),
-                       nthreads or max_threads(), ctypes.byref(it), ctypes.byref(rr))
+    st = lib().nlo_pcg_timed(n, _p(rp, _c_int_p), _p(ci, _c_int_p), _p(va, _c_dbl_p), _p(b, _c_dbl_p),
+                             _p(x, _c_dbl_p), eps, 5 * n if max_iter is None else max_iter, int(jacobi),
+                             nthreads or max_threads(), float(max_seconds), ctypes.byref(it),
+                             ctypes.byref(rr))
     return x, int(st), int(it.value), float(rr.value)
 
 

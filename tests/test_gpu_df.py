@@ -35,13 +35,17 @@ def test_df_solve_matches_oracle(gpu_ok, oracle_mod, lscm_small):
     for eps in (1e-10, 1e-12):
         x, info = M.solve(b, eps=eps, precision="df")
         x64, i64 = M.solve(b, eps=eps, precision="double")
-        assert info.status == "converged" and info.precision == "df" and info.refinement_steps == 0
+        assert info.precision == "df" and info.refinement_steps == 0
         assert i64.precision == "double"
-        # same stopping rule as FP64: the recursive residual; the true one
-        # (FP64) stays within a small factor of the threshold
+        # same stopping rule as FP64 (the recursive residual, then the true
+        # one checked in FP64 and the iteration continued while it misses);
+        # double-float's recurrence drifts further (rounding at ~2^-48), so
+        # its true residual may stall a little above eps -- the status says so
+        assert info.status in ("converged", "true_residual_stalled")
+        assert (info.status == "converged") == (info.true_rel_residual <= eps)
         assert info.rel_residual <= eps and info.true_rel_residual <= 3 * eps
-        # iterations within 25 % of FP64's (double-float rounds at ~2^-48)
-        assert abs(info.iterations - i64.iterations) <= 0.25 * i64.iterations
+        # iterations close to FP64's (the continuations add some)
+        assert abs(info.iterations - i64.iterations) <= 0.6 * i64.iterations
         if eps == 1e-12:
             assert rel(x, xd) <= 1e-8 and rel(x64, xd) <= 1e-8
 
@@ -142,6 +146,9 @@ def test_opennl_context_double_float(gpu_ok):
     xa, ia = solver.solve_opennl(rs, precision="auto", eps=1e-12)
     xf, if_ = solver.solve_opennl(rs, precision="df", eps=1e-12)
     xd, id_ = solver.solve_opennl(rs, precision="double", eps=1e-12)
-    assert if_["ok"] and if_["status"] == "converged"
+    # nlSolve succeeds when OpenNL's own rule (the recursive residual) is met;
+    # NL_GB300_STATUS tells whether the true residual met eps too
+    assert if_["ok"] and if_["status"] in ("converged", "true_residual_stalled")
+    assert (if_["status"] == "converged") == (if_["true_error"] <= 1e-12)
     assert np.array_equal(xa, xd) and ia["iterations"] == id_["iterations"]
     assert rel(xf, xd) <= 1e-8

@@ -23,8 +23,9 @@ def _submit(srv, kind, obj, arrival=-1.0):
     return srv.submit_rows(obj, arrival) if kind == "rows" else srv.submit_square(obj, arrival)
 
 
+@pytest.mark.parametrize("schedule", ["srpt", "all"])
 @pytest.mark.parametrize("precision", ["mixed", "double", "auto"])
-def test_result_same_alone_and_in_mix(gpu_ok, precision):
+def test_result_same_alone_and_in_mix(gpu_ok, precision, schedule):
     reqs = _requests()
     alone = []
     for kind, obj in reqs:
@@ -33,7 +34,10 @@ def test_result_same_alone_and_in_mix(gpu_ok, precision):
         x, infos, lat = srv.wait(t)
         alone.append((x.copy(), [i.iterations for i in infos]))
         srv.close()
-    srv = solver.Server(precision=precision, budget_bytes=2e9, epoch_iters=64)
+    # short epochs (0.5 ms time box, or 64 iterations), so that every
+    # system crosses several epoch boundaries in the mix
+    srv = solver.Server(precision=precision, budget_bytes=2e9, epoch_iters=64, schedule=schedule,
+                        epoch_ms=0.5)
     tickets = [_submit(srv, kind, obj, arrival=0.002 * i) for i, (kind, obj) in enumerate(reqs)]
     for t, (xa, ia) in zip(tickets, alone):
         x, infos, lat = srv.wait(t)
@@ -148,7 +152,7 @@ def test_lone_large_system_continues_on_graph(gpu_ok):
     assert A.n // A.tile_rows >= 384
     x1, i1 = A.solve(fs.rhs[0])
     xs, infos, _ = solver.batch_solve([A], [fs.rhs[0]])
-    srv = solver.Server(precision="double", epoch_iters=32)
+    srv = solver.Server(precision="double", epoch_iters=32, schedule="all")
     t = srv.submit_square(fs)
     x, infs, _ = srv.wait(t)
     st = srv.stats()
@@ -166,11 +170,11 @@ def test_switch_back_from_graph_when_requests_arrive(gpu_ok):
     small = systems.fairing_system(40, 37, seed=32)
     alone = []
     for kind, obj in (("rows", big), ("square", small)):
-        srv = solver.Server(precision="auto", epoch_iters=64)
+        srv = solver.Server(precision="auto", epoch_iters=64, schedule="all")
         x, infs, _ = srv.wait(_submit(srv, kind, obj))
         alone.append((x.copy(), [i.iterations for i in infs]))
         srv.close()
-    srv = solver.Server(precision="auto", epoch_iters=64)
+    srv = solver.Server(precision="auto", epoch_iters=64, schedule="all")
     t1 = _submit(srv, "rows", big, arrival=0.0)
     t2 = _submit(srv, "square", small, arrival=0.05)
     for t, (xa, ia) in zip((t1, t2), alone):
@@ -192,7 +196,7 @@ def test_large_systems_share_graph_epochs(gpu_ok):
         A = solver.Matrix(fs.rp, fs.ci, fs.va)
         assert A.n // A.tile_rows >= 384
         alone.append(A.solve(fs.rhs[0]))
-    srv = solver.Server(precision="double", epoch_iters=32)
+    srv = solver.Server(precision="double", epoch_iters=32, schedule="all")
     ta, tb = srv.submit_square(fa), srv.submit_square(fb)
     for t, (x1, i1) in zip((ta, tb), alone):
         x, infs, _ = srv.wait(t)
@@ -209,7 +213,7 @@ def test_graph_continuation_after_slot_reuse(gpu_ok):
     (stream-ordered pool); its graph chunks must run on its own matrix."""
     fa = systems.fairing_system(420, 400, seed=51, n_rhs=1)
     fb = systems.fairing_system(420, 400, seed=52, n_rhs=1, lam=3e-2)
-    srv = solver.Server(precision="double", epoch_iters=32)
+    srv = solver.Server(precision="double", epoch_iters=32, schedule="all")
     for fs in (fa, fb):
         A = solver.Matrix(fs.rp, fs.ci, fs.va)
         x1, i1 = A.solve(fs.rhs[0])
@@ -218,3 +222,51 @@ def test_graph_continuation_after_slot_reuse(gpu_ok):
         assert np.array_equal(x[0], x1)
     assert srv.stats()["graph_epochs"] >= 2
     srv.close()
+
+
+def test_srpt_serves_light_requests_first(gpu_ok):
+    """SRPT epochs: a large least-squares request submitted first does not
+    hold back light requests that arrive after it; every result is still
+    bit-identical to its solve alone."""
+    big = systems.lscm_system(260, 250, seed=61)
+    lights = [systems.fairing_system(50 + 7 * i, 45, seed=62 + i) for i in range(4)]
+    srv = solver.Server(precision="auto")
+    x_big_alone, i_big_alone, _ = srv.wait(srv.submit_rows(big))
+    alone = [srv.wait(srv.submit_square(f))[:2] for f in lights]
+    srv.close()
+    srv = solver.Server(precision="auto")
+    t_big = srv.submit_rows(big, arrival=0.0)
+    t_l = [srv.submit_square(f, arrival=0.01) for f in lights]
+    lat_l = []
+    for t, (xa, ia) in zip(t_l, alone):
+        x, infs, lat = srv.wait(t)
+        assert all(i.status == "converged" for i in infs)
+        assert [i.iterations for i in infs] == [i.iterations for i in ia]
+        assert np.array_equal(x, xa)
+        lat_l.append(lat)
+    x, infs, lat_big = srv.wait(t_big)
+    srv.close()
+    assert infs[0].iterations == i_big_alone[0].iterations and np.array_equal(x, x_big_alone)
+    assert max(lat_l) < lat_big
+
+
+def test_srpt_chunks_follow_their_target_length(gpu_ok, tmp_path, monkeypatch):
+    """SRPT executor: after a system's 16-iteration probe, its chunks are
+    sized from its measured time per iteration to last about epoch_ms
+    (trace of the chunks, NLGB_SERVER_TRACE)."""
+    trace = tmp_path / "trace.csv"
+    monkeypatch.setenv("NLGB_SERVER_TRACE", str(trace))
+    reqs = [systems.lscm_system(120 + 3 * i, 110, seed=71 + i) for i in range(6)]
+    srv = solver.Server(precision="double", epoch_ms=5.0)
+    tickets = [srv.submit_rows(r) for r in reqs]
+    for t in tickets:
+        x, infs, _ = srv.wait(t)
+        assert infs[0].status == "converged"
+    srv.close()
+    rows = [l.split(",") for l in trace.read_text().splitlines() if l.startswith("C,")]
+    iters = np.array([int(r[6]) - int(r[5]) for r in rows])
+    ms = np.array([float(r[7]) for r in rows])
+    assert (iters <= 16).sum() >= len(reqs)                 # one probe per system
+    long_ = ms[iters > 16]
+    assert len(long_) >= 6
+    assert 1.0 <= float(np.median(long_)) <= 15.0, ms
