@@ -471,9 +471,9 @@ cudaError_t assemble_normal_equations(const LSRowsDevice& R, DeviceCRS& out, dou
   }
   crs_free(out);
   out.n = nf; out.m = nf; out.nnz = nnz;
-  NLGB_CUDA_TRY(cudaMalloc(&out.rp, sizeof(int) * (nf + 1)));
-  NLGB_CUDA_TRY(cudaMalloc(&out.ci, sizeof(int) * std::max(1LL, nnz)));
-  NLGB_CUDA_TRY(cudaMalloc(&out.va, sizeof(double) * std::max(1LL, nnz)));
+  NLGB_CUDA_TRY(cudaMallocAsync(&out.rp, sizeof(int) * (nf + 1), s));
+  NLGB_CUDA_TRY(cudaMallocAsync(&out.ci, sizeof(int) * std::max(1LL, nnz), s));
+  NLGB_CUDA_TRY(cudaMallocAsync(&out.va, sizeof(double) * std::max(1LL, nnz), s));
   k_to_int<<<blocks_for(nf + 1), 256, 0, s>>>(rp64.p, out.rp, nf + 1);
   count_launches(1);
   NLGB_CUDA_TRY(cudaGetLastError());
@@ -535,9 +535,9 @@ cudaError_t assemble_square(const LSRowsDevice& R, DeviceCRS& out, double* rhs_o
   }
   crs_free(out);
   out.n = (int)n; out.m = (int)n; out.nnz = nnz;
-  NLGB_CUDA_TRY(cudaMalloc(&out.rp, sizeof(int) * (n + 1)));
-  NLGB_CUDA_TRY(cudaMalloc(&out.ci, sizeof(int) * std::max(1LL, nnz)));
-  NLGB_CUDA_TRY(cudaMalloc(&out.va, sizeof(double) * std::max(1LL, nnz)));
+  NLGB_CUDA_TRY(cudaMallocAsync(&out.rp, sizeof(int) * (n + 1), s));
+  NLGB_CUDA_TRY(cudaMallocAsync(&out.ci, sizeof(int) * std::max(1LL, nnz), s));
+  NLGB_CUDA_TRY(cudaMallocAsync(&out.va, sizeof(double) * std::max(1LL, nnz), s));
   k_to_int<<<blocks_for(n + 1), 256, 0, s>>>(rp64.p, out.rp, n + 1);
   count_launches(1);
   if (n > 0) {

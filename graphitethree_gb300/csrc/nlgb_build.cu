@@ -163,13 +163,15 @@ struct DevBuf {
 // Device copies of the mesh (the caller's arrays may be host or device) and
 // the triangle-index check.
 cudaError_t mesh_to_device(int n_verts, const double* xyz, int n_tris, const int* tris, DevBuf& dx,
-                           DevBuf& dt, cudaStream_t s, bool* bad_index) {
+                           DevBuf& dt, cudaStream_t s, bool* bad_index, bool check) {
   NLGB_CUDA_TRY(dx.alloc<double>(3 * (size_t)n_verts, s));
   NLGB_CUDA_TRY(dt.alloc<int>(3 * (size_t)n_tris, s));
   if (n_verts > 0)
     NLGB_CUDA_TRY(cudaMemcpyAsync(dx.p, xyz, sizeof(double) * 3 * (size_t)n_verts, cudaMemcpyDefault, s));
   if (n_tris > 0)
     NLGB_CUDA_TRY(cudaMemcpyAsync(dt.p, tris, sizeof(int) * 3 * (size_t)n_tris, cudaMemcpyDefault, s));
+  *bad_index = false;
+  if (!check) return cudaSuccess;
   DevBuf flag;
   NLGB_CUDA_TRY(flag.alloc<int>(1, s));
   NLGB_CUDA_TRY(cudaMemsetAsync(flag.p, 0, sizeof(int), s));
@@ -189,10 +191,10 @@ cudaError_t mesh_to_device(int n_verts, const double* xyz, int n_tris, const int
 
 cudaError_t build_lscm_system(int n_verts, const double* xyz, int n_tris, const int* tris,
                               const int pins[2], const double pin_uv[4], DeviceCRS& out,
-                              double* rhs_out, cudaStream_t s, bool* bad_input) {
+                              double* rhs_out, cudaStream_t s, bool* bad_input, bool check_indices) {
   *bad_input = false;
   DevBuf dx, dt;
-  NLGB_CUDA_TRY(mesh_to_device(n_verts, xyz, n_tris, tris, dx, dt, s, bad_input));
+  NLGB_CUDA_TRY(mesh_to_device(n_verts, xyz, n_tris, tris, dx, dt, s, bad_input, check_indices));
   if (*bad_input) return cudaSuccess;
   const int p0 = std::min(pins[0], pins[1]), p1 = std::max(pins[0], pins[1]);
   const double* uv0 = pins[0] <= pins[1] ? pin_uv : pin_uv + 2;
@@ -224,10 +226,11 @@ cudaError_t build_lscm_system(int n_verts, const double* xyz, int n_tris, const 
 }
 
 cudaError_t build_fairing_system(int n_verts, const double* xyz, int n_tris, const int* tris,
-                                 double lambda, DeviceCRS& out, cudaStream_t s, bool* bad_input) {
+                                 double lambda, DeviceCRS& out, cudaStream_t s, bool* bad_input,
+                                 bool check_indices) {
   *bad_input = false;
   DevBuf dx, dt;
-  NLGB_CUDA_TRY(mesh_to_device(n_verts, xyz, n_tris, tris, dx, dt, s, bad_input));
+  NLGB_CUDA_TRY(mesh_to_device(n_verts, xyz, n_tris, tris, dx, dt, s, bad_input, check_indices));
   if (*bad_input) return cudaSuccess;
   const long long n_edge_rows = 3LL * n_tris, n_rows = n_edge_rows + n_verts;
   const long long n_coefs = 2 * n_edge_rows + n_verts;

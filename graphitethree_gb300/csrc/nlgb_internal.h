@@ -54,6 +54,11 @@ cudaError_t crs_upload(DeviceCRS& A, int n, int m, const int* rp, const int* ci,
 cudaError_t crs_adopt_device(DeviceCRS& A, int n, int m, long long nnz, int* rp, int* ci,
                              double* va, cudaStream_t s);
 void crs_free(DeviceCRS& A);
+// Stream-ordered release (no device-wide synchronisation): the arrays are
+// freed when stream s reaches this point; work of other streams that used
+// them must have completed.  The arrays of a DeviceCRS come from
+// cudaMallocAsync (the device's default pool).
+void crs_free_async(DeviceCRS& A, cudaStream_t s);
 cudaError_t crs_prepare(DeviceCRS& A, bool need_fp32, cudaStream_t s);  // jacobi, fp32, tuning
 // crs_prepare plus the double-float copies; *usable is false (and no copy is
 // made) when a value or 1/diagonal lies outside [2^-100, 2^100] or is not
@@ -175,12 +180,15 @@ cudaError_t assemble_square(const LSRowsDevice& rows, DeviceCRS& out, double* rh
 // Mesh system builders (nlgb_build.cu).  Vertices xyz (n_verts x 3) and
 // triangles (n_tris x 3) may be host or device arrays; *bad_input is set
 // (and nothing built) when a triangle index is out of range.
+// check_indices = false: the caller validated the triangle indices on the
+// host (no device check, one host synchronisation less).
 cudaError_t build_lscm_system(int n_verts, const double* xyz, int n_tris, const int* tris,
                               const int pins[2], const double pin_uv[4], DeviceCRS& out,
                               double* rhs_out /* 2 n_verts - 4, device */, cudaStream_t s,
-                              bool* bad_input);
+                              bool* bad_input, bool check_indices = true);
 cudaError_t build_fairing_system(int n_verts, const double* xyz, int n_tris, const int* tris,
-                                 double lambda, DeviceCRS& out, cudaStream_t s, bool* bad_input);
+                                 double lambda, DeviceCRS& out, cudaStream_t s, bool* bad_input,
+                                 bool check_indices = true);
 
 // Krylov solvers for general square systems (nlgb_krylov.cu): BiCGSTAB and
 // restarted GMRES(restart), FP64, right preconditioning by dinv (Jacobi; all

@@ -154,8 +154,9 @@ struct nlgb_server_s {
   std::vector<Req*> future, pending, active;
   std::deque<Req*> admitted;
   std::condition_variable cv_admit;   // wakes the admission thread
-  std::thread adm_th;
-  bool admitter_done = false;
+  std::vector<std::thread> adm_th;
+  int admitters_live = 0;
+  bool admitter_done = false;         // every admission thread has exited
   long long sys_in_flight = 0;        // systems admitted or being admitted (guarded by mu)
   size_t used = 0;
   // statistics (guarded by mu)
@@ -221,6 +222,7 @@ constexpr double kServiceFloorBytes = 1.6e5;
 constexpr long long kProbeIters = 16;      // SRPT: first epoch of a new system
 constexpr int kReserveCtas = 16;           // persistent-kernel slots left to system builds
 constexpr long long kUnrollPlainIters = 4;  // a chunk pauses on whole passes of 4 iterations
+constexpr int kAdmitters = 2;               // admission threads of the batched server
 double iteration_cost(const Req& r, bool mixed) {
   const double n = double(r.A.n), z = double(r.A.nnz);
   const double b = mixed ? 8.0 * z + 56.0 * n : 12.0 * z + 108.0 * n;
@@ -251,13 +253,14 @@ bool admit(nlgb_server_s* S, Req* r, cudaStream_t s, bool df_slots) {
     // build the system from the mesh on the GPU (right-hand sides: LSCM's
     // from the pins, fairing's given by the caller)
     bool bad = false;
-    e = cudaMalloc(&r->d_rhs, sizeof(double) * std::max<size_t>(1, (size_t)r->n_rhs * r->n));
+    e = cudaMallocAsync((void**)&r->d_rhs, sizeof(double) * std::max<size_t>(1, (size_t)r->n_rhs * r->n), s);
     if (e == cudaSuccess && r->mesh_kind == NLGB_MESH_LSCM) {
+      // (triangle indices were checked on the host at submission)
       e = build_lscm_system(r->n_verts, r->xyz.data(), r->n_tris, r->tris.data(), r->pins, r->pin_uv,
-                            r->A, r->d_rhs, s, &bad);
+                            r->A, r->d_rhs, s, &bad, false);
     } else if (e == cudaSuccess) {
       e = build_fairing_system(r->n_verts, r->xyz.data(), r->n_tris, r->tris.data(), r->lambda, r->A, s,
-                               &bad);
+                               &bad, false);
       if (e == cudaSuccess)
         e = cudaMemcpyAsync(r->d_rhs, r->b.data(), sizeof(double) * (size_t)r->n_rhs * r->n,
                             cudaMemcpyHostToDevice, s);
@@ -282,7 +285,8 @@ bool admit(nlgb_server_s* S, Req* r, cudaStream_t s, bool df_slots) {
     if (r->has_weight) up((void**)&dw, r->weight.data(), sizeof(double) * r->weight.size());
     if (r->has_xl) up((void**)&dxl, r->xl.data(), sizeof(double) * r->xl.size());
     else up((void**)&dxl, nullptr, 0);
-    if (e == cudaSuccess) e = cudaMalloc(&r->d_rhs, sizeof(double) * std::max<size_t>(1, (size_t)r->n_rhs * r->n));
+    if (e == cudaSuccess)
+      e = cudaMallocAsync((void**)&r->d_rhs, sizeof(double) * std::max<size_t>(1, (size_t)r->n_rhs * r->n), s);
     if (e == cudaSuccess) {
       LSRowsDevice R;
       R.n_rows = r->n_rows; R.n_coefs = nc; R.n_free = r->n; R.n_vars = r->n_vars;
@@ -342,12 +346,14 @@ bool admit(nlgb_server_s* S, Req* r, cudaStream_t s, bool df_slots) {
   return true;
 }
 
+// Stream-ordered release of a request's device memory (no device-wide
+// synchronisation: the solver's other streams keep running).
 void release(nlgb_server_s* S, Req* r, cudaStream_t s) {
   for (auto& sl : r->slots) sl.release(s);
   r->slots.clear();
-  cudaStreamSynchronize(s);
-  crs_free(r->A);
-  cudaFree(r->d_rhs);
+  r->graphs.clear();
+  crs_free_async(r->A, s);
+  if (r->d_rhs) cudaFreeAsync(r->d_rhs, s);
   r->d_rhs = nullptr;
   add_used(S, -(long long)r->bytes);
   r->bytes = 0;
@@ -485,8 +491,13 @@ double estimate_left(Req* r, int k, const SysState& h) {
 // requests join the next epoch.
 void admitter(nlgb_server_s* S) {
   cudaSetDevice(S->device);
+  // Builds run at the highest stream priority: their kernels are short and
+  // the solver's streams keep the GPU busy; at the default priority every
+  // host synchronisation of a build would wait behind queued solver work.
+  int least = 0, greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&least, &greatest);
   cudaStream_t su = nullptr;
-  cudaStreamCreateWithFlags(&su, cudaStreamNonBlocking);
+  cudaStreamCreateWithPriority(&su, cudaStreamNonBlocking, greatest);
   std::unique_lock<std::mutex> lk(S->mu);
   for (;;) {
     while (!S->incoming.empty()) {
@@ -535,6 +546,7 @@ void admitter(nlgb_server_s* S) {
       lk.unlock();
       const double ta = S->now();
       bool ok = admit(S, pick, su, true);
+      const double tg = S->now();
       if (ok && S->cfg.schedule == NLGB_SCHEDULE_SRPT) {
         // instantiate the chunk graphs here, off the worker's path
         pick->graphs.resize((size_t)pick->n_rhs);
@@ -546,8 +558,8 @@ void admitter(nlgb_server_s* S) {
       }
       const double tb = S->now();
       if (S->trace)
-        std::fprintf(S->trace, "A,%.6f,%lld,%d,%d,%.6f,%zu,%.6f\n", ta, pick->id,
-                     pick->kind == 2 ? pick->mesh_kind : -1, pick->n, tb - ta, pick->bytes, pick->arrival);
+        std::fprintf(S->trace, "A,%.6f,%lld,%d,%d,%.6f,%zu,%.6f,%.6f\n", ta, pick->id,
+                     pick->kind == 2 ? pick->mesh_kind : -1, pick->n, tb - ta, pick->bytes, pick->arrival, tb - tg);
       if (!ok) {
         release(S, pick, su);
         {
@@ -570,8 +582,9 @@ void admitter(nlgb_server_s* S) {
     if (!S->future.empty()) wait_s = std::min(wait_s, std::max(0.0, S->future.front()->arrival - S->now()));
     S->cv_admit.wait_for(lk, std::chrono::duration<double>(wait_s));
   }
-  S->admitter_done = true;
+  if (--S->admitters_live == 0) S->admitter_done = true;
   S->cv_work.notify_all();
+  S->cv_admit.notify_all();
   lk.unlock();
   cudaStreamSynchronize(su);
   cudaStreamDestroy(su);
@@ -828,8 +841,10 @@ void worker_streams(nlgb_server_s* S) {
     float ms = 0.f;
   };
   std::vector<Lane> lanes((size_t)ns);
-  cudaStream_t su = nullptr;
-  cudaStreamCreateWithFlags(&su, cudaStreamNonBlocking);
+  int least = 0, greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  cudaStream_t su = nullptr;   // result downloads and releases: ahead of the chunks
+  cudaStreamCreateWithPriority(&su, cudaStreamNonBlocking, greatest);
   bool init_ok = true;
   for (Lane& l : lanes)
     init_ok = init_ok && cudaStreamCreateWithFlags(&l.s, cudaStreamNonBlocking) == cudaSuccess &&
@@ -1171,6 +1186,15 @@ nlgb_server nlgb_server_create(const nlgb_server_config* cfg) {
   }
   S->st.budget_bytes = S->cfg.hbm_budget_bytes;
   cudaGetDevice(&S->device);
+  // Requests allocate and free their device memory stream-ordered from the
+  // device's default pool; keeping freed memory in the pool makes the next
+  // request's allocations cheap.
+  cudaMemPool_t pool = nullptr;
+  if (cudaDeviceGetDefaultMemPool(&pool, S->device) == cudaSuccess) {
+    unsigned long long keep = ~0ULL;   // release threshold: never trim
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  cudaGetLastError();
   void* flag = nullptr;
   if (cudaHostAlloc(&flag, sizeof(int), cudaHostAllocMapped) != cudaSuccess ||
       cudaHostGetDevicePointer((void**)&S->abort_dev, flag, 0) != cudaSuccess) {
@@ -1187,14 +1211,18 @@ nlgb_server nlgb_server_create(const nlgb_server_config* cfg) {
       std::fprintf(S->trace, "# E,t0,t1,kind,systems,teams,team_ctas,queue_ctas,grid,planned_GB,done_GB,ms,"
                              "team_ms_min,team_ms_med,team_ms_max,queue_ms,admits,admit_s,active_requests\n"
                              "# C,t,request,rhs,mixed,iter_before,iter_after,ms,status,stage\n"
-                             "# A,t,request,mesh_kind,n,seconds,bytes,arrival\n");
+                             "# A,t,request,mesh_kind,n,seconds,bytes,arrival,graph_seconds\n");
   }
   S->origin = Clock::now();
   S->th = std::thread(S->cfg.mode == NLGB_SERVER_SERIAL
                           ? worker_serial
                           : (S->cfg.schedule == NLGB_SCHEDULE_SRPT ? worker_streams : worker_batched),
                       S);
-  if (S->cfg.mode != NLGB_SERVER_SERIAL) S->adm_th = std::thread(admitter, S);
+  if (S->cfg.mode != NLGB_SERVER_SERIAL) {
+    // two admission threads: a request's upload and build overlap another's
+    S->admitters_live = kAdmitters;
+    for (int i = 0; i < kAdmitters; ++i) S->adm_th.emplace_back(admitter, S);
+  }
   return S;
 }
 
@@ -1383,7 +1411,8 @@ void nlgb_server_destroy(nlgb_server S) {
     S->cv_admit.notify_all();
   }
   if (S->th.joinable()) S->th.join();
-  if (S->adm_th.joinable()) S->adm_th.join();
+  for (std::thread& t : S->adm_th)
+    if (t.joinable()) t.join();
   if (S->abort_host) cudaFreeHost(const_cast<int*>(S->abort_host));
   if (S->trace) std::fclose(S->trace);
   delete S;

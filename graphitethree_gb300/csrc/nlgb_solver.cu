@@ -712,9 +712,9 @@ cudaError_t crs_upload(DeviceCRS& A, int n, int m, const int* rp, const int* ci,
   crs_free(A);
   const long long nnz = rp[n];
   A.n = n; A.m = m; A.nnz = nnz;
-  NLGB_CUDA_TRY(cudaMalloc(&A.rp, (size_t)(n + 1) * sizeof(int)));
-  NLGB_CUDA_TRY(cudaMalloc(&A.ci, (size_t)std::max(1LL, nnz) * sizeof(int)));
-  NLGB_CUDA_TRY(cudaMalloc(&A.va, (size_t)std::max(1LL, nnz) * sizeof(double)));
+  NLGB_CUDA_TRY(cudaMallocAsync(&A.rp, (size_t)(n + 1) * sizeof(int), s));
+  NLGB_CUDA_TRY(cudaMallocAsync(&A.ci, (size_t)std::max(1LL, nnz) * sizeof(int), s));
+  NLGB_CUDA_TRY(cudaMallocAsync(&A.va, (size_t)std::max(1LL, nnz) * sizeof(double), s));
   NLGB_CUDA_TRY(cudaMemcpyAsync(A.rp, rp, (size_t)(n + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
   if (nnz > 0) {
     NLGB_CUDA_TRY(cudaMemcpyAsync(A.ci, ci, (size_t)nnz * sizeof(int), cudaMemcpyHostToDevice, s));
@@ -735,6 +735,14 @@ void crs_free(DeviceCRS& A) {
   cudaFree(A.rp); cudaFree(A.ci); cudaFree(A.va); cudaFree(A.va32);
   cudaFree(A.dinv); cudaFree(A.dinv32);
   cudaFree(A.vadf); cudaFree(A.dinvdf);
+  A = DeviceCRS();
+}
+
+void crs_free_async(DeviceCRS& A, cudaStream_t s) {
+  if (!A.owns) { A = DeviceCRS(); return; }
+  for (void* p : {(void*)A.rp, (void*)A.ci, (void*)A.va, (void*)A.va32, (void*)A.dinv, (void*)A.dinv32,
+                  (void*)A.vadf, (void*)A.dinvdf})
+    if (p) cudaFreeAsync(p, s);
   A = DeviceCRS();
 }
 
@@ -759,8 +767,8 @@ cudaError_t crs_prepare(DeviceCRS& A, bool need_fp32, cudaStream_t s) {
     A.tile_rows = c.tile_rows;
   }
   if (!A.dinv) {
-    NLGB_CUDA_TRY(cudaMalloc(&A.dinv, (size_t)std::max(1, A.n) * sizeof(double)));
-    NLGB_CUDA_TRY(cudaMalloc(&A.dinv32, (size_t)std::max(1, A.n) * sizeof(float)));
+    NLGB_CUDA_TRY(cudaMallocAsync(&A.dinv, (size_t)std::max(1, A.n) * sizeof(double), s));
+    NLGB_CUDA_TRY(cudaMallocAsync(&A.dinv32, (size_t)std::max(1, A.n) * sizeof(float), s));
     if (A.n > 0) {
       k_jacobi<<<(A.n + 255) / 256, 256, 0, s>>>(A.n, A.rp, A.ci, A.va, A.dinv, A.dinv32);
       count_launches(1);
@@ -768,7 +776,7 @@ cudaError_t crs_prepare(DeviceCRS& A, bool need_fp32, cudaStream_t s) {
     NLGB_CUDA_TRY(cudaGetLastError());
   }
   if (need_fp32 && !A.va32) {
-    NLGB_CUDA_TRY(cudaMalloc(&A.va32, (size_t)std::max(1LL, A.nnz) * sizeof(float)));
+    NLGB_CUDA_TRY(cudaMallocAsync(&A.va32, (size_t)std::max(1LL, A.nnz) * sizeof(float), s));
     if (A.nnz > 0) {
       k_to_f32<<<grid_for(A.nnz, 256), 256, 0, s>>>(A.nnz, A.va, A.va32);
       count_launches(1);
@@ -809,8 +817,8 @@ cudaError_t crs_prepare_df(DeviceCRS& A, bool* usable, cudaStream_t s) {
     A.df_state = ok ? 1 : -1;
   }
   if (A.df_state > 0 && !A.vadf) {
-    NLGB_CUDA_TRY(cudaMalloc(&A.vadf, (size_t)std::max(1LL, A.nnz) * sizeof(float2)));
-    NLGB_CUDA_TRY(cudaMalloc(&A.dinvdf, (size_t)std::max(1, A.n) * sizeof(float2)));
+    NLGB_CUDA_TRY(cudaMallocAsync(&A.vadf, (size_t)std::max(1LL, A.nnz) * sizeof(float2), s));
+    NLGB_CUDA_TRY(cudaMallocAsync(&A.dinvdf, (size_t)std::max(1, A.n) * sizeof(float2), s));
     if (A.nnz > 0) {
       k_to_df<<<grid_for(A.nnz, 256), 256, 0, s>>>(A.nnz, A.va, A.vadf);
       count_launches(1);
