@@ -23,7 +23,7 @@ LIB_NAME = "libnl_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["nlgb_solver.cu", "nlgb_assembly.cu", "nlgb_blas.cu", "nlgb_batch.cu",
-              "nlgb_noalloc.cu", "nlgb_build.cu", "nlgb_krylov.cu"]
+              "nlgb_noalloc.cu", "nlgb_build.cu", "nlgb_krylov.cu", "nlgb_ssor.cu"]
 CPP_SOURCES = ["nl_api.cpp", "nl_matrix_api.cpp", "nlgb_api.cpp", "nlgb_server.cpp"]
 
 

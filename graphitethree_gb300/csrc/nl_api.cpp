@@ -708,14 +708,22 @@ void nlRowScaling(NLdouble value) {
 }
 
 // NL_BICGSTAB / NL_GMRES: general (non-symmetric) square systems, FP64,
-// Jacobi or no right preconditioning (nlgb_krylov.cu).
+// Jacobi, SSOR or no right preconditioning (nlgb_krylov.cu); and NL_CG with
+// the SSOR preconditioner (nlgb_ssor.cu).
 static NLboolean solve_krylov(Context* c) {
   const int nf = c->n_free();
   const int k = c->nb_systems;
   cudaStream_t s = api_stream();
   double* ones = nullptr;
   const double* dinv = c->A.dinv;
-  if (c->precond == NL_PRECOND_NONE) {
+  SsorPrecond ssor;
+  const bool use_ssor = c->precond == NL_PRECOND_SSOR;
+  if (use_ssor && ssor.build(c->A, c->omega, s) != cudaSuccess) {
+    nl_error(NL_DEVICE_ERROR, std::string("nlSolve: SSOR preconditioner: ") + last_error());
+    c->status = NL_GB300_STATUS_DEVICE_ERR;
+    return NL_FALSE;
+  }
+  if (c->precond == NL_PRECOND_NONE || use_ssor) {
     std::vector<double> h((size_t)std::max(1, nf), 1.0);
     if (cudaMalloc(&ones, sizeof(double) * h.size()) != cudaSuccess ||
         cudaMemcpy(ones, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -726,7 +734,9 @@ static NLboolean solve_krylov(Context* c) {
     }
     dinv = ones;
   }
-  const int method = c->solver == NL_BICGSTAB ? KRYLOV_BICGSTAB : KRYLOV_GMRES;
+  const int method = c->solver == NL_BICGSTAB ? KRYLOV_BICGSTAB
+                   : c->solver == NL_GMRES  ? KRYLOV_GMRES
+                                            : 0;   // CG (with SSOR)
   const long long max_iter = c->max_iterations >= 0 ? c->max_iterations : 5LL * nf;
   bool ok = true;
   long long iters = 0;
@@ -738,9 +748,11 @@ static NLboolean solve_krylov(Context* c) {
     for (int f = 0; f < nf; ++f) xf[f] = c->values[(size_t)sys * c->nb_variables + c->free_vars[f]];
     KrylovResult kr;
     cudaError_t e = cudaMemcpyAsync(c->d_x, xf.data(), sizeof(double) * nf, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess)
+    if (e == cudaSuccess && method == 0)
+      e = pcg_ssor(c->A, ssor, c->d_rhs + (size_t)sys * nf, c->d_x, c->threshold, max_iter, s, &kr);
+    else if (e == cudaSuccess)
       e = krylov_solve(c->A, dinv, c->d_rhs + (size_t)sys * nf, c->d_x, method, c->threshold, max_iter,
-                       c->inner_iterations, s, &kr);
+                       c->inner_iterations, s, &kr, use_ssor ? &ssor : nullptr);
     if (e == cudaSuccess) e = cudaMemcpyAsync(xf.data(), c->d_x, sizeof(double) * nf, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
@@ -753,7 +765,10 @@ static NLboolean solve_krylov(Context* c) {
     iters += kr.iterations;
     err = std::max(err, kr.rel_residual);
     terr = std::max(terr, kr.true_rel_residual);
-    if (kr.status != NL_GB300_STATUS_CONVERGED) { ok = false; worst = kr.status; }
+    if (kr.status != NL_GB300_STATUS_CONVERGED) {
+      worst = kr.status;
+      if (kr.status != NL_GB300_STATUS_TRUE_RESIDUAL_STALLED) ok = false;
+    }
   }
   cudaFree(ones);
   c->used_iterations = iters;
@@ -775,16 +790,12 @@ NLboolean nlSolve(void) {
     return NL_FALSE;
   }
   c->status = NL_GB300_STATUS_NONE;
-  if (c->precond == NL_PRECOND_SSOR) {
-    nl_error(NL_INVALID_OPERATION, "nlSolve: NL_PRECOND_SSOR is not built; use NL_PRECOND_JACOBI");
-    c->status = NL_GB300_STATUS_BAD_INPUT;
-    return NL_FALSE;
-  }
   if (!c->assembled && !assemble(c)) { c->status = NL_GB300_STATUS_DEVICE_ERR; return NL_FALSE; }
   const int nf = c->n_free();
   const int k = c->nb_systems;
   cudaStream_t s = api_stream();
-  if (c->solver == NL_BICGSTAB || c->solver == NL_GMRES) return solve_krylov(c);
+  if (c->solver == NL_BICGSTAB || c->solver == NL_GMRES || c->precond == NL_PRECOND_SSOR)
+    return solve_krylov(c);
   if (!c->pcg_bound) {
     if (c->precond == NL_PRECOND_NONE) {
       // Identity preconditioner: CG on the same matrix with D^-1 = 1.

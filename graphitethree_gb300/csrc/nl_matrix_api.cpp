@@ -5,10 +5,10 @@
 // nlSparseMatrixAdd, compressed to CRS by nlMatrixCompress, multiplied by
 // nlMultMatrixVector and solved by nlSolveSystemIterative(nlHostBlas(), M, P,
 // b, x, NL_CG, eps, max_iter, inner_iter).  Every product and solve runs on
-// the GPU; host vectors are staged through device buffers.  Direct solvers
-// (nlMatrixFactorize) and SSOR are not built and report NULL, which the
-// reference wrapper already handles ("Could not factorize matrix",
-// matrix.cpp:331).
+// the GPU; host vectors are staged through device buffers.  Preconditioners:
+// Jacobi and SSOR (level-scheduled sweeps, nlgb_ssor.cu).  Direct solvers
+// (nlMatrixFactorize) are not built and report NULL, which the reference
+// wrapper already handles ("Could not factorize matrix", matrix.cpp:331).
 #include "../../include/nl.h"
 #include "nlgb_internal.h"
 
@@ -24,7 +24,7 @@ using namespace nlgb;
 
 namespace {
 
-enum Kind { K_DYNAMIC = 1, K_CRS = 2, K_JACOBI = 3 };
+enum Kind { K_DYNAMIC = 1, K_CRS = 2, K_JACOBI = 3, K_SSOR = 4 };
 
 // Standard-layout objects: the public NLMatrixStruct header comes first so
 // an NLMatrix handle points at it (matrix.cpp reads m, n and type directly).
@@ -45,6 +45,10 @@ struct LibMatrix {
   double* dinv;
   double* ones;     // identity-preconditioner diagonal, built on demand
   float* ones32;
+  // SSOR: the sweeps' data, built on the device copy of the matrix it was
+  // created from (which must outlive it)
+  SsorPrecond* ssor;
+  DeviceCRS* ssor_base;
 };
 
 void destroy_matrix(NLMatrix M);
@@ -63,6 +67,7 @@ LibMatrix* new_matrix(NLuint m, NLuint n, int kind, NLenum type) {
   L->rp = nullptr; L->ci = nullptr; L->va = nullptr;
   L->dev = nullptr; L->dev_valid = false;
   L->dinv = nullptr; L->ones = nullptr; L->ones32 = nullptr;
+  L->ssor = nullptr; L->ssor_base = nullptr;
   return L;
 }
 
@@ -73,6 +78,7 @@ void destroy_matrix(NLMatrix M) {
   delete L->rp; delete L->ci; delete L->va;
   if (L->dev) { crs_free(*L->dev); delete L->dev; }
   cudaFree(L->dinv); cudaFree(L->ones); cudaFree(L->ones32);
+  delete L->ssor;
   delete L;
 }
 
@@ -200,6 +206,15 @@ void nlMultMatrixVector(NLMatrix M, const double* x, double* y) {
   LibMatrix* L = (LibMatrix*)M;
   if (!L) { report("nlMultMatrixVector: null matrix"); return; }
   cudaStream_t s = api_stream();
+  if (L->kind == K_SSOR) {
+    // the preconditioner as a matrix: y = M^-1 x
+    Staged sx, sy;
+    if (!sx.in(x, L->pub.n, s) || !sy.in(y, L->pub.n, s)) { report("nlMultMatrixVector: staging failed"); return; }
+    if (L->ssor->apply(sx.d, sy.d, s) != cudaSuccess) report(last_error());
+    sy.out(y, L->pub.n, s);
+    cudaStreamSynchronize(s);
+    return;
+  }
   if (L->kind == K_JACOBI) {
     Staged sx, sy;
     if (!sx.in(x, L->pub.n, s) || !sy.in(y, L->pub.n, s)) { report("nlMultMatrixVector: staging failed"); return; }
@@ -241,9 +256,26 @@ NLMatrix nlNewJacobiPreconditioner(NLMatrix M) {
   return (NLMatrix)P;
 }
 
-NLMatrix nlNewSSORPreconditioner(NLMatrix, double) {
-  report("nlNewSSORPreconditioner: SSOR is not built for the GPU path (use Jacobi)");
-  return nullptr;
+NLMatrix nlNewSSORPreconditioner(NLMatrix M, double omega) {
+  LibMatrix* L = (LibMatrix*)M;
+  if (!L || (L->kind != K_DYNAMIC && L->kind != K_CRS) || L->pub.m != L->pub.n) {
+    report("nlNewSSORPreconditioner: needs a square sparse matrix");
+    return nullptr;
+  }
+  if (!(omega > 0.0 && omega < 2.0)) {
+    report("nlNewSSORPreconditioner: omega must be in (0, 2)");
+    return nullptr;
+  }
+  if (!ensure_device(L, false)) return nullptr;
+  LibMatrix* P = new_matrix(L->pub.m, L->pub.n, K_SSOR, NL_MATRIX_OTHER);
+  P->ssor = new SsorPrecond();
+  P->ssor_base = L->dev;
+  if (P->ssor->build(*L->dev, omega, api_stream()) != cudaSuccess) {
+    report(last_error());
+    destroy_matrix((NLMatrix)P);
+    return nullptr;
+  }
+  return (NLMatrix)P;
 }
 
 NLMatrix nlMatrixFactorize(NLMatrix, NLenum) {
@@ -263,16 +295,21 @@ NLuint nlSolveSystemIterative(NLBlas_t, NLMatrix M, NLMatrix P, const double* b,
     return 0;
   }
   LibMatrix* PL = (LibMatrix*)P;
-  if (PL && PL->kind != K_JACOBI) {
-    report("nlSolveSystemIterative: only a Jacobi preconditioner (or NULL) is supported");
+  if (PL && PL->kind != K_JACOBI && PL->kind != K_SSOR) {
+    report("nlSolveSystemIterative: the preconditioner must be Jacobi, SSOR or NULL");
     return 0;
   }
   if (!ensure_device(L, false)) { report(last_error()); return 0; }
+  if (PL && PL->kind == K_SSOR && (PL->ssor_base != L->dev || PL->pub.n != L->pub.n)) {
+    report("nlSolveSystemIterative: the SSOR preconditioner was built for another matrix");
+    return 0;
+  }
   cudaStream_t s = api_stream();
   const NLuint n = L->pub.n;
   DeviceCRS view = *L->dev;   // shallow view with the requested preconditioner
   view.owns = false;
-  if (PL) {
+  SsorPrecond* ssor = (PL && PL->kind == K_SSOR) ? PL->ssor : nullptr;
+  if (PL && !ssor) {
     view.dinv = PL->dinv;
   } else {
     if (!L->ones) {
@@ -292,7 +329,17 @@ NLuint nlSolveSystemIterative(NLBlas_t, NLMatrix M, NLMatrix P, const double* b,
     // general square systems; inner_iter is GMRES's restart length
     KrylovResult kr;
     if (krylov_solve(*L->dev, view.dinv, sb.d, sx.d, solver == NL_BICGSTAB ? KRYLOV_BICGSTAB : KRYLOV_GMRES,
-                     eps, max_iter, std::max<NLuint>(1, inner_iter), s, &kr) != cudaSuccess) {
+                     eps, max_iter, std::max<NLuint>(1, inner_iter), s, &kr, ssor) != cudaSuccess) {
+      report(last_error());
+      return 0;
+    }
+    sx.out(x, n, s);
+    cudaStreamSynchronize(s);
+    return (NLuint)kr.iterations;
+  }
+  if (ssor) {
+    KrylovResult kr;
+    if (pcg_ssor(*L->dev, *ssor, sb.d, sx.d, eps, max_iter, s, &kr) != cudaSuccess) {
       report(last_error());
       return 0;
     }

@@ -200,9 +200,44 @@ struct KrylovResult {
   double rel_residual = 0.0;      // recursive (BiCGSTAB) / restart-time true (GMRES)
   double true_rel_residual = 0.0; // ||b - A x|| / ||b|| of the returned x
 };
+struct SsorPrecond;
+// P (may be null): a general preconditioner (SSOR) applied instead of the
+// diagonal one; dinv must then be all ones.
 cudaError_t krylov_solve(const DeviceCRS& A, const double* dinv, const double* b, double* x,
                          int method, double eps, long long max_iter, int restart, cudaStream_t s,
-                         KrylovResult* res);
+                         KrylovResult* res, SsorPrecond* P = nullptr);
+
+// SSOR preconditioner of a symmetric CRS matrix (nlgb_ssor.cu):
+// M = (D + w L) D^-1 (D + w L^T) / (w (2 - w)); apply() computes z = M^-1 r
+// by level-scheduled forward and backward sweeps (each row as the sequential
+// sweep computes it, the rows of a level in parallel).  A must outlive it.
+struct SsorPrecond {
+  int n = 0;
+  double omega = 1.5;
+  const DeviceCRS* A = nullptr;
+  int* rows_f = nullptr;         // rows grouped by forward-sweep level
+  int* rows_b = nullptr;         // rows grouped by backward-sweep level
+  std::vector<int> ptr_f, ptr_b; // level boundaries (host)
+  double* diag = nullptr;        // a_ii (1 where missing or zero)
+  double* y = nullptr;           // forward-sweep result
+  struct Cached { const double* r; double* z; cudaGraphExec_t exec; };
+  std::vector<Cached> graphs;    // captured sweeps per (r, z) pair of the solve
+  SsorPrecond() = default;
+  SsorPrecond(const SsorPrecond&) = delete;
+  SsorPrecond& operator=(const SsorPrecond&) = delete;
+  ~SsorPrecond() { release(); }
+  cudaError_t build(const DeviceCRS& A, double omega, cudaStream_t s);
+  cudaError_t apply(const double* r, double* z, cudaStream_t s);   // r, z device vectors
+  void release();
+
+ private:
+  cudaError_t launch_sweeps(const double* r, double* z, cudaStream_t s);
+};
+struct KrylovResult;
+// CG with the SSOR preconditioner (FP64; true-residual check as the other
+// FP64 solvers).  b, x device vectors (x: initial guess, replaced).
+cudaError_t pcg_ssor(const DeviceCRS& A, SsorPrecond& P, const double* b, double* x, double eps,
+                     long long max_iter, cudaStream_t s, KrylovResult* res);
 
 // Device BLAS-1 (FP64).
 cudaError_t dev_dot(const double* x, const double* y, long long n, double* out_host, cudaStream_t s);

@@ -419,6 +419,24 @@ __global__ void k_gm_update_x(KrView v, GmVecs w) {
   }
 }
 
+// With a general (SSOR) preconditioner: t = V y (the correction before
+// preconditioning), then x += M^-1 t.
+__global__ void k_gm_vy(KrView v, GmVecs w, double* t) {
+  KrState* st = v.st;
+  if (*((volatile int*)&st->status) != ST_RUNNING) return;
+  const int k = st->j;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < v.n; i += (long long)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int c = 0; c < k; ++c) s += st->y[c] * w.V[(size_t)c * w.ld + i];
+    t[i] = s;
+  }
+}
+__global__ void k_gm_add_x(KrView v, double* x, const double* z) {
+  if (*((volatile int*)&v.st->status) != ST_RUNNING) return;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < v.n; i += (long long)gridDim.x * blockDim.x)
+    x[i] += z[i];
+}
+
 int grid1(long long n) { return (int)std::max(1LL, std::min<long long>((n + 255) / 256, 152LL * 8)); }
 
 }  // namespace
@@ -435,12 +453,13 @@ int grid1(long long n) { return (int)std::max(1LL, std::min<long long>((n + 255)
 
 cudaError_t krylov_solve(const DeviceCRS& A, const double* dinv, const double* b, double* x,
                          int method, double eps, long long max_iter, int restart, cudaStream_t s,
-                         KrylovResult* res) {
+                         KrylovResult* res, SsorPrecond* P) {
   const int n = A.n;
   const int tile_rows = A.tile_rows > 0 ? A.tile_rows : 128;
   const int n_tiles = std::max(1, (n + tile_rows - 1) / tile_rows);
   const int m = std::max(1, std::min(restart, kMaxRestart));
-  const int n_vec = method == KRYLOV_BICGSTAB ? 7 : (m + 2);   // work vectors
+  // work vectors (+ two for GMRES's correction around a general preconditioner)
+  const int n_vec = method == KRYLOV_BICGSTAB ? 7 : (m + 2 + (P ? 2 : 0));
   const size_t ld = (size_t)((n + 31) / 32 * 32);
   double* work = nullptr;
   double* part = nullptr;
@@ -473,21 +492,27 @@ cudaError_t krylov_solve(const DeviceCRS& A, const double* dinv, const double* b
     int status = ST_RUNNING;
     while (e == cudaSuccess && status == ST_RUNNING) {
       for (int c = 0; c < kChunk; ++c) {
+        // (with a general preconditioner dinv is all ones: y = p, z = s,
+        // then y = M^-1 p, z = M^-1 s)
         k_bi_p<<<n_tiles, kCTA, 0, s>>>(v, w);
+        if (P && e == cudaSuccess) e = P->apply(w.p, w.y, s);
         NLGB_KR_T((k_bi_v<T><<<n_tiles, kCTA, 0, s>>>(v, w)));
         k_bi_alpha<<<1, kCTA, 0, s>>>(v);
         k_bi_s<<<n_tiles, kCTA, 0, s>>>(v, w);
+        if (P && e == cudaSuccess) e = P->apply(w.r, w.z, s);
         NLGB_KR_T((k_bi_t<T><<<n_tiles, kCTA, 0, s>>>(v, w)));
         k_bi_omega<<<1, kCTA, 0, s>>>(v);
         k_bi_xr<<<n_tiles, kCTA, 0, s>>>(v, w);
         k_bi_end<<<1, kCTA, 0, s>>>(v);
         launches += 8;
       }
-      e = cudaGetLastError();
+      if (e == cudaSuccess) e = cudaGetLastError();
       if (e == cudaSuccess) e = poll(&status);
     }
   } else if (e == cudaSuccess) {
     GmVecs w{b, x, work, work + (size_t)(m + 1) * ld, ld};
+    double* t = P ? work + (size_t)(m + 2) * ld : nullptr;
+    double* tz = P ? work + (size_t)(m + 3) * ld : nullptr;
     int status = ST_RUNNING;
     bool first = true;
     while (e == cudaSuccess && status == ST_RUNNING) {
@@ -497,7 +522,11 @@ cudaError_t krylov_solve(const DeviceCRS& A, const double* dinv, const double* b
       launches += 3;
       first = false;
       for (int j = 0; j < m; ++j) {
-        k_gm_precond<<<grid1(n), 256, 0, s>>>(v, w, j);
+        if (P) {
+          if (e == cudaSuccess) e = P->apply(w.V + (size_t)j * ld, w.u, s);   // u = M^-1 V_j
+        } else {
+          k_gm_precond<<<grid1(n), 256, 0, s>>>(v, w, j);
+        }
         NLGB_KR_T((k_gm_spmv<T><<<n_tiles, kCTA, 0, s>>>(v, w, j)));
         for (int round = 0; round < 2; ++round) {     // CGS2
           k_gm_multidot<<<n_tiles, kCTA, 0, s>>>(v, w, j);
@@ -509,9 +538,16 @@ cudaError_t krylov_solve(const DeviceCRS& A, const double* dinv, const double* b
         launches += 10;
       }
       k_gm_solve_y<<<1, 32, 0, s>>>(v);
-      k_gm_update_x<<<grid1(n), 256, 0, s>>>(v, w);
+      if (P) {
+        k_gm_vy<<<grid1(n), 256, 0, s>>>(v, w, t);
+        if (e == cudaSuccess) e = P->apply(t, tz, s);
+        k_gm_add_x<<<grid1(n), 256, 0, s>>>(v, w.x, tz);
+        launches += 1;
+      } else {
+        k_gm_update_x<<<grid1(n), 256, 0, s>>>(v, w);
+      }
       launches += 2;
-      e = cudaGetLastError();
+      if (e == cudaSuccess) e = cudaGetLastError();
       if (e == cudaSuccess) e = poll(&status);
     }
   }

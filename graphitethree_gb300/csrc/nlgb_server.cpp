@@ -24,6 +24,7 @@
 #include "nlgb_internal.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
@@ -91,6 +92,7 @@ struct Req {
   std::vector<double> ms_per_iter;
   std::vector<nlgb_result> res;
   double t_done = 0.0;
+  double t_built = 0.0, t_prepared = 0.0;   // admission phases (server clock, tracing)
   int status = NL_GB300_STATUS_NONE;
   std::string error;
 };
@@ -298,7 +300,9 @@ bool admit(nlgb_server_s* S, Req* r, cudaStream_t s, bool df_slots) {
     cudaStreamSynchronize(s);
     cudaFree(drp); cudaFree(dcol); cudaFree(dval); cudaFree(drhs); cudaFree(dw); cudaFree(dxl);
   }
+  r->t_built = S->now();
   if (e == cudaSuccess) e = crs_prepare(r->A, mixed, s);
+  r->t_prepared = S->now();
   bool dfl = false;   // false also when the matrix is outside double-float's range: FP64 runs
   if (e == cudaSuccess && prec == NL_GB300_PRECISION_DOUBLE_FLOAT) e = crs_prepare_df(r->A, &dfl, s);
   if (e == cudaSuccess) {
@@ -558,8 +562,9 @@ void admitter(nlgb_server_s* S) {
       }
       const double tb = S->now();
       if (S->trace)
-        std::fprintf(S->trace, "A,%.6f,%lld,%d,%d,%.6f,%zu,%.6f,%.6f\n", ta, pick->id,
-                     pick->kind == 2 ? pick->mesh_kind : -1, pick->n, tb - ta, pick->bytes, pick->arrival, tb - tg);
+        std::fprintf(S->trace, "A,%.6f,%lld,%d,%d,%.6f,%zu,%.6f,%.6f,%.6f,%.6f\n", ta, pick->id,
+                     pick->kind == 2 ? pick->mesh_kind : -1, pick->n, tb - ta, pick->bytes, pick->arrival, tb - tg,
+                     pick->t_built - ta, pick->t_prepared - pick->t_built);
       if (!ok) {
         release(S, pick, su);
         {
@@ -829,6 +834,20 @@ void worker_batched(nlgb_server_s* S) {
 // first, for a probe of kProbeIters iterations).  A system's chunks run one
 // after the other (the next one is queued only after the previous one was
 // seen to finish), so its iterates are those of the single-system solver.
+struct LaneSignal {
+  nlgb_server_s* S = nullptr;
+  std::atomic<int>* flag = nullptr;
+};
+
+// Host function queued after a lane's chunk and state copy (runs on a CUDA
+// thread; no CUDA calls): the lane is done.
+void CUDART_CB lane_finished(void* p) {
+  LaneSignal* g = static_cast<LaneSignal*>(p);
+  g->flag->store(1);
+  { std::lock_guard<std::mutex> lk(g->S->mu); }   // the waiter is asleep or sees the flag
+  g->S->cv_work.notify_all();
+}
+
 void worker_streams(nlgb_server_s* S) {
   cudaSetDevice(S->device);
   const int ns = std::max(1, S->cfg.streams > 0 ? S->cfg.streams : 16);
@@ -841,6 +860,22 @@ void worker_streams(nlgb_server_s* S) {
     float ms = 0.f;
   };
   std::vector<Lane> lanes((size_t)ns);
+  // Completion of a lane's chunk is signalled by a host function queued
+  // after it (no polling of the streams, which would contend with the
+  // admission threads' CUDA calls): it raises the lane's flag and wakes the
+  // worker.
+  std::vector<std::atomic<int>> done_flag((size_t)ns);
+  std::vector<LaneSignal> signal((size_t)ns);
+  for (int i = 0; i < ns; ++i) {
+    done_flag[i].store(0);
+    signal[i].S = S;
+    signal[i].flag = &done_flag[i];
+  }
+  auto any_done = [&]() {
+    for (int i = 0; i < ns; ++i)
+      if (done_flag[i].load()) return true;
+    return false;
+  };
   int least = 0, greatest = 0;
   cudaDeviceGetStreamPriorityRange(&least, &greatest);
   cudaStream_t su = nullptr;   // result downloads and releases: ahead of the chunks
@@ -958,11 +993,10 @@ void worker_streams(nlgb_server_s* S) {
     // retire finished chunks
     cudaError_t e = cudaSuccess;
     bool progress = false;
-    for (Lane& l : lanes) {
-      if (!l.r) continue;
-      const cudaError_t q = cudaStreamQuery(l.s);
-      if (q == cudaErrorNotReady) continue;
-      if (q != cudaSuccess) { e = q; set_error(std::string("server chunk: ") + cudaGetErrorString(q)); break; }
+    for (int i = 0; i < ns; ++i) {
+      Lane& l = lanes[(size_t)i];
+      if (!l.r || !done_flag[i].load()) continue;
+      done_flag[i].store(0);
       e = retire(l);
       if (e != cudaSuccess) break;
       progress = true;
@@ -984,12 +1018,14 @@ void worker_streams(nlgb_server_s* S) {
         if (S->admitter_done && S->admitted.empty()) break;
         S->cv_work.wait_for(lk, std::chrono::milliseconds(20));
       } else {
-        std::this_thread::sleep_for(std::chrono::microseconds(50));
+        std::unique_lock<std::mutex> lk(S->mu);
+        S->cv_work.wait_for(lk, std::chrono::milliseconds(5), any_done);
       }
       continue;
     }
     // give every free lane the least-work system that is not running
-    for (Lane& l : lanes) {
+    for (int li = 0; li < ns; ++li) {
+      Lane& l = lanes[(size_t)li];
       if (l.r) continue;
       Req* best = nullptr;
       int bk = -1;
@@ -1021,6 +1057,7 @@ void worker_streams(nlgb_server_s* S) {
         e = best->graphs[bk]->run(best->slots[bk].view, iters, l.s, &l.ms, best->mixed_now[bk] != 0);
       if (e == cudaSuccess)
         e = cudaMemcpyAsync(l.h, best->slots[bk].view.st, sizeof(SysState), cudaMemcpyDeviceToHost, l.s);
+      if (e == cudaSuccess) e = cudaLaunchHostFunc(l.s, lane_finished, &signal[(size_t)li]);
       busy_change(+1);
       progress = true;
       if (e != cudaSuccess) break;
@@ -1032,13 +1069,11 @@ void worker_streams(nlgb_server_s* S) {
       break;
     }
     if (!progress) {
-      if (n_busy > 0) {
-        std::this_thread::sleep_for(std::chrono::microseconds(20));
-      } else {
-        std::unique_lock<std::mutex> lk(S->mu);
-        S->cv_work.wait_for(lk, std::chrono::milliseconds(20),
-                            [&] { return !S->admitted.empty() || S->admitter_done || S->aborting; });
-      }
+      // sleep until a chunk finishes, a request is admitted or the server stops
+      std::unique_lock<std::mutex> lk(S->mu);
+      S->cv_work.wait_for(lk, std::chrono::milliseconds(n_busy > 0 ? 5 : 20), [&] {
+        return any_done() || !S->admitted.empty() || S->admitter_done || S->aborting;
+      });
     }
   }
   for (Lane& l : lanes) if (l.s) cudaStreamSynchronize(l.s);
@@ -1211,7 +1246,7 @@ nlgb_server nlgb_server_create(const nlgb_server_config* cfg) {
       std::fprintf(S->trace, "# E,t0,t1,kind,systems,teams,team_ctas,queue_ctas,grid,planned_GB,done_GB,ms,"
                              "team_ms_min,team_ms_med,team_ms_max,queue_ms,admits,admit_s,active_requests\n"
                              "# C,t,request,rhs,mixed,iter_before,iter_after,ms,status,stage\n"
-                             "# A,t,request,mesh_kind,n,seconds,bytes,arrival,graph_seconds\n");
+                             "# A,t,request,mesh_kind,n,seconds,bytes,arrival,graph_seconds,build_seconds,prepare_seconds\n");
   }
   S->origin = Clock::now();
   S->th = std::thread(S->cfg.mode == NLGB_SERVER_SERIAL

@@ -402,7 +402,8 @@ def solve_opennl(rs: RowStream, precision: str = "double", eps: float = 1e-10,
         nl.nlSolverParameteri(nl.NL_SOLVER, {"cg": nl.NL_CG, "bicgstab": nl.NL_BICGSTAB,
                                              "gmres": nl.NL_GMRES}[solver])
         nl.nlSolverParameteri(nl.NL_PRECONDITIONER, {"jacobi": nl.NL_PRECOND_JACOBI,
-                                                     "none": nl.NL_PRECOND_NONE}[preconditioner])
+                                                     "none": nl.NL_PRECOND_NONE,
+                                                     "ssor": nl.NL_PRECOND_SSOR}[preconditioner])
         if inner_iterations is not None:
             nl.nlSolverParameteri(nl.NL_INNER_ITERATIONS, int(inner_iterations))
         nl.nlSolverParameterd(nl.NL_THRESHOLD, eps)

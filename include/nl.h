@@ -136,7 +136,9 @@ typedef void*          NLContext;
 
 #define NL_PRECOND_NONE    0x000
 #define NL_PRECOND_JACOBI  0x300
-#define NL_PRECOND_SSOR    0x301  /* rejected: not built */
+#define NL_PRECOND_SSOR    0x301  /* SSOR with relaxation NL_OMEGA (default 1.5):
+                                     level-scheduled sweeps on the GPU, CG /
+                                     BiCGSTAB / GMRES (symmetric matrices) */
 
 /* ---- nlEnable / nlDisable / nlIsEnabled ---- */
 #define NL_NORMALIZE_ROWS  0x400
@@ -240,7 +242,10 @@ void     nlMatrixCompress(NLMatrix* M);                            /* :309 */
 void     nlMultMatrixVector(NLMatrix M, const double* x, double* y); /* :303 */
 NLuint   nlMatrixNNZ(NLMatrix M);
 NLMatrix nlNewJacobiPreconditioner(NLMatrix M);                   /* :364 */
-NLMatrix nlNewSSORPreconditioner(NLMatrix M, double omega);       /* :367, returns NULL */
+/* SSOR of a square symmetric sparse matrix, M = (D + w L) D^-1 (D + w L^T) /
+ * (w (2 - w)); must not outlive M nor follow changes to it (the reference
+ * wrapper creates it just before nlSolveSystemIterative and deletes it after). */
+NLMatrix nlNewSSORPreconditioner(NLMatrix M, double omega);       /* :367 */
 NLMatrix nlMatrixFactorize(NLMatrix M, NLenum solver);            /* :317-327, returns NULL */
 
 /* ---- BLAS abstraction (scene_graph/NL/blas.cpp:66-144) ---- */
@@ -278,7 +283,7 @@ NLBlas_t nlCUDABlas(void);     /* same table; name kept for OpenNL's CUDA-extens
 void     nlBlasResetStats(NLBlas_t blas);
 
 /* Iterative solve of M x = b (matrix.cpp:390-393).  M: CRS, dynamic or
- * device matrix; P: NULL or a Jacobi preconditioner; b, x: host or device
+ * device matrix; P: NULL, a Jacobi or an SSOR preconditioner; b, x: host or device
  * vectors of size M->n (x is the initial guess).  solver: NL_CG /
  * NL_SOLVER_DEFAULT (Jacobi-PCG), NL_BICGSTAB or NL_GMRES (restart length
  * inner_iter; both FP64, right-preconditioned by P); returns the number of

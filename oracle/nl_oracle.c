@@ -313,6 +313,101 @@ int nlo_pcg(int n, const int* rp, const int* ci, const double* va, const double*
                          rel_res_out);
 }
 
+/* SSOR preconditioner of a symmetric A = L + D + L^T, relaxation omega in
+ * (0, 2): M = (D + omega L) D^-1 (D + omega L^T) / (omega (2 - omega)).
+ * z = M^-1 r by the two sequential sweeps
+ *   forward:  y_i = (omega (2 - omega) r_i - omega sum_{j<i} a_ij y_j) / d_i
+ *   backward: z_i = y_i - (omega / d_i) sum_{j>i} a_ij z_j
+ * (row entries in their CRS order; d_i = a_ii, 1 when missing or zero). */
+static void ssor_apply(int n, const int* rp, const int* ci, const double* va, const double* d,
+                       double omega, const double* r, double* y, double* z) {
+    const double c = omega * (2.0 - omega);
+    for (int i = 0; i < n; ++i) {
+        double s = c * r[i];
+        for (int k = rp[i]; k < rp[i + 1]; ++k)
+            if (ci[k] < i) s = s - omega * va[k] * y[ci[k]];
+        y[i] = s / d[i];
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        double s = 0.0;
+        for (int k = rp[i]; k < rp[i + 1]; ++k)
+            if (ci[k] > i) s = s + va[k] * z[ci[k]];
+        z[i] = y[i] - omega * s / d[i];
+    }
+}
+
+static void ssor_diag(int n, const int* rp, const int* ci, const double* va, double* d) {
+    for (int i = 0; i < n; ++i) {
+        double di = 0.0;
+        for (int k = rp[i]; k < rp[i + 1]; ++k)
+            if (ci[k] == i) di += va[k];
+        d[i] = di != 0.0 ? di : 1.0;
+    }
+}
+
+/* PCG with the SSOR preconditioner (sequential sweeps, the rest as
+ * nlo_pcg).  Returns 1 converged, 2 max_iter, 3 breakdown. */
+int nlo_pcg_ssor(int n, const int* rp, const int* ci, const double* va, const double* b, double* x,
+                 double eps, long long max_iter, double omega, long long* iters_out,
+                 double* rel_res_out) {
+    const size_t sz = sizeof(double) * (n > 0 ? n : 1);
+    double *r = (double*)calloc(1, sz), *z = (double*)calloc(1, sz), *p = (double*)calloc(1, sz);
+    double *q = (double*)calloc(1, sz), *d = (double*)calloc(1, sz), *y = (double*)calloc(1, sz);
+    int status = 0;
+    long long it = 0;
+    ssor_diag(n, rp, ci, va, d);
+    const double bb = dot(n, b, b, 1);
+    double rr = 0.0, rho = 0.0;
+    if (!(bb > 0.0)) {
+        for (int i = 0; i < n; ++i) x[i] = 0.0;
+        status = bb == 0.0 ? 1 : 3;
+        goto done;
+    }
+    nlo_spmv(n, rp, ci, va, x, q, 1);
+    for (int i = 0; i < n; ++i) r[i] = b[i] - q[i];
+    ssor_apply(n, rp, ci, va, d, omega, r, y, z);
+    for (int i = 0; i < n; ++i) p[i] = z[i];
+    rho = dot(n, r, z, 1);
+    rr = dot(n, r, r, 1);
+    while (1) {
+        if (rr <= eps * eps * bb) { status = 1; break; }
+        if (it >= max_iter) { status = 2; break; }
+        nlo_spmv(n, rp, ci, va, p, q, 1);
+        const double pq = dot(n, p, q, 1);
+        if (!(pq > 0.0)) { status = 3; break; }
+        const double alpha = rho / pq;
+        for (int i = 0; i < n; ++i) {
+            x[i] = x[i] + alpha * p[i];
+            r[i] = r[i] - alpha * q[i];
+        }
+        ssor_apply(n, rp, ci, va, d, omega, r, y, z);
+        const double rho_new = dot(n, r, z, 1);
+        rr = dot(n, r, r, 1);
+        ++it;
+        if (rr <= eps * eps * bb) { status = 1; break; }
+        if (it >= max_iter) { status = 2; break; }
+        if (!(rho_new > 0.0)) { status = 3; break; }
+        const double beta = rho_new / rho;
+        rho = rho_new;
+        for (int i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+    }
+done:
+    if (iters_out) *iters_out = it;
+    if (rel_res_out) *rel_res_out = bb > 0.0 ? sqrt(rr / bb) : 0.0;
+    free(r); free(z); free(p); free(q); free(d); free(y);
+    return status;
+}
+
+/* z = M^-1 r of the SSOR preconditioner above (tests of the sweeps). */
+void nlo_ssor_apply(int n, const int* rp, const int* ci, const double* va, double omega, const double* r,
+                    double* z) {
+    const size_t sz = sizeof(double) * (n > 0 ? n : 1);
+    double *d = (double*)calloc(1, sz), *y = (double*)calloc(1, sz);
+    ssor_diag(n, rp, ci, va, d);
+    ssor_apply(n, rp, ci, va, d, omega, r, y, z);
+    free(d); free(y);
+}
+
 int nlo_max_threads(void) {
 #ifdef _OPENMP
     return omp_get_max_threads();

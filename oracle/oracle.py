@@ -7,6 +7,8 @@ arm may import this module; the library never does.
   stream (C, nl_oracle.c), bit-exact reference for the GPU row-merge.
 * ``pcg``: FP64 Jacobi-PCG with OpenMP threads (C), the timed CPU baseline
   and the iterative oracle.
+* ``pcg_ssor`` / ``ssor_apply``: CG with the SSOR preconditioner, sequential
+  sweeps (C), the oracle of the GPU's level-scheduled sweeps.
 * ``direct_solve``: scipy SuperLU, the FP64 direct oracle.
 * ``pcg_df``: numpy restatement of the double-float Jacobi-PCG (float pairs
   hi + lo, error-free transformations in float32), for the algorithm's
@@ -66,6 +68,11 @@ def lib():
         L.nlo_pcg_timed.argtypes = [ctypes.c_int, _c_int_p, _c_int_p, _c_dbl_p, _c_dbl_p, _c_dbl_p,
                                     ctypes.c_double, ctypes.c_longlong, ctypes.c_int, ctypes.c_int,
                                     ctypes.c_double, _c_ll_p, _c_dbl_p]
+        L.nlo_pcg_ssor.restype = ctypes.c_int
+        L.nlo_pcg_ssor.argtypes = [ctypes.c_int, _c_int_p, _c_int_p, _c_dbl_p, _c_dbl_p, _c_dbl_p,
+                                   ctypes.c_double, ctypes.c_longlong, ctypes.c_double, _c_ll_p, _c_dbl_p]
+        L.nlo_ssor_apply.argtypes = [ctypes.c_int, _c_int_p, _c_int_p, _c_dbl_p, ctypes.c_double, _c_dbl_p,
+                                     _c_dbl_p]
         L.nlo_max_threads.restype = ctypes.c_int
         _lib = L
     return _lib
@@ -167,6 +174,33 @@ def pcg(rp, ci, va, b, x0=None, eps: float = 1e-10, max_iter: int | None = None,
                              nthreads or max_threads(), float(max_seconds), ctypes.byref(it),
                              ctypes.byref(rr))
     return x, int(st), int(it.value), float(rr.value)
+
+
+def pcg_ssor(rp, ci, va, b, x0=None, eps: float = 1e-10, max_iter: int | None = None,
+             omega: float = 1.5):
+    """FP64 CG with the SSOR preconditioner (sequential forward and backward
+    sweeps, relaxation omega).  Returns (x, status, iterations, rel_residual)."""
+    rp = np.ascontiguousarray(rp, np.int32); ci = np.ascontiguousarray(ci, np.int32)
+    va = np.ascontiguousarray(va, np.float64); b = np.ascontiguousarray(b, np.float64)
+    n = rp.shape[0] - 1
+    x = np.zeros(n) if x0 is None else np.array(x0, np.float64, copy=True)
+    it = ctypes.c_longlong()
+    rr = ctypes.c_double()
+    st = lib().nlo_pcg_ssor(n, _p(rp, _c_int_p), _p(ci, _c_int_p), _p(va, _c_dbl_p), _p(b, _c_dbl_p),
+                            _p(x, _c_dbl_p), eps, 5 * n if max_iter is None else max_iter, float(omega),
+                            ctypes.byref(it), ctypes.byref(rr))
+    return x, int(st), int(it.value), float(rr.value)
+
+
+def ssor_apply(rp, ci, va, r, omega: float = 1.5):
+    """z = M^-1 r for the SSOR preconditioner (sequential sweeps)."""
+    rp = np.ascontiguousarray(rp, np.int32); ci = np.ascontiguousarray(ci, np.int32)
+    va = np.ascontiguousarray(va, np.float64); r = np.ascontiguousarray(r, np.float64)
+    n = rp.shape[0] - 1
+    z = np.empty(n)
+    lib().nlo_ssor_apply(n, _p(rp, _c_int_p), _p(ci, _c_int_p), _p(va, _c_dbl_p), float(omega),
+                         _p(r, _c_dbl_p), _p(z, _c_dbl_p))
+    return z
 
 
 def direct_solve(rp, ci, va, b):

@@ -106,16 +106,20 @@ def test_variables_and_locks(ctx):
     assert nl.nlGetError() == nl.NL_INVALID_VALUE
 
 
-def test_unsupported_preconditioner_fails_loudly(ctx):
-    """SSOR is not built: nlSolve refuses it (no silent substitution)."""
+def test_ssor_preconditioner_parameter(ctx):
+    """NL_PRECOND_SSOR is accepted (the GPU runs it, tests/test_gpu_ssor.py);
+    without a device nlSolve fails loudly instead of returning a result."""
     nl.nlSolverParameteri(nl.NL_NB_VARIABLES, 1)
     nl.nlSolverParameteri(nl.NL_PRECONDITIONER, nl.NL_PRECOND_SSOR)
+    nl.nlSolverParameterd(nl.NL_OMEGA, 1.2)
+    assert nl.nlGetIntegerv(nl.NL_PRECONDITIONER) == nl.NL_PRECOND_SSOR
+    assert nl.nlGetDoublev(nl.NL_OMEGA) == 1.2
+    if nl.nlInitExtension("GB300"):
+        pytest.skip("a GPU is present: the solve itself is covered by the GPU tests")
     nl.nlBegin(nl.NL_SYSTEM); nl.nlBegin(nl.NL_MATRIX)
     nl.nlBegin(nl.NL_ROW); nl.nlCoefficient(0, 1.0); nl.nlRightHandSide(1.0); nl.nlEnd(nl.NL_ROW)
     nl.nlEnd(nl.NL_MATRIX); nl.nlEnd(nl.NL_SYSTEM)
     assert nl.nlSolve() == 0
-    assert "SSOR" in nl.nlGetErrorString()
-    assert nl.nlGetIntegerv(nl.NL_GB300_STATUS) == nl.NL_GB300_STATUS_BAD_INPUT
 
 
 def test_krylov_solver_parameters(ctx):
@@ -163,6 +167,6 @@ def test_matrix_api_host_side(nllib):
     assert nl.nlMatrixNNZ(M) == 4
     M = nl.nlMatrixCompress(M)
     assert nl.nlMatrixNNZ(M) == 4
-    assert nl.nlNewSSORPreconditioner(M, 1.5) is None
+    assert nl.nlNewSSORPreconditioner(M, 2.5) is None     # relaxation outside (0, 2)
     assert nl.nlMatrixFactorize(M, nl.NL_SUPERLU_EXT) is None
     nl.nlDeleteMatrix(M)
