@@ -59,6 +59,8 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 os.environ.setdefault("NLGB_QUIET", "1")
+# one hardware work queue per server stream (read at CUDA context creation)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 import numpy as np  # noqa: E402
 
@@ -87,6 +89,7 @@ def parse_args():
     p.add_argument("--eps", type=float, default=1e-10)
     p.add_argument("--budget-gb", type=float, default=150.0)
     p.add_argument("--plain-steps", type=int, default=2, help="steps of the serial plain-FP64 arm")
+    p.add_argument("--streams", type=int, default=16, help="concurrent chunk streams of the batched server")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-spmv", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
@@ -390,7 +393,8 @@ def run_stream(stream, args, mode: str, precision: str, keep_x: bool = False):
     """One step: replay the window in real time through the C ABI, end it
     `drain` seconds after the window, abort what is left.  Returns a dict."""
     from graphitethree_gb300 import solver
-    srv = solver.Server(budget_bytes=args.budget_gb * 1e9, precision=precision, mode=mode, eps=args.eps)
+    srv = solver.Server(budget_bytes=args.budget_gb * 1e9, precision=precision, mode=mode, eps=args.eps,
+                        streams=args.streams)
     srv.reset_clock()
     T0 = args.lead
     tickets = [srv.submit_mesh(r.kind, r.V, r.F, b=r.b, lam=r.lam, arrival=T0 + r.arrival) for r in stream]

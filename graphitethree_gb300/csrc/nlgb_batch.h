@@ -106,6 +106,20 @@ struct SystemSlot {
 // Resumable PCG chunks (FP64, double-float or mixed precision) of a system
 // whose buffers and device state belong to a SystemSlot, as CUDA graphs (see
 // nlgb_solver.cu).
+// Host-mapped record of one system's chunks (pinned host memory, written by
+// the device over the C2C link): the host sets the next chunk's budget
+// before launching it; the chunk's last kernel copies the system's state
+// here, stores the chunk's device duration and then bumps `seq`, so that a
+// host thread sees the end of a chunk by reading memory, without a CUDA call.
+struct ChunkMirror {
+  SysState st;                   // the system's state after the last chunk
+  long long budget;              // host: iterations of the next chunk
+  unsigned long long t_start;    // device: %globaltimer at the chunk's start
+  unsigned long long t_ns;       // device: the chunk's duration
+  unsigned int seq;              // device: +1 after st and t_ns of a chunk are written
+  unsigned int pad_;
+};
+
 class ViewGraph {
  public:
   ViewGraph() = default;
@@ -122,11 +136,21 @@ class ViewGraph {
   cudaError_t run(const SysView& v, long long iters, cudaStream_t s, float* ms, bool mixed = false);
   bool done() const;
   cudaError_t finish(long long iters_before, long long iters_after);
+  // Mirrored chunks: the graph reads its budget from `m` (host-mapped) and
+  // ends by writing the state there (ChunkMirror).  launch() is then the
+  // only CUDA call of a chunk: the caller writes m->budget, launches and
+  // polls m->seq; account() counts the chunk's kernels afterwards.
+  // A graph (re)built here is uploaded on `upload` when given, so that its
+  // first launch does not pay for it.
+  cudaError_t prepare(const SysView& v, bool mixed, ChunkMirror* m, cudaStream_t upload = nullptr);
+  cudaError_t launch(cudaStream_t s);
+  void account(long long iters_before, long long iters_after);
 
  private:
   cudaError_t build(const SysView& v, bool mixed);
   cudaError_t run_eager(cudaStream_t s, long long iters);
   SysView view_{};
+  ChunkMirror* mirror_ = nullptr;
   bool mixed_ = false;
   cudaGraphExec_t exec_ = nullptr;
   cudaEvent_t e0_ = nullptr, e1_ = nullptr;

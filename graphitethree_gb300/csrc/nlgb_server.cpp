@@ -88,6 +88,7 @@ struct Req {
   // in flight, whether it runs the mixed iteration now, a pending switch to
   // FP64, and the measured time per iteration (ms; < 0 unknown)
   std::vector<std::unique_ptr<ViewGraph>> graphs;
+  std::vector<int> mirror_idx;       // per system, its ChunkMirror in the server's pool
   std::vector<int> running, mixed_now, need_fallback;
   std::vector<double> ms_per_iter;
   std::vector<nlgb_result> res;
@@ -172,8 +173,28 @@ struct nlgb_server_s {
   // executor polls it once per while-loop pass.
   volatile int* abort_host = nullptr;
   int* abort_dev = nullptr;
-  // Tracing (environment NLGB_SERVER_TRACE = path): one CSV line per epoch
-  // ("E", ...) and per admission ("A", ...), written by the worker thread.
+  // SRPT stream executor: one ChunkMirror per admitted system (pinned,
+  // mapped; max_systems of them) and the free indices (guarded by mu)
+  ChunkMirror* mirrors = nullptr;
+  std::vector<int> mirror_free;
+  // Requests whose systems are all done, handed by the worker to the
+  // completion threads (result download, release; guarded by mu)
+  std::deque<Req*> finished;
+  std::condition_variable cv_complete;
+  std::vector<std::thread> cmp_th;
+  bool worker_done = false;
+  // Chunk graphs of released requests.  Destroying an executable graph
+  // waits for the device to be idle, which would stall every thread's CUDA
+  // calls behind the chunks in flight; they are destroyed by the completion
+  // threads when no chunk runs (or, past kGraveyardCap, the oldest ones
+  // regardless).  Guarded by mu; lanes_busy is the worker's count of
+  // chunks in flight.
+  std::vector<std::unique_ptr<ViewGraph>> graveyard;
+  std::atomic<int> lanes_busy{0};
+  // Tracing (environment NLGB_SERVER_TRACE = path): CSV lines per epoch of
+  // the persistent kernel ("E"), per chunk ("C"), per admission ("A"), per
+  // completion ("D", "R") and one summary of the stream worker's host time
+  // ("W"); the file starts with the column names.
   FILE* trace = nullptr;
 
   double now() const { return std::chrono::duration<double>(Clock::now() - origin).count(); }
@@ -224,7 +245,9 @@ constexpr double kServiceFloorBytes = 1.6e5;
 constexpr long long kProbeIters = 16;      // SRPT: first epoch of a new system
 constexpr int kReserveCtas = 16;           // persistent-kernel slots left to system builds
 constexpr long long kUnrollPlainIters = 4;  // a chunk pauses on whole passes of 4 iterations
-constexpr int kAdmitters = 2;               // admission threads of the batched server
+constexpr int kAdmitters = 4;               // admission threads of the batched server
+constexpr int kCompleters = 2;              // completion threads of the SRPT stream executor
+constexpr size_t kGraveyardCap = 1024;      // chunk graphs kept for destruction at an idle moment
 double iteration_cost(const Req& r, bool mixed) {
   const double n = double(r.A.n), z = double(r.A.nnz);
   const double b = mixed ? 8.0 * z + 56.0 * n : 12.0 * z + 108.0 * n;
@@ -353,9 +376,22 @@ bool admit(nlgb_server_s* S, Req* r, cudaStream_t s, bool df_slots) {
 // Stream-ordered release of a request's device memory (no device-wide
 // synchronisation: the solver's other streams keep running).
 void release(nlgb_server_s* S, Req* r, cudaStream_t s) {
+  const double t0 = S->trace ? S->now() : 0.0;
   for (auto& sl : r->slots) sl.release(s);
   r->slots.clear();
+  const double t1 = S->trace ? S->now() : 0.0;
+  if (!r->graphs.empty()) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    for (auto& g : r->graphs)
+      if (g) S->graveyard.push_back(std::move(g));
+  }
   r->graphs.clear();
+  if (S->trace) std::fprintf(S->trace, "R,%.6f,%lld,%.6f,%.6f\n", S->now(), r->id, t1 - t0, S->now() - t1);
+  if (!r->mirror_idx.empty()) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    for (int i : r->mirror_idx) S->mirror_free.push_back(i);
+    r->mirror_idx.clear();
+  }
   crs_free_async(r->A, s);
   if (r->d_rhs) cudaFreeAsync(r->d_rhs, s);
   r->d_rhs = nullptr;
@@ -452,6 +488,7 @@ void fail_all_waiting(nlgb_server_s* S, const char* why) {
 // device memory and report it.
 void complete_request(nlgb_server_s* S, Req* r, cudaStream_t su) {
   bool ok = true;
+  const double t0 = S->trace ? S->now() : 0.0;
   for (int k = 0; k < r->n_rhs; ++k) {
     if (r->res[k].status == NL_GB300_STATUS_ABORTED) continue;   // nothing to return
     if (r->slots[k].df && df_unpack(r->slots[k].view.x, r->n, su) != cudaSuccess) ok = false;
@@ -463,7 +500,10 @@ void complete_request(nlgb_server_s* S, Req* r, cudaStream_t su) {
       r->status = r->res[k].status;
   cudaStreamSynchronize(su);
   if (r->status == NL_GB300_STATUS_NONE) r->status = NL_GB300_STATUS_CONVERGED;
+  const double t1 = S->trace ? S->now() : 0.0;
   release(S, r, su);
+  if (S->trace)
+    std::fprintf(S->trace, "D,%.6f,%lld,%d,%.6f,%.6f\n", S->now(), r->id, r->n, t1 - t0, S->now() - t1);
   finish_request(S, r, ok);
 }
 
@@ -552,12 +592,25 @@ void admitter(nlgb_server_s* S) {
       bool ok = admit(S, pick, su, true);
       const double tg = S->now();
       if (ok && S->cfg.schedule == NLGB_SCHEDULE_SRPT) {
-        // instantiate the chunk graphs here, off the worker's path
+        // instantiate the chunk graphs here, off the worker's path; each
+        // system reports its chunks through its own mirror (the pool holds
+        // max_systems, and sys_in_flight counted this request's systems)
+        {
+          std::lock_guard<std::mutex> g(S->mu);
+          for (int k = 0; k < pick->n_rhs && !S->mirror_free.empty(); ++k) {
+            pick->mirror_idx.push_back(S->mirror_free.back());
+            S->mirror_free.pop_back();
+          }
+        }
+        ok = (int)pick->mirror_idx.size() == pick->n_rhs;
         pick->graphs.resize((size_t)pick->n_rhs);
         for (int k = 0; k < pick->n_rhs && ok; ++k) {
+          ChunkMirror* m = &S->mirrors[pick->mirror_idx[k]];
+          m->budget = 0;
           pick->graphs[k].reset(new ViewGraph());
-          ok = pick->graphs[k]->prepare(pick->slots[k].view, pick->slots[k].mixed) == cudaSuccess;
+          ok = pick->graphs[k]->prepare(pick->slots[k].view, pick->slots[k].mixed, m, su) == cudaSuccess;
         }
+        if (ok) ok = cudaStreamSynchronize(su) == cudaSuccess;
         if (!ok) pick->error = std::string("admission failed: ") + last_error();
       }
       const double tb = S->now();
@@ -834,18 +887,54 @@ void worker_batched(nlgb_server_s* S) {
 // first, for a probe of kProbeIters iterations).  A system's chunks run one
 // after the other (the next one is queued only after the previous one was
 // seen to finish), so its iterates are those of the single-system solver.
-struct LaneSignal {
-  nlgb_server_s* S = nullptr;
-  std::atomic<int>* flag = nullptr;
-};
+// A lane's chunk has ended once its mirror's sequence number moved.
+inline unsigned int mirror_seq(const ChunkMirror* m) {
+  return __atomic_load_n(&m->seq, __ATOMIC_ACQUIRE);
+}
 
-// Host function queued after a lane's chunk and state copy (runs on a CUDA
-// thread; no CUDA calls): the lane is done.
-void CUDART_CB lane_finished(void* p) {
-  LaneSignal* g = static_cast<LaneSignal*>(p);
-  g->flag->store(1);
-  { std::lock_guard<std::mutex> lk(g->S->mu); }   // the waiter is asleep or sees the flag
-  g->S->cv_work.notify_all();
+// Completion thread of the SRPT stream executor: downloads the results of
+// requests whose systems are all done, releases their memory
+// (stream-ordered) and wakes the admission threads; the worker only hands
+// them over, so that its chunk launches never wait on these copies.
+void completer(nlgb_server_s* S) {
+  cudaSetDevice(S->device);
+  int least = 0, greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  cudaStream_t su = nullptr;
+  cudaStreamCreateWithPriority(&su, cudaStreamNonBlocking, greatest);
+  std::unique_lock<std::mutex> lk(S->mu);
+  for (;;) {
+    // destroy the chunk graphs of released requests while no chunk runs,
+    // or the oldest ones once there are too many
+    size_t n_bury = 0;
+    if (S->lanes_busy.load() == 0) n_bury = S->graveyard.size();
+    else if (S->graveyard.size() > kGraveyardCap) n_bury = S->graveyard.size() - kGraveyardCap / 2;
+    if (n_bury > 0) {
+      std::vector<std::unique_ptr<ViewGraph>> bury;
+      bury.reserve(n_bury);
+      for (size_t i = 0; i < n_bury; ++i) bury.push_back(std::move(S->graveyard[i]));
+      S->graveyard.erase(S->graveyard.begin(), S->graveyard.begin() + (long)n_bury);
+      lk.unlock();
+      bury.clear();
+      lk.lock();
+      continue;
+    }
+    if (S->finished.empty()) {
+      if (S->worker_done) break;
+      S->cv_complete.wait_for(lk, std::chrono::milliseconds(50));
+      continue;
+    }
+    Req* r = S->finished.front();
+    S->finished.pop_front();
+    lk.unlock();
+    complete_request(S, r, su);
+    lk.lock();
+    S->sys_in_flight -= r->n_rhs;
+    S->cv_admit.notify_all();
+  }
+  lk.unlock();
+  cudaStreamSynchronize(su);
+  cudaStreamDestroy(su);
 }
 
 void worker_streams(nlgb_server_s* S) {
@@ -853,43 +942,31 @@ void worker_streams(nlgb_server_s* S) {
   const int ns = std::max(1, S->cfg.streams > 0 ? S->cfg.streams : 16);
   struct Lane {
     cudaStream_t s = nullptr;
-    SysState* h = nullptr;      // pinned copy of the system's state after the chunk
+    ChunkMirror* m = nullptr;   // the running system's mirror
+    unsigned int seq0 = 0;      // its sequence number before the chunk
     Req* r = nullptr;
     int k = -1;
     long long iter_before = 0;
-    float ms = 0.f;
+    double t_free = -1.0;       // server clock when the lane's last chunk was seen done (tracing)
   };
   std::vector<Lane> lanes((size_t)ns);
-  // Completion of a lane's chunk is signalled by a host function queued
-  // after it (no polling of the streams, which would contend with the
-  // admission threads' CUDA calls): it raises the lane's flag and wakes the
-  // worker.
-  std::vector<std::atomic<int>> done_flag((size_t)ns);
-  std::vector<LaneSignal> signal((size_t)ns);
-  for (int i = 0; i < ns; ++i) {
-    done_flag[i].store(0);
-    signal[i].S = S;
-    signal[i].flag = &done_flag[i];
-  }
-  auto any_done = [&]() {
-    for (int i = 0; i < ns; ++i)
-      if (done_flag[i].load()) return true;
-    return false;
-  };
   int least = 0, greatest = 0;
   cudaDeviceGetStreamPriorityRange(&least, &greatest);
-  cudaStream_t su = nullptr;   // result downloads and releases: ahead of the chunks
+  cudaStream_t su = nullptr;   // aborts and failures: result downloads and releases
   cudaStreamCreateWithPriority(&su, cudaStreamNonBlocking, greatest);
   bool init_ok = true;
-  for (Lane& l : lanes)
-    init_ok = init_ok && cudaStreamCreateWithFlags(&l.s, cudaStreamNonBlocking) == cudaSuccess &&
-              cudaMallocHost(&l.h, sizeof(SysState)) == cudaSuccess;
+  for (Lane& l : lanes) init_ok = init_ok && cudaStreamCreateWithFlags(&l.s, cudaStreamNonBlocking) == cudaSuccess;
   if (!init_ok) {
     std::lock_guard<std::mutex> lk(S->mu);
     S->fatal = std::string("server streams: ") + cudaGetErrorString(cudaGetLastError());
     S->cv_admit.notify_all();
   }
   const double target_ms = S->cfg.epoch_ms > 0.0 ? S->cfg.epoch_ms : 10.0;
+  // host time of the worker's loop by part (tracing): retiring chunks,
+  // completing requests, launching chunks (of which the graph launches),
+  // waiting; and the time lanes sat finished before their next launch
+  double w_retire = 0.0, w_complete = 0.0, w_launch = 0.0, w_run = 0.0, w_wait = 0.0, w_gap = 0.0;
+  long long w_loops = 0, w_launches = 0;
   int n_busy = 0;
   double t_busy0 = 0.0;
   auto busy_change = [&](int delta) {
@@ -900,6 +977,8 @@ void worker_streams(nlgb_server_s* S) {
     }
     t_busy0 = t;
     n_busy += delta;
+    S->lanes_busy.store(n_busy);
+    if (n_busy == 0) S->cv_complete.notify_all();   // an idle moment for the graveyard
   };
   auto finish_abort_all = [&]() {
     for (Req* r : S->active) {
@@ -917,11 +996,12 @@ void worker_streams(nlgb_server_s* S) {
     S->active.clear();
   };
   // one finished chunk: results, estimates, completion
-  auto retire = [&](Lane& l) -> cudaError_t {
+  auto retire = [&](Lane& l) {
     Req* r = l.r;
     const int k = l.k;
-    const SysState h = *l.h;
-    cudaError_t e = r->graphs[k]->finish(l.iter_before, h.iter);
+    const SysState h = l.m->st;
+    const float ms = float(double(l.m->t_ns) * 1e-6);
+    r->graphs[k]->account(l.iter_before, h.iter);
     const long long di = h.iter - l.iter_before;
     const bool mixed_chunk = r->mixed_now[k] != 0;
     const double bytes_it = mixed_chunk ? 8.0 * double(r->A.nnz) + 56.0 * double(r->A.n)
@@ -930,14 +1010,14 @@ void worker_streams(nlgb_server_s* S) {
       std::lock_guard<std::mutex> lk(S->mu);
       S->st.epochs += 1;
       S->st.graph_epochs += 1;
-      S->st.graph_s += l.ms * 1e-3;
+      S->st.graph_s += ms * 1e-3;
       S->st.epoch_algo_bytes += double(di) * bytes_it;
       if (!mixed_chunk) S->st.graph_algo_bytes += double(di) * bytes_it;
     }
     if (S->trace)
       std::fprintf(S->trace, "C,%.6f,%lld,%d,%d,%lld,%lld,%.3f,%d,%d\n", S->now(), r->id, k, mixed_chunk ? 1 : 0,
-                   l.iter_before, h.iter, l.ms, h.status, h.stage);
-    if (di > 0) r->ms_per_iter[k] = double(l.ms) / double(di);
+                   l.iter_before, h.iter, ms, h.status, h.stage);
+    if (di > 0) r->ms_per_iter[k] = double(ms) / double(di);
     r->est_left[k] = estimate_left(r, k, h);
     r->sys_stage[k] = h.stage;
     r->sys_iter[k] = h.iter;
@@ -949,39 +1029,39 @@ void worker_streams(nlgb_server_s* S) {
       r->sys_stage[k] = 0;
     } else if (h.stage == 3) {
       r->sys_done[k] = 1;
-      fill_result(r->res[k], h, l.ms * 1e-3, r->A.n, r->A.nnz,
+      fill_result(r->res[k], h, ms * 1e-3, r->A.n, r->A.nnz,
                   r->slots[k].mixed ? NL_GB300_PRECISION_MIXED
                                     : (r->slots[k].df ? NL_GB300_PRECISION_DOUBLE_FLOAT
                                                       : NL_GB300_PRECISION_DOUBLE));
     }
     l.r = nullptr;
     l.k = -1;
+    l.m = nullptr;
     busy_change(-1);
-    return e;
   };
-  auto complete_finished = [&]() {
-    bool freed = false;
+  // requests whose systems are all done go to the completion threads
+  auto hand_over_finished = [&]() {
+    bool any = false;
     for (size_t i = 0; i < S->active.size();) {
       Req* r = S->active[i];
       bool all = true;
       for (int k = 0; k < r->n_rhs; ++k) all = all && r->sys_done[k] && !r->running[k];
       if (!all) { ++i; continue; }
       S->active.erase(S->active.begin() + (long)i);
-      complete_request(S, r, su);
-      {
-        std::lock_guard<std::mutex> lk(S->mu);
-        S->sys_in_flight -= r->n_rhs;
-      }
-      freed = true;
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->finished.push_back(r);
+      any = true;
     }
-    if (freed) S->cv_admit.notify_all();
+    if (any) S->cv_complete.notify_all();
   };
   while (S->fatal.empty()) {
+    bool have_admitted = false;
     {
       std::unique_lock<std::mutex> lk(S->mu);
       while (!S->admitted.empty()) {
         S->active.push_back(S->admitted.front());
         S->admitted.pop_front();
+        have_admitted = true;
       }
       if (S->active.empty() && n_busy == 0) {
         if (S->admitter_done) break;
@@ -991,23 +1071,26 @@ void worker_streams(nlgb_server_s* S) {
       }
     }
     // retire finished chunks
-    cudaError_t e = cudaSuccess;
-    bool progress = false;
-    for (int i = 0; i < ns; ++i) {
-      Lane& l = lanes[(size_t)i];
-      if (!l.r || !done_flag[i].load()) continue;
-      done_flag[i].store(0);
-      e = retire(l);
-      if (e != cudaSuccess) break;
+    bool progress = have_admitted;
+    double tw = S->now();
+    ++w_loops;
+    for (Lane& l : lanes) {
+      if (!l.r || mirror_seq(l.m) == l.seq0) continue;
+      l.t_free = S->now();
+      retire(l);
       progress = true;
     }
-    if (e != cudaSuccess) {
-      std::lock_guard<std::mutex> lk(S->mu);
-      S->fatal = last_error();
-      S->cv_admit.notify_all();
-      break;
+    {
+      const double t = S->now();
+      w_retire += t - tw;
+      tw = t;
     }
-    complete_finished();
+    hand_over_finished();
+    {
+      const double t = S->now();
+      w_complete += t - tw;
+      tw = t;
+    }
     if (S->aborting) {
       // running chunks see the abort flag within one loop pass; when they
       // are all back, the active requests end as aborted
@@ -1018,14 +1101,13 @@ void worker_streams(nlgb_server_s* S) {
         if (S->admitter_done && S->admitted.empty()) break;
         S->cv_work.wait_for(lk, std::chrono::milliseconds(20));
       } else {
-        std::unique_lock<std::mutex> lk(S->mu);
-        S->cv_work.wait_for(lk, std::chrono::milliseconds(5), any_done);
+        std::this_thread::sleep_for(std::chrono::microseconds(100));
       }
       continue;
     }
     // give every free lane the least-work system that is not running
-    for (int li = 0; li < ns; ++li) {
-      Lane& l = lanes[(size_t)li];
+    cudaError_t e = cudaSuccess;
+    for (Lane& l : lanes) {
       if (l.r) continue;
       Req* best = nullptr;
       int bk = -1;
@@ -1048,32 +1130,52 @@ void worker_streams(nlgb_server_s* S) {
         e = chunk_fallback_fp64(best->slots[bk].view.st, l.s);
         best->need_fallback[bk] = 0;
       }
+      ChunkMirror* m = &S->mirrors[best->mirror_idx[bk]];
       l.r = best;
       l.k = bk;
+      l.m = m;
       l.iter_before = best->sys_iter[bk];
-      l.ms = 0.f;
+      l.seq0 = mirror_seq(m);
       best->running[bk] = 1;
+      // the budget is read by the chunk's first kernel
+      __atomic_store_n(&m->budget, iters, __ATOMIC_RELEASE);
+      const double tr = S->now();
+      if (l.t_free >= 0.0) w_gap += tr - l.t_free;
+      // (a system switched to FP64 after a stagnation gets its FP64 graph
+      // here; otherwise prepare keeps the graph)
       if (e == cudaSuccess)
-        e = best->graphs[bk]->run(best->slots[bk].view, iters, l.s, &l.ms, best->mixed_now[bk] != 0);
-      if (e == cudaSuccess)
-        e = cudaMemcpyAsync(l.h, best->slots[bk].view.st, sizeof(SysState), cudaMemcpyDeviceToHost, l.s);
-      if (e == cudaSuccess) e = cudaLaunchHostFunc(l.s, lane_finished, &signal[(size_t)li]);
+        e = best->graphs[bk]->prepare(best->slots[bk].view, best->mixed_now[bk] != 0, m, l.s);
+      if (e == cudaSuccess) e = best->graphs[bk]->launch(l.s);
+      w_run += S->now() - tr;
+      ++w_launches;
       busy_change(+1);
       progress = true;
       if (e != cudaSuccess) break;
     }
     if (e != cudaSuccess) {
       std::lock_guard<std::mutex> lk(S->mu);
-      S->fatal = last_error();
+      S->fatal = std::string("server chunk launch: ") + cudaGetErrorString(e);
       S->cv_admit.notify_all();
       break;
     }
+    {
+      const double t = S->now();
+      w_launch += t - tw;
+      tw = t;
+    }
     if (!progress) {
-      // sleep until a chunk finishes, a request is admitted or the server stops
-      std::unique_lock<std::mutex> lk(S->mu);
-      S->cv_work.wait_for(lk, std::chrono::milliseconds(n_busy > 0 ? 5 : 20), [&] {
-        return any_done() || !S->admitted.empty() || S->admitter_done || S->aborting;
-      });
+      // chunks in flight: poll their mirrors again shortly (the admission
+      // threads' notifications are seen at the top of the loop); idle: sleep
+      // until a request is admitted or the server stops
+      if (n_busy > 0) {
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
+      } else {
+        std::unique_lock<std::mutex> lk(S->mu);
+        S->cv_work.wait_for(lk, std::chrono::milliseconds(20), [&] {
+          return !S->admitted.empty() || S->admitter_done || S->aborting;
+        });
+      }
+      w_wait += S->now() - tw;
     }
   }
   for (Lane& l : lanes) if (l.s) cudaStreamSynchronize(l.s);
@@ -1095,10 +1197,16 @@ void worker_streams(nlgb_server_s* S) {
       if (!S->admitter_done) S->cv_work.wait_for(lk, std::chrono::milliseconds(20));
     }
   }
-  for (Lane& l : lanes) {
-    if (l.h) cudaFreeHost(l.h);
-    if (l.s) cudaStreamDestroy(l.s);
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->worker_done = true;
+    S->cv_complete.notify_all();
   }
+  if (S->trace)
+    std::fprintf(S->trace, "W,%.6f,%.6f,%.6f,%.6f,%.6f,%.6f,%.6f,%lld,%lld\n", S->now(), w_retire, w_complete,
+                 w_launch, w_run, w_wait, w_gap, w_loops, w_launches);
+  for (Lane& l : lanes)
+    if (l.s) cudaStreamDestroy(l.s);
   cudaStreamDestroy(su);
 }
 
@@ -1205,6 +1313,7 @@ nlgb_server nlgb_server_create(const nlgb_server_config* cfg) {
   if (cfg) S->cfg = *cfg;
   if (S->cfg.epoch_iters <= 0) S->cfg.epoch_iters = 256;
   if (S->cfg.max_systems <= 0) S->cfg.max_systems = 8192;
+  S->cfg.max_systems = std::min(S->cfg.max_systems, 65536);
   if (!(S->cfg.epoch_ms >= 0.0)) S->cfg.epoch_ms = 10.0;
   if (S->cfg.streams <= 0) S->cfg.streams = 16;
   S->cfg.streams = std::min(S->cfg.streams, 128);
@@ -1240,13 +1349,39 @@ nlgb_server nlgb_server_create(const nlgb_server_config* cfg) {
   }
   S->abort_host = static_cast<volatile int*>(flag);
   *S->abort_host = 0;
+  const bool streams = S->cfg.mode != NLGB_SERVER_SERIAL && S->cfg.schedule == NLGB_SCHEDULE_SRPT;
+  if (streams) {
+    // one chunk mirror per system that may be in flight; the graphs embed
+    // the device view of these pointers, the worker reads the host view
+    // (the same address under unified addressing, checked here)
+    void* mp = nullptr;
+    void* md = nullptr;
+    const size_t bytes = sizeof(ChunkMirror) * (size_t)S->cfg.max_systems;
+    if (cudaHostAlloc(&mp, bytes, cudaHostAllocMapped) != cudaSuccess ||
+        cudaHostGetDevicePointer(&md, mp, 0) != cudaSuccess || md != mp) {
+      set_error(std::string("nlgb_server_create: chunk mirrors: ") +
+                (md && md != mp ? "mapped pointer differs from the host pointer"
+                                : cudaGetErrorString(cudaGetLastError())));
+      if (mp) cudaFreeHost(mp);
+      cudaFreeHost(flag);
+      delete S;
+      return nullptr;
+    }
+    std::memset(mp, 0, bytes);
+    S->mirrors = static_cast<ChunkMirror*>(mp);
+    S->mirror_free.reserve((size_t)S->cfg.max_systems);
+    for (int i = S->cfg.max_systems - 1; i >= 0; --i) S->mirror_free.push_back(i);
+  }
   if (const char* tp = std::getenv("NLGB_SERVER_TRACE")) {
     S->trace = std::fopen(tp, "a");
     if (S->trace)
       std::fprintf(S->trace, "# E,t0,t1,kind,systems,teams,team_ctas,queue_ctas,grid,planned_GB,done_GB,ms,"
                              "team_ms_min,team_ms_med,team_ms_max,queue_ms,admits,admit_s,active_requests\n"
                              "# C,t,request,rhs,mixed,iter_before,iter_after,ms,status,stage\n"
-                             "# A,t,request,mesh_kind,n,seconds,bytes,arrival,graph_seconds,build_seconds,prepare_seconds\n");
+                             "# A,t,request,mesh_kind,n,seconds,bytes,arrival,graph_seconds,build_seconds,prepare_seconds\n"
+                             "# W,t,retire_s,complete_s,launch_s,graph_launch_s,wait_s,lane_idle_s,loops,launches\n"
+                             "# D,t,request,n,download_s,release_s\n"
+                             "# R,t,request,slots_s,graphs_s\n");
   }
   S->origin = Clock::now();
   S->th = std::thread(S->cfg.mode == NLGB_SERVER_SERIAL
@@ -1254,10 +1389,13 @@ nlgb_server nlgb_server_create(const nlgb_server_config* cfg) {
                           : (S->cfg.schedule == NLGB_SCHEDULE_SRPT ? worker_streams : worker_batched),
                       S);
   if (S->cfg.mode != NLGB_SERVER_SERIAL) {
-    // two admission threads: a request's upload and build overlap another's
+    // several admission threads: uploads, builds and graph instantiations
+    // of different requests overlap
     S->admitters_live = kAdmitters;
     for (int i = 0; i < kAdmitters; ++i) S->adm_th.emplace_back(admitter, S);
   }
+  if (streams)
+    for (int i = 0; i < kCompleters; ++i) S->cmp_th.emplace_back(completer, S);
   return S;
 }
 
@@ -1448,6 +1586,10 @@ void nlgb_server_destroy(nlgb_server S) {
   if (S->th.joinable()) S->th.join();
   for (std::thread& t : S->adm_th)
     if (t.joinable()) t.join();
+  for (std::thread& t : S->cmp_th)
+    if (t.joinable()) t.join();
+  S->graveyard.clear();
+  if (S->mirrors) cudaFreeHost(S->mirrors);
   if (S->abort_host) cudaFreeHost(const_cast<int*>(S->abort_host));
   if (S->trace) std::fclose(S->trace);
   delete S;

@@ -327,6 +327,44 @@ __global__ void k_chunk_end(SysState* st) {
   if (st->status != ST_RUNNING) st->stage = 3;
 }
 
+__device__ __forceinline__ unsigned long long chunk_clock_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Mirrored chunks (ChunkMirror): the budget comes from host-mapped memory
+// written before the launch; the start time is kept there for the end.
+__global__ void k_chunk_start_m(SysState* st, ChunkMirror* m, int unroll) {
+  const long long budget = *reinterpret_cast<volatile long long*>(&m->budget);
+  const long long iters = budget > 0 ? budget : 1;
+  st->iter_stop = st->iter + iters;
+  st->guard_cap = st->guard + iters / unroll + 4;
+  *reinterpret_cast<volatile unsigned long long*>(&m->t_start) = chunk_clock_ns();
+}
+
+// End of a mirrored chunk (one warp): the k_chunk_end rule, then the state
+// copied to the mirror, the duration, a system-scope fence by every lane,
+// and last the sequence number the host polls.
+__global__ void k_chunk_end_m(SysState* st, ChunkMirror* m) {
+  if (threadIdx.x == 0 && st->status != ST_RUNNING) st->stage = 3;
+  __syncwarp();
+  static_assert(sizeof(SysState) % 8 == 0, "SysState is copied in 8-byte words");
+  const unsigned long long* src = reinterpret_cast<const unsigned long long*>(st);
+  volatile unsigned long long* dst = reinterpret_cast<volatile unsigned long long*>(&m->st);
+  for (int i = (int)threadIdx.x; i < (int)(sizeof(SysState) / 8); i += (int)blockDim.x) dst[i] = __ldcg(src + i);
+  if (threadIdx.x == 0) {
+    const unsigned long long t0 = *reinterpret_cast<volatile unsigned long long*>(&m->t_start);
+    *reinterpret_cast<volatile unsigned long long*>(&m->t_ns) = chunk_clock_ns() - t0;
+  }
+  __threadfence_system();
+  __syncwarp();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* seq = &m->seq;
+    *seq = *seq + 1u;
+  }
+}
+
 // After the final residual: the true-residual check (single thread).  A
 // continuation sets the status back to running and stage 4.
 __global__ void k_check(SysState* st) {
@@ -1184,11 +1222,15 @@ cudaError_t ViewGraph::build(const SysView& v, bool mixed) {
   SysState* st = v.st;
   void* ae[] = {&st};
   const int vg = (v.n_tiles + vec_tiles_for(v.tile_rows) - 1) / vec_tiles_for(v.tile_rows);
-  cudaGraphNode_t n_start, n_loop, n_fin, n_end, prev = nullptr;
+  cudaGraphNode_t n_start, n_loop, n_fin, n_end, prev = nullptr, n_first = nullptr;
   cudaGraph_t body;
+  ChunkMirror* mirror = mirror_;
+  int unroll = kUnrollPlain;
+  void* am[] = {&st, &mirror, &unroll};
+  if (mirror_) NLGB_CUDA_TRY(add_kernel(g, &n_first, nullptr, (const void*)k_chunk_start_m, 1, 1, am));
   if (!mixed) {
     cudaGraphNode_t n_init, n_res;
-    NLGB_CUDA_TRY(add_kernel(g, &n_init, nullptr, ks.init_chunk, v.n_tiles, kCTA, a1));
+    NLGB_CUDA_TRY(add_kernel(g, &n_init, n_first, ks.init_chunk, v.n_tiles, kCTA, a1));
     NLGB_CUDA_TRY(add_kernel(g, &n_res, n_init, ks.resume_p, vg, kCTA, a1));
     NLGB_CUDA_TRY(add_kernel(g, &n_start, n_res, (const void*)k_resume_mark, 1, 1, ae));
     NLGB_CUDA_TRY(add_while(g, &n_loop, n_start, h, &body));
@@ -1201,7 +1243,7 @@ cudaError_t ViewGraph::build(const SysView& v, bool mixed) {
     }
   } else {
     cudaGraphNode_t n_outer;
-    NLGB_CUDA_TRY(add_kernel(g, &n_outer, nullptr, ks.mx_outer, v.n_tiles, kCTA, a1));
+    NLGB_CUDA_TRY(add_kernel(g, &n_outer, n_first, ks.mx_outer, v.n_tiles, kCTA, a1));
     NLGB_CUDA_TRY(add_kernel(g, &n_start, n_outer, (const void*)k_mark_started, 1, 1, ae));
     NLGB_CUDA_TRY(add_while(g, &n_loop, n_start, h, &body));
     for (int u = 0; u < kUnrollInner; ++u) {
@@ -1230,7 +1272,12 @@ cudaError_t ViewGraph::build(const SysView& v, bool mixed) {
     NLGB_CUDA_TRY(add_kernel(g, &n_chk, n_fin, (const void*)k_check, 1, 1, ae));
     n_fin = n_chk;
   }
-  NLGB_CUDA_TRY(add_kernel(g, &n_end, n_fin, (const void*)k_chunk_end, 1, 1, ae));
+  if (mirror_) {
+    void* aem[] = {&st, &mirror};
+    NLGB_CUDA_TRY(add_kernel(g, &n_end, n_fin, (const void*)k_chunk_end_m, 1, 32, aem));
+  } else {
+    NLGB_CUDA_TRY(add_kernel(g, &n_end, n_fin, (const void*)k_chunk_end, 1, 1, ae));
+  }
   cudaError_t e = cudaGraphInstantiate(&exec_, g, 0);
   cudaGraphDestroy(g);
   NLGB_CUDA_TRY(e);
@@ -1249,9 +1296,37 @@ static bool same_view(const SysView& a, const SysView& b) {
          a.q32 == b.q32 && a.c32 == b.c32 && a.abort_flag == b.abort_flag;
 }
 
-cudaError_t ViewGraph::prepare(const SysView& v, bool mixed) {
-  if (!exec_ || mixed != mixed_ || !same_view(v, view_)) NLGB_CUDA_TRY(build(v, mixed));
+cudaError_t ViewGraph::prepare(const SysView& v, bool mixed) { return prepare(v, mixed, nullptr); }
+
+cudaError_t ViewGraph::prepare(const SysView& v, bool mixed, ChunkMirror* m, cudaStream_t upload) {
+  if (!exec_ || mixed != mixed_ || m != mirror_ || !same_view(v, view_)) {
+    mirror_ = m;
+    NLGB_CUDA_TRY(build(v, mixed));
+    if (upload) NLGB_CUDA_TRY(cudaGraphUpload(exec_, upload));
+  }
   return cudaSuccess;
+}
+
+cudaError_t ViewGraph::launch(cudaStream_t s) {
+  if (!mirror_) return cudaErrorInvalidValue;
+  if (eager_mode()) {
+    k_chunk_start_m<<<1, 1, 0, s>>>(view_.st, mirror_, kUnrollPlain);
+    NLGB_CUDA_TRY(cudaGetLastError());
+    const long long budget = *reinterpret_cast<volatile long long*>(&mirror_->budget);
+    return run_eager(s, budget > 0 ? budget : 1);
+  }
+  if (!exec_) return cudaErrorInvalidValue;
+  return cudaGraphLaunch(exec_, s);
+}
+
+void ViewGraph::account(long long iters_before, long long iters_after) {
+  if (eager_counted_) {   // run_eager counted its launches (plus the chunk start)
+    eager_counted_ = false;
+    count_launches(1);
+    return;
+  }
+  const long long passes = (std::max(0LL, iters_after - iters_before) + kUnrollPlain - 1) / kUnrollPlain;
+  count_launches((mixed_ ? 5 : 7) + std::max(1LL, passes) * (3LL * kUnrollPlain + 1));
 }
 
 cudaError_t ViewGraph::run(const SysView& v, long long iters, cudaStream_t s, float* ms, bool mixed) {
@@ -1332,7 +1407,13 @@ cudaError_t ViewGraph::run_eager(cudaStream_t s, long long iters) {
   }
   NLGB_CUDA_TRY(go(ks.fin_if, view_.n_tiles, kCTA, a1));
   if (!mixed_) NLGB_CUDA_TRY(go((const void*)k_check, 1, 1, ae));
-  NLGB_CUDA_TRY(go((const void*)k_chunk_end, 1, 1, ae));
+  if (mirror_) {
+    ChunkMirror* mirror = mirror_;
+    void* aem[] = {&st, &mirror};
+    NLGB_CUDA_TRY(go((const void*)k_chunk_end_m, 1, 32, aem));
+  } else {
+    NLGB_CUDA_TRY(go((const void*)k_chunk_end, 1, 1, ae));
+  }
   count_launches(launched);
   eager_counted_ = true;
   return cudaSuccess;
@@ -1343,16 +1424,10 @@ cudaError_t ViewGraph::finish(long long iters_before, long long iters_after) {
   pending_ = false;
   NLGB_CUDA_TRY(cudaEventSynchronize(e1_));
   if (ms_) NLGB_CUDA_TRY(cudaEventElapsedTime(ms_, e0_, e1_));
-  if (eager_counted_) {   // run_eager counted its launches (plus the chunk start)
-    eager_counted_ = false;
-    count_launches(1);
-    return cudaSuccess;
-  }
   // kernels executed: chunk start and end, the fixed nodes before and after
   // the loop, and per while-body pass 3 kernels per unrolled iteration + the
   // guard (mixed: + 2 per reliable update, counted as passes x 1 here)
-  const long long passes = (std::max(0LL, iters_after - iters_before) + kUnrollPlain - 1) / kUnrollPlain;
-  count_launches((mixed_ ? 5 : 7) + std::max(1LL, passes) * (3LL * kUnrollPlain + 1));
+  account(iters_before, iters_after);
   return cudaSuccess;
 }
 

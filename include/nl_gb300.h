@@ -209,7 +209,7 @@ typedef struct {
     long long max_iter;          /* < 0: 5 n per system                         */
     double    inner_eps;         /* mixed reliable-update factor (0.1)         */
     long long epoch_iters;       /* iterations per system per epoch (256)      */
-    int       max_systems;       /* active systems at once (default 8192)      */
+    int       max_systems;       /* active systems at once (8192; <= 65536)    */
     int       schedule;          /* NLGB_SCHEDULE_SRPT (default) / _ALL         */
     double    epoch_ms;          /* SRPT: target length of a chunk (10 ms)     */
     int       streams;           /* SRPT: concurrent chunks (default 16)        */
