@@ -99,15 +99,23 @@ def parse_args():
     p.add_argument("--profile-case", choices=["spmv", "batch", "batch_small", "batch_lscm", "plain", "mixed",
                                               "plain_lscm", "mixed_lscm", "df_lscm", "kernels"], default=None,
                    help="run one small case for an ncu capture and exit")
-    p.add_argument("--workload", choices=["stream", "configs"], default="stream",
-                   help="configs: measure the other benchmark configurations and exit")
+    p.add_argument("--workload", choices=["stream", "configs", "sweep"], default="stream",
+                   help="configs: measure the other benchmark configurations and exit; sweep: the "
+                        "serving stream at several arrival rates (--rates, --windows), both arms")
+    p.add_argument("--charts", type=int, default=256, help="configs: charts of the batched uneven LSCM case")
+    p.add_argument("--rates", type=str, default="100,1000,10000", help="sweep: arrival rates (requests/s)")
+    p.add_argument("--windows", type=str, default="60,6,0.6", help="sweep: arrival window per rate (s)")
     return p.parse_args()
 
 
-def measure_configs():
-    """Configs 1, 2, 3 (reduced: 256 charts) and 5 -- plain FP64 vs mixed,
-    serial vs batched -- one JSON line (device times from CUDA events)."""
+def measure_configs(args):
+    """Configs 1, 2, 3 (`--charts` charts) and 5 -- plain FP64 vs mixed,
+    serial vs batched, errors against the FP64 oracles -- one JSON line
+    (device times from CUDA events)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
     from graphitethree_gb300 import meshes, solver, systems
+    from oracle import oracle
     out = {"workload": "configs"}
     t_start = time.perf_counter()
 
@@ -126,20 +134,38 @@ def measure_configs():
     out["config1_lscm256"] = {"assembly_s": asm,
                               "plain": rec(M1.solve(rhs1[0])[1], M1.n, M1.nnz),
                               "mixed": rec(M1.solve(rhs1[0], precision="mixed")[1], M1.n, M1.nnz)}
+    def errors(x, ref):
+        d = np.abs(x - ref)
+        return {"max_abs_over_max": float(d.max() / max(np.abs(ref).max(), 1e-300)),
+                "rel_2norm": float(np.linalg.norm(x - ref) / max(np.linalg.norm(ref), 1e-300))}
+
     progress("config 2")
     fs = systems.fairing_system(2048, 2048, seed=2)
     A = solver.Matrix(fs.rp, fs.ci, fs.va)
-    out["config2_fairing2048"] = {f"rhs{k}_{p}": rec(A.solve(fs.rhs[k], precision=p)[1], A.n, A.nnz)
-                                  for k in range(3) for p in ("double", "mixed")}
+    c2 = {}
+    for k in range(3):
+        # per coordinate: both forms against the oracle's FP64 Jacobi-PCG run
+        # to 1e-14 (kappa ~ 1e3; the C oracle, all host threads)
+        t0 = time.perf_counter()
+        xo, st, it, rr = oracle.pcg(fs.rp, fs.ci, fs.va, fs.rhs[k], eps=1e-14)
+        c2[f"rhs{k}_oracle"] = {"iterations": int(it), "converged": int(st) == 1,
+                                "seconds": time.perf_counter() - t0}
+        for p in ("double", "mixed"):
+            x, inf = A.solve(fs.rhs[k], precision=p)
+            c2[f"rhs{k}_{p}"] = rec(inf, A.n, A.nnz)
+            c2[f"rhs{k}_{p}"]["error_vs_oracle_pcg_1e-14"] = errors(x, xo)
+    out["config2_fairing2048"] = c2
     A.close()
-    progress("config 3: assembling charts")
-    nx, ny = meshes.chart_sizes(256, seed=3, side_min=16, side_max=512)
-    mats, bs, unknowns = [], [], 0
-    for c in range(256):
-        M, rhs, _ = solver.assemble(systems.lscm_system(int(nx[c]), int(ny[c]), seed=1000 + c))
-        mats.append(M); bs.append(rhs[0]); unknowns += M.n
-    c3 = {"charts": 256, "unknowns": unknowns,
-          "sides": "long side log-uniform [16,512], aspect log-uniform [1,4]"}
+    progress(f"config 3: building {args.charts} charts on the GPU")
+    nx, ny = meshes.chart_sizes(args.charts, seed=3, side_min=16, side_max=512)
+    mats, bs, unknowns, build_s = [], [], 0, 0.0
+    for c in range(args.charts):
+        V, F = meshes.height_field(int(nx[c]), int(ny[c]), 1000 + c)
+        M, rhs, secs = solver.build_lscm(V, F)
+        mats.append(M); bs.append(rhs); unknowns += M.n; build_s += secs
+    c3 = {"charts": args.charts, "unknowns": unknowns, "gpu_build_s": build_s,
+          "sides": "long side log-uniform [16,512], aspect log-uniform [1,4]; LSCM systems built on "
+                   "the GPU from each chart's mesh (nlgb_build_lscm, pins 0 and nv-1)"}
     for p in ("double", "mixed"):
         progress(f"config 3: batched {p} ({unknowns} unknowns)")
         xs, infos, ks = solver.batch_solve(mats, bs, precision=p)
@@ -148,11 +174,18 @@ def measure_configs():
         c3[f"batched_{p}_s"] = ks
         c3[f"batched_{p}_converged"] = sum(i.status == "converged" for i in infos)
     progress("config 3: serial plain")
-    serial = 0.0
+    serial, serial_iters = 0.0, 0
     for M, b in zip(mats, bs):
-        serial += M.solve(b)[1].seconds
+        inf = M.solve(b)[1]
+        serial += inf.seconds
+        serial_iters += inf.iterations
     c3["serial_plain_s"] = serial
-    out["config3_charts_reduced"] = c3
+    c3["serial_plain_iterations"] = serial_iters
+    c3["batched_speedup_double"] = serial / c3["batched_double_s"] if c3["batched_double_s"] > 0 else None
+    c3["batched_speedup_mixed"] = serial / c3["batched_mixed_s"] if c3["batched_mixed_s"] > 0 else None
+    for M in mats:
+        M.close()
+    out["config3_charts"] = c3
     progress("mesh builders")
     V1, F1 = meshes.height_field(256, 256, seed=1)
     V2, F2 = meshes.height_field(2048, 2048, seed=2)
@@ -191,9 +224,107 @@ def measure_configs():
     progress("config 5")
     f5 = systems.fairing_system(1024, 1024, seed=5, lam=1e-4, n_rhs=1, stretch_bands=16, rhs_normal=True)
     A5 = solver.Matrix(f5.rp, f5.ci, f5.va)
-    out["config5_stretched"] = {"plain_1e-12": rec(A5.solve(f5.rhs[0], eps=1e-12)[1], A5.n, A5.nnz),
-                                "mixed_1e-12": rec(A5.solve(f5.rhs[0], eps=1e-12, precision="mixed")[1],
-                                                   A5.n, A5.nnz)}
+    x5, i5 = A5.solve(f5.rhs[0], eps=1e-12)
+    x5m, i5m = A5.solve(f5.rhs[0], eps=1e-12, precision="mixed")
+    c5 = {"plain_1e-12": rec(i5, A5.n, A5.nnz), "mixed_1e-12": rec(i5m, A5.n, A5.nnz)}
+    A5.close()
+    progress("config 5: FP64 direct oracle (SuperLU)")
+    t0 = time.perf_counter()
+    Ah = sp.csr_matrix((f5.va, f5.ci, f5.rp), shape=(f5.n, f5.n)).tocsc()
+    xd = spla.spsolve(Ah, f5.rhs[0])
+    c5["direct_oracle"] = {"seconds": time.perf_counter() - t0,
+                           "rel_residual": float(np.linalg.norm(Ah @ xd - f5.rhs[0]) / np.linalg.norm(f5.rhs[0])),
+                           "note": "backward stable: its own forward error is up to ~kappa x 1e-16 ~ 1e-8"}
+    c5["plain_1e-12"]["error_vs_direct"] = errors(x5, xd)
+    c5["mixed_1e-12"]["error_vs_direct"] = errors(x5m, xd)
+    out["config5_stretched"] = c5
+    print(json.dumps(out))
+
+
+def run_sweep(args):
+    """The serving stream at each rate of --rates over the matching window of
+    --windows, through the batched server (AUTO precision) and the serial
+    plain-FP64 server.  Requests are drawn cyclically from the seeded 4-s
+    window at 100/s (405 meshes; every request is uploaded, built and solved
+    from scratch, nothing is shared between requests on the device) and
+    submitted in real time by a submitter thread.  One JSON line."""
+    import dataclasses
+    from graphitethree_gb300 import solver, systems
+    pool = systems.stream_window(100.0, 4.0, args.seed)
+    rates = [float(v) for v in args.rates.split(",")]
+    windows = [float(v) for v in args.windows.split(",")]
+    out = {"workload": "sweep", "pool_requests": len(pool), "drain_s": args.drain, "rows": []}
+    for rate, window in zip(rates, windows):
+        rng = np.random.default_rng(args.seed + int(rate))
+        t, reqs = 0.0, []
+        while True:
+            t += float(rng.exponential(1.0 / rate))
+            if t >= window:
+                break
+            reqs.append(dataclasses.replace(pool[len(reqs) % len(pool)], rid=len(reqs), arrival=t))
+        row = {"rate_per_s": rate, "window_s": window, "requests": len(reqs)}
+        for arm, mode, prec in (("batched_auto", "batched", "auto"), ("serial_fp64", "serial", "double")):
+            srv = solver.Server(budget_bytes=args.budget_gb * 1e9, precision=prec, mode=mode, eps=args.eps,
+                                streams=args.streams)
+            srv.reset_clock()
+            T0 = 0.5
+            tickets = [None] * len(reqs)
+            lag = [0.0]
+
+            t_end = T0 + window + args.drain
+
+            def submitter():
+                # a request not submitted by the end of the step (the host
+                # copies fell behind the arrivals) counts as not completed
+                for i, r in enumerate(reqs):
+                    dt = T0 + r.arrival - srv.now()
+                    if dt > 0:
+                        time.sleep(dt)
+                    if srv.now() >= t_end:
+                        break
+                    lag[0] = max(lag[0], srv.now() - (T0 + r.arrival))
+                    try:
+                        tickets[i] = srv.submit_mesh(r.kind, r.V, r.F, b=r.b, lam=r.lam,
+                                                     arrival=T0 + r.arrival)
+                    except solver.SolverError:
+                        break
+
+            th = threading.Thread(target=submitter)
+            th.start()
+            while srv.now() < t_end:
+                time.sleep(min(0.05, max(0.0, t_end - srv.now())))
+            srv.abort()
+            th.join()
+            lat_all, lat_done = [], []
+            for r, tk in zip(reqs, tickets):
+                arr = T0 + r.arrival
+                ok = False
+                if tk is not None:
+                    try:
+                        x, inf, lat = srv.wait(tk)
+                        ok = arr + lat <= t_end
+                    except solver.SolverError:
+                        ok = False
+                if ok:
+                    lat_all.append(lat)
+                    lat_done.append(lat)
+                else:
+                    lat_all.append(max(0.0, t_end - arr))
+            st = srv.stats()
+            srv.close()
+            span = window + args.drain
+            row[arm] = {"completed": len(lat_done), "solves_per_s": len(lat_done) / span,
+                        "submitted": sum(tk is not None for tk in tickets),
+                        "p50_s": pct(lat_all, 50), "p99_s": pct(lat_all, 99),
+                        "completed_p50_s": pct(lat_done, 50), "completed_p99_s": pct(lat_done, 99),
+                        "censored_fraction": 1.0 - len(lat_done) / max(1, len(reqs)),
+                        "peak_admitted_gb": st["peak_bytes"] / 1e9,
+                        "mean_admitted_gb": st["byte_seconds"] / t_end / 1e9,
+                        "max_submit_lag_s": lag[0]}
+            print(f"[sweep] rate {rate} window {window}: {arm} {row[arm]}", file=sys.stderr, flush=True)
+        b, s = row["batched_auto"]["solves_per_s"], row["serial_fp64"]["solves_per_s"]
+        row["speedup"] = b / s if s > 0 else None
+        out["rows"].append(row)
     print(json.dumps(out))
 
 
@@ -587,7 +718,10 @@ def main():
         profile_case(args.profile_case)
         return
     if args.workload == "configs":
-        measure_configs()
+        measure_configs(args)
+        return
+    if args.workload == "sweep":
+        run_sweep(args)
         return
     if args.impl == "reference":
         if rank == 0:

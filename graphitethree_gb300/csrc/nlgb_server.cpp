@@ -574,16 +574,29 @@ void admitter(nlgb_server_s* S) {
       ++j;
     }
     S->future.erase(S->future.begin(), S->future.begin() + (long)j);
-    // first fit in arrival order
+    // SRPT schedule: of the arrived requests that fit the HBM budget, the
+    // one with the least estimated work (its footprint, which scales with
+    // the bytes of an iteration, times sqrt(n) for the O(sqrt(n)) Jacobi-CG
+    // iterations of a 2D mesh operator); under overload the budget then
+    // holds the requests that can finish soonest instead of the oldest.
+    // ALL schedule: first fit in arrival order.
+    const bool shortest = S->cfg.schedule == NLGB_SCHEDULE_SRPT;
     Req* pick = nullptr;
+    size_t pick_i = 0;
+    double pick_key = 0.0;
     for (size_t i = 0; i < S->pending.size(); ++i) {
       Req* r = S->pending[i];
-      if (S->used + r->bytes <= S->cfg.hbm_budget_bytes && S->sys_in_flight + r->n_rhs <= S->cfg.max_systems) {
+      if (S->used + r->bytes > S->cfg.hbm_budget_bytes || S->sys_in_flight + r->n_rhs > S->cfg.max_systems)
+        continue;
+      const double key = double(r->bytes) * std::sqrt(double(std::max(1, r->n)));
+      if (!pick || (shortest && key < pick_key)) {
         pick = r;
-        S->pending.erase(S->pending.begin() + (long)i);
-        break;
+        pick_i = i;
+        pick_key = key;
+        if (!shortest) break;
       }
     }
+    if (pick) S->pending.erase(S->pending.begin() + (long)pick_i);
     if (pick) {
       add_used_locked(S, (long long)pick->bytes);
       S->sys_in_flight += pick->n_rhs;
