@@ -10,17 +10,19 @@ in [1e3, 1e6], a seeded square-ish grid patch with the bump model -- replayed
 in real time through the C ABI (nlgb_server_submit_mesh with host buffers:
 the server uploads the mesh, builds the system on the GPU, solves, and
 copies the solution back to the host) to the continuous-batching server
-(HBM budget 150 GB, least-attained-service epochs, precision AUTO: mixed
-FP32/FP64 for the square fairing systems, FP64 for the least-squares LSCM
-normal equations).  The step ends `--drain` seconds after the window; the
-server is then aborted.  Every step replays the same seeded stream from
-scratch (upload, build, solve, download: nothing is cached).
+(HBM budget 150 GB, shortest-work-first admission, `--streams` concurrent
+CUDA streams running chunks of the PCG iteration graph, the system with the
+least estimated remaining work first; precision AUTO: mixed FP32/FP64 for
+the square fairing systems, FP64 for the least-squares LSCM normal
+equations).  The step ends `--drain` seconds after the window; the server is
+then aborted.  Every step replays the same seeded stream from scratch
+(upload, build, solve, download: nothing is cached).
 
 Reported:
   e2e         completed requests / (window + drain): a request counts when
               its solution is on the host before the step ends;
-  value       completed requests / device time of the server's solver
-              epochs in the step (the GPU-side throughput);
+  value       completed requests / time during which the server had
+              at least one chunk in flight (the GPU-side throughput);
   latency     p50 / p99 from arrival to solution on the host over every
               request of the window, an unfinished one counted as censored
               at the end of the step (p50 / p99 of the completed ones
@@ -28,9 +30,9 @@ Reported:
   plain_fp64  the same stream through the serial FP64 server (graph-captured
               single-system PCG, one request at a time, first come first
               served);
-  roofline    achieved algorithmic GB/s (bytes from the iteration counts,
-              CUDA-event time) of the executor that dominates the step vs the
-              measured HBM peak; roofline_other: the other one;
+  roofline    achieved algorithmic GB/s of the step's chunk kernels (bytes
+              from the iteration counts, over the time with a chunk in
+              flight) vs the measured HBM peak;
   spmv_fp64   the FP64 CRS SpMV on the 2048^2 cotangent Laplacian (4.2M
               rows, 29.3M nonzeros) vs the measured HBM peak;
   parity      statuses and true residuals of the completed requests, and
@@ -43,6 +45,8 @@ Reported:
   hbm         peak and mean device footprint admitted by the server.
 `--impl reference` runs only the CPU reference arm (the oracle port: the
 reference's own OpenNL source is not in the checkout) and prints its line.
+`--workload sweep` runs the stream at several arrival rates (both arms),
+`--workload configs` the other benchmark configurations.
 """
 from __future__ import annotations
 
@@ -96,8 +100,9 @@ def parse_args():
     p.add_argument("--no-parity", action="store_true")
     p.add_argument("--parity-max-unknowns", type=int, default=300_000,
                    help="largest completed request checked against the direct oracle")
-    p.add_argument("--profile-case", choices=["spmv", "batch", "batch_small", "batch_lscm", "plain", "mixed",
-                                              "plain_lscm", "mixed_lscm", "df_lscm", "kernels"], default=None,
+    p.add_argument("--profile-case", choices=["spmv", "batch", "batch_small", "batch_lscm", "stream_mid",
+                                              "plain", "mixed", "plain_lscm", "mixed_lscm", "df_lscm",
+                                              "kernels"], default=None,
                    help="run one small case for an ncu capture and exit")
     p.add_argument("--workload", choices=["stream", "configs", "sweep"], default="stream",
                    help="configs: measure the other benchmark configurations and exit; sweep: the "
@@ -134,6 +139,16 @@ def measure_configs(args):
     out["config1_lscm256"] = {"assembly_s": asm,
                               "plain": rec(M1.solve(rhs1[0])[1], M1.n, M1.nnz),
                               "mixed": rec(M1.solve(rhs1[0], precision="mixed")[1], M1.n, M1.nnz)}
+    progress("SSOR vs Jacobi (context API)")
+    rs_s = systems.lscm_system(128, 128, seed=4)
+    ssor = {"system": "LSCM 128^2 (32,764 unknowns), nlSolve with NL_PRECONDITIONER"}
+    for pc in ("jacobi", "ssor"):
+        solver.solve_opennl(rs_s, preconditioner=pc, max_iter=8)          # warm-up
+        _, inf = solver.solve_opennl(rs_s, preconditioner=pc)
+        ssor[pc] = {k: inf[k] for k in ("status", "iterations", "elapsed", "true_error")}
+        ssor[pc]["us_per_iteration"] = 1e6 * inf["elapsed"] / max(1, inf["iterations"])
+    out["ssor"] = ssor
+
     def errors(x, ref):
         d = np.abs(x - ref)
         return {"max_abs_over_max": float(d.max() / max(np.abs(ref).max(), 1e-300)),
@@ -406,6 +421,23 @@ def profile_case(which):
         print(json.dumps({"case": which, "kernel_ms": ks * 1e3, "iterations": infos[0].iterations,
                           "us_per_iteration": 1e3 * ks * 1e3 / max(1, infos[0].iterations)}))
         return
+    if which == "stream_mid":
+        # mid-size requests of the serving stream through the server's
+        # stream executor (chunk kernels launched one by one): an LSCM mesh
+        # of 150^2 vertices (44,996 unknowns) and a fairing mesh of 300^2
+        # (90,000 unknowns, 3 right-hand sides), 48 FP64 iterations each
+        from graphitethree_gb300 import meshes
+        os.environ["NLGB_EAGER_SOLVE"] = "1"
+        srv = solver.Server(precision="double", eps=1e-30, max_iter=48, budget_bytes=4e9)
+        V1, F1 = meshes.height_field(150, 150, 11)
+        V2, F2 = meshes.height_field(300, 300, 12)
+        b2 = np.ascontiguousarray(1e-2 * V2.T)
+        t1 = srv.submit_mesh("lscm", V1, F1)
+        t2 = srv.submit_mesh("fairing", V2, F2, b=b2, lam=1e-2)
+        i1, i2 = srv.wait(t1)[1], srv.wait(t2)[1]
+        srv.close()
+        print(json.dumps({"case": which, "iterations": [i.iterations for i in i1 + i2]}))
+        return
     if which == "batch_small":
         # one small LSCM system (4,604 unknowns, 35 tiles) in the persistent
         # kernel: a latency-bound team of 35 CTAs, 1000 FP64 iterations
@@ -618,11 +650,18 @@ def oracle_errors(stream, res, args):
                "requests_checked": len(jobs), "requests_completed": len(res["done_ids"]),
                "max_unknowns_checked": max([j[0] for j in jobs], default=0),
                "seconds": time.perf_counter() - t0}
+    above = 0
     for kind in ("lscm", "fairing"):
         for what in ("direct", "pcg"):
             v = out[kind][what]
             summary[f"{kind}_{what}"] = {"systems": len(v), "max": max(v, default=None),
                                         "above_1e-8": int(sum(e > 1e-8 for e in v))}
+            above += summary[f"{kind}_{what}"]["above_1e-8"]
+    # the benchmark spec's bar, stated as pass / fail over every checked system
+    summary["all_within_1e-8"] = above == 0
+    summary["note"] = ("at a relative residual of 1e-10 the error of any solution, the oracle's own PCG "
+                       "included, is bounded only by kappa x 1e-10; the LSCM normal equations have "
+                       "kappa up to ~1e6 after Jacobi scaling")
     return summary
 
 
@@ -794,7 +833,6 @@ def main():
                                 "capture of k_spmv_pq on the 1.3M-unknown LSCM system (the vector kernels "
                                 "stream exactly their bytes), times this workload's algorithmic bytes per chunk",
                 "fp64_note": "the FP64 phases are co-limited by GB300's FP64 pipe, not only by HBM"}
-    other = None
 
     infos = [i for infs in last["infos"].values() for i in infs]
     statuses = {}
@@ -842,7 +880,6 @@ def main():
                     "censored_fraction": 1.0 - len(lat_done) / max(1, len(lat_all)), "unit": "s"},
         "plain_fp64": plain,
         "roofline": roofline,
-        "roofline_other": other,
         "spmv_fp64": spmv,
         "cpu_baseline": cpu,
         "cpu_baseline_1thread": None if cpu1 is None else {k: cpu1[k] for k in ("value", "unit", "cores",
