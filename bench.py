@@ -91,9 +91,16 @@ def parse_args():
     p.add_argument("--lead", type=float, default=1.5,
                    help="submission lead time before the window opens (s; not timed)")
     p.add_argument("--eps", type=float, default=1e-10)
+    p.add_argument("--eps-lsq", type=float, default=3e-11,
+                   help="relative residual of the least-squares (LSCM) requests, every arm: the "
+                        "normal equations square kappa, and at 1e-10 a few LSCM solutions of the "
+                        "stream sit just above 1e-8 from the direct solve")
     p.add_argument("--budget-gb", type=float, default=150.0)
     p.add_argument("--plain-steps", type=int, default=2, help="steps of the serial plain-FP64 arm")
     p.add_argument("--streams", type=int, default=16, help="concurrent chunk streams of the batched server")
+    p.add_argument("--min-tile-rows", type=int, default=1024,
+                   help="batched server: minimum rows per tile (fewer, fuller CTAs per system when "
+                        "16 streams share the GPU; the serial arm keeps the single-system tiling)")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-spmv", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
@@ -280,7 +287,8 @@ def run_sweep(args):
         row = {"rate_per_s": rate, "window_s": window, "requests": len(reqs)}
         for arm, mode, prec in (("batched_auto", "batched", "auto"), ("serial_fp64", "serial", "double")):
             srv = solver.Server(budget_bytes=args.budget_gb * 1e9, precision=prec, mode=mode, eps=args.eps,
-                                streams=args.streams)
+                                streams=args.streams, eps_least_squares=args.eps_lsq,
+                                min_tile_rows=args.min_tile_rows if mode == "batched" else 0)
             srv.reset_clock()
             T0 = 0.5
             tickets = [None] * len(reqs)
@@ -557,7 +565,8 @@ def run_stream(stream, args, mode: str, precision: str, keep_x: bool = False):
     `drain` seconds after the window, abort what is left.  Returns a dict."""
     from graphitethree_gb300 import solver
     srv = solver.Server(budget_bytes=args.budget_gb * 1e9, precision=precision, mode=mode, eps=args.eps,
-                        streams=args.streams)
+                        streams=args.streams, eps_least_squares=args.eps_lsq,
+                        min_tile_rows=args.min_tile_rows if mode == "batched" else 0)
     srv.reset_clock()
     T0 = args.lead
     tickets = [srv.submit_mesh(r.kind, r.V, r.F, b=r.b, lam=r.lam, arrival=T0 + r.arrival) for r in stream]
@@ -633,7 +642,8 @@ def oracle_errors(stream, res, args):
     for rid in res["done_ids"]:
         r = by_id[rid]
         if r.unknowns <= args.parity_max_unknowns and rid in res["xs"]:
-            jobs.append((r.unknowns, (r.kind, r.V, r.F, r.b, r.lam, res["xs"][rid], args.eps, pcg_max)))
+            eps = args.eps_lsq if r.kind == "lscm" else args.eps
+            jobs.append((r.unknowns, (r.kind, r.V, r.F, r.b, r.lam, res["xs"][rid], eps, pcg_max)))
     jobs.sort(key=lambda j: -j[0])
     workers = max(1, min(16, (os.cpu_count() or 2) - 1))
     t0 = time.perf_counter()
@@ -687,7 +697,8 @@ def cpu_stream(stream, args, threads):
             if left <= 0:
                 ok = False
                 break
-            _, status, _, _ = oracle.pcg(rp, ci, va, rhs[k], eps=args.eps, nthreads=threads, max_seconds=left)
+            eps = args.eps_lsq if r.kind == "lscm" else args.eps
+            _, status, _, _ = oracle.pcg(rp, ci, va, rhs[k], eps=eps, nthreads=threads, max_seconds=left)
             if status != 1:
                 ok = False
                 break
@@ -699,7 +710,7 @@ def cpu_stream(stream, args, threads):
             "completed": done, "p50_latency_s": pct(lat, 50),
             "sample": f"the same stream window ({len(stream)} requests arriving in {args.window:g} s, "
                       f"+{args.drain:g} s drain): host LSCM rows + C normal-equation assembly or host "
-                      f"cotangent CRS, FP64 Jacobi-PCG to {args.eps:g} (C, OpenMP), first come first "
+                      f"cotangent CRS, FP64 Jacobi-PCG to {args.eps:g} ({args.eps_lsq:g} for LSCM; C, OpenMP), first come first "
                       f"served, each step bounded by window + drain ({span:g} s); completions / {span:g} s"}
 
 
@@ -711,10 +722,12 @@ def config(args, stream):
                         f"({n_l} LSCM, {len(stream) - n_l} fairing), "
                         f"{sum(r.unknowns for r in stream)} unknowns",
             "requests": len(stream), "rate_per_s": args.rate, "window_s": args.window, "drain_s": args.drain,
-            "rel_residual": args.eps, "hbm_budget_gb": args.budget_gb,
+            "rel_residual": args.eps, "rel_residual_least_squares": args.eps_lsq,
+            "hbm_budget_gb": args.budget_gb,
             "precision": "auto: mixed FP32/FP64 (with FP64 fallback) for the square fairing "
                         "systems, FP64 for the least-squares LSCM normal equations",
             "schedule": "shortest estimated remaining work first, epochs time-boxed to 10 ms",
+            "min_tile_rows": args.min_tile_rows,
             "l2": "inputs larger than L2 for the large requests; every step re-uploads, rebuilds and "
                   "re-solves every request (no cached data)"}
 

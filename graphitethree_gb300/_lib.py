@@ -64,7 +64,8 @@ class NlgbServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_size_t), ("mode", C.c_int), ("precision", C.c_int),
                 ("eps", C.c_double), ("max_iter", C.c_longlong), ("inner_eps", C.c_double),
                 ("epoch_iters", C.c_longlong), ("max_systems", C.c_int), ("schedule", C.c_int),
-                ("epoch_ms", C.c_double), ("streams", C.c_int)]
+                ("epoch_ms", C.c_double), ("streams", C.c_int), ("eps_least_squares", C.c_double),
+                ("min_tile_rows", C.c_int)]
 
 
 class NlgbServerStats(C.Structure):

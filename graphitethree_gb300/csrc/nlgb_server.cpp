@@ -202,6 +202,12 @@ struct nlgb_server_s {
 
 namespace {
 
+// Least-squares request: a row stream assembled into normal equations, or an
+// LSCM mesh.
+bool req_least_squares(const Req& r) {
+  return (r.kind == 1 && r.least_squares) || (r.kind == 2 && r.mesh_kind == NLGB_MESH_LSCM);
+}
+
 // Precision of one request: NL_GB300_PRECISION_AUTO runs square systems in
 // mixed precision and least-squares row submissions (normal equations,
 // kappa(A^T A) = kappa(A)^2, too ill-conditioned for FP32 values on meshes)
@@ -211,8 +217,7 @@ namespace {
 // ends with a true residual a few times above the threshold.)
 int req_precision(const nlgb_server_s* S, const Req& r) {
   if (S->cfg.precision == NL_GB300_PRECISION_AUTO) {
-    const bool ls = (r.kind == 1 && r.least_squares) || (r.kind == 2 && r.mesh_kind == NLGB_MESH_LSCM);
-    return ls ? NL_GB300_PRECISION_DOUBLE : NL_GB300_PRECISION_MIXED;
+    return req_least_squares(r) ? NL_GB300_PRECISION_DOUBLE : NL_GB300_PRECISION_MIXED;
   }
   return S->cfg.precision;
 }
@@ -254,9 +259,9 @@ double iteration_cost(const Req& r, bool mixed) {
   return std::max(b, kServiceFloorBytes);
 }
 
-SolveParams params_of(const nlgb_server_s* S, int precision) {
+SolveParams params_of(const nlgb_server_s* S, const Req& r, int precision) {
   SolveParams p;
-  p.eps = S->cfg.eps;
+  p.eps = (req_least_squares(r) && S->cfg.eps_least_squares > 0.0) ? S->cfg.eps_least_squares : S->cfg.eps;
   p.max_iter = S->cfg.max_iter;
   p.precision = precision;
   p.inner_eps = S->cfg.inner_eps;
@@ -325,6 +330,10 @@ bool admit(nlgb_server_s* S, Req* r, cudaStream_t s, bool df_slots) {
   }
   r->t_built = S->now();
   if (e == cudaSuccess) e = crs_prepare(r->A, mixed, s);
+  // throughput tiling of the batched server (config.min_tile_rows): set
+  // before any slot, graph or plan reads the layout
+  if (e == cudaSuccess && S->cfg.mode == NLGB_SERVER_BATCHED && S->cfg.min_tile_rows > r->A.tile_rows)
+    r->A.tile_rows = S->cfg.min_tile_rows;
   r->t_prepared = S->now();
   bool dfl = false;   // false also when the matrix is outside double-float's range: FP64 runs
   if (e == cudaSuccess && prec == NL_GB300_PRECISION_DOUBLE_FLOAT) e = crs_prepare_df(r->A, &dfl, s);
@@ -335,7 +344,7 @@ bool admit(nlgb_server_s* S, Req* r, cudaStream_t s, bool df_slots) {
     r->bytes = actual;
     r->iter_cost = iteration_cost(*r, mixed);
     r->slots.resize((size_t)r->n_rhs);
-    const SolveParams prm = params_of(S, prec);
+    const SolveParams prm = params_of(S, *r, prec);
     for (int k = 0; k < r->n_rhs && e == cudaSuccess; ++k) {
       e = r->slots[k].alloc(&r->A, mixed, s, dfl && df_slots);
       if (e != cudaSuccess) break;
@@ -1239,7 +1248,7 @@ void worker_serial(nlgb_server_s* S) {
     // with the graph-captured single-system solver (which polls the abort
     // flag once per while-loop pass).
     bool ok = admit(S, r, s, false);
-    const SolveParams prm = params_of(S, req_precision(S, *r));
+    const SolveParams prm = params_of(S, *r, req_precision(S, *r));
     if (ok) {
       PcgSolver pcg;
       ok = pcg.bind(&r->A, s) == cudaSuccess;
@@ -1312,6 +1321,8 @@ void nlgb_server_default_config(nlgb_server_config* c) {
   c->schedule = NLGB_SCHEDULE_SRPT;
   c->epoch_ms = 10.0;
   c->streams = 16;
+  c->eps_least_squares = 0.0;
+  c->min_tile_rows = 0;
 }
 
 nlgb_server nlgb_server_create(const nlgb_server_config* cfg) {
@@ -1330,6 +1341,8 @@ nlgb_server nlgb_server_create(const nlgb_server_config* cfg) {
   if (!(S->cfg.epoch_ms >= 0.0)) S->cfg.epoch_ms = 10.0;
   if (S->cfg.streams <= 0) S->cfg.streams = 16;
   S->cfg.streams = std::min(S->cfg.streams, 128);
+  // tiles of a multiple of 128 rows, at most 2^20
+  S->cfg.min_tile_rows = S->cfg.min_tile_rows <= 0 ? 0 : std::min(((S->cfg.min_tile_rows + 127) / 128) * 128, 1 << 20);
   if (S->cfg.schedule != NLGB_SCHEDULE_SRPT && S->cfg.schedule != NLGB_SCHEDULE_ALL) {
     set_error("nlgb_server_create: unknown schedule");
     delete S;

@@ -175,8 +175,11 @@ __device__ __forceinline__ bool elect_last(unsigned int* counter) {
   return am_last != 0;
 }
 
+// Eight CTAs per SM like k_spmv_pq (at the 48 registers the compiler
+// otherwise takes, five fit, and the autotuner's one-wave grid of up to 1,216
+// CTAs ran in two waves).
 template <bool D>
-__global__ void __launch_bounds__(kCTA) k_update_xr(SysView s) {
+__global__ void __launch_bounds__(kCTA, 8) k_update_xr(SysView s) {
   if (ld_status(s.st) != ST_RUNNING) return;
   const double alpha = __ldcg(&s.st->alpha);
   for (int t = vec_t0(s), t1 = vec_t1(s); t < t1; ++t) {
@@ -190,7 +193,7 @@ __global__ void __launch_bounds__(kCTA) k_update_xr(SysView s) {
 }
 
 template <bool D>
-__global__ void __launch_bounds__(kCTA) k_update_p(SysView s) {
+__global__ void __launch_bounds__(kCTA, 8) k_update_p(SysView s) {
   if (ld_status(s.st) != ST_RUNNING) return;
   const double beta = __ldcg(&s.st->beta);
   for (int t = vec_t0(s), t1 = vec_t1(s); t < t1; ++t) phase_update_p<D>(s, t, beta);

@@ -198,7 +198,8 @@ class Server:
     def __init__(self, budget_bytes: float = 150e9, precision: str = "mixed", mode: str = "batched",
                  eps: float = 1e-10, epoch_iters: int = 256, inner_eps: float = 0.1,
                  max_systems: int = 8192, max_iter: int = -1, schedule: str = "srpt",
-                 epoch_ms: float = 10.0, streams: int = 16):
+                 epoch_ms: float = 10.0, streams: int = 16, eps_least_squares: float = 0.0,
+                 min_tile_rows: int = 0):
         L = _lib.load()
         cfg = _lib.NlgbServerConfig()
         L.nlgb_server_default_config(ctypes.byref(cfg))
@@ -213,6 +214,8 @@ class Server:
         cfg.schedule = K["NLGB_SCHEDULE_SRPT"] if schedule == "srpt" else K["NLGB_SCHEDULE_ALL"]
         cfg.epoch_ms = epoch_ms
         cfg.streams = streams
+        cfg.eps_least_squares = eps_least_squares
+        cfg.min_tile_rows = min_tile_rows
         h = L.nlgb_server_create(ctypes.byref(cfg))
         if not h:
             raise SolverError(f"nlgb_server_create failed: {_lib.last_error()}")

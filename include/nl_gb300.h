@@ -213,6 +213,25 @@ typedef struct {
     int       schedule;          /* NLGB_SCHEDULE_SRPT (default) / _ALL         */
     double    epoch_ms;          /* SRPT: target length of a chunk (10 ms)     */
     int       streams;           /* SRPT: concurrent chunks (default 16)        */
+    double    eps_least_squares; /* relative residual of least-squares
+                                    submissions (rows with least_squares,
+                                    LSCM meshes); <= 0 (default): eps.  The
+                                    normal equations square kappa, so a
+                                    solution error bound (e.g. 1e-8 against a
+                                    direct solve) can need a residual below
+                                    the one square systems stop at.        */
+    int       min_tile_rows;     /* batched server: each system is cut into
+                                    tiles of at least this many rows (rounded
+                                    up to a multiple of 128).  0 (default): the
+                                    single-system autotuner's tiling, which
+                                    spreads one system over every SM.  When
+                                    many systems share the GPU, fewer and
+                                    fuller CTAs per system pay: 1024 completed
+                                    5 % more requests of the serving stream
+                                    than 0.  Results stay bit-identical alone
+                                    and in any mix; against nlgb_solve they
+                                    are bit-identical when the matrix has the
+                                    same layout (nlgb_matrix_set_layout).   */
 } nlgb_server_config;
 
 typedef struct {

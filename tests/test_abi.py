@@ -56,3 +56,13 @@ def test_extension_hook_rejects_direct_solvers(nllib):
 def test_no_alloc_free_library_load(nllib):
     # loading must not require a GPU: the library initialises CUDA lazily
     assert isinstance(nllib, ctypes.CDLL)
+
+
+def test_server_config_mirror_matches_header():
+    """The ctypes mirror of nlgb_server_config lists the header's fields in
+    the header's order (the struct is passed by pointer)."""
+    text = (INCLUDE / "nl_gb300.h").read_text()
+    body = text.split("} nlgb_server_config;")[0].rsplit("typedef struct {", 1)[1]
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    fields = re.findall(r"\b(\w+);", body)
+    assert fields == [f[0] for f in _lib.NlgbServerConfig._fields_]

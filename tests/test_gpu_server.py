@@ -76,6 +76,65 @@ def test_server_matches_oracle_and_single_solver(gpu_ok, oracle_mod):
     srv.close()
 
 
+@pytest.mark.parametrize("mode", ["batched", "serial"])
+def test_least_squares_tolerance_applies_to_lscm_only(gpu_ok, mode):
+    """eps_least_squares: the LSCM (least-squares) request stops at its own
+    threshold, the square one at eps; each result equals the single-system
+    solver's at that threshold bit for bit."""
+    rs = systems.lscm_system(40, 36, seed=21)
+    fs = systems.fairing_system(50, 44, seed=22)
+    srv = solver.Server(precision="auto", mode=mode, eps=1e-10, eps_least_squares=3e-11)
+    t1, t2 = srv.submit_rows(rs), srv.submit_square(fs)
+    x1, i1, _ = srv.wait(t1)
+    x2, i2, _ = srv.wait(t2)
+    srv.close()
+    assert i1[0].status == "converged" and i1[0].true_rel_residual <= 3e-11
+    assert all(i.status == "converged" and i.true_rel_residual <= 1e-10 for i in i2)
+    M, rhs, _ = solver.assemble(rs)
+    x_ref, inf = M.solve(rhs[0], eps=3e-11)
+    assert inf.iterations == i1[0].iterations and np.array_equal(x_ref, x1[0])
+    x_loose, inf_loose = M.solve(rhs[0], eps=1e-10)
+    assert inf_loose.iterations < i1[0].iterations
+    F = solver.Matrix(fs.rp, fs.ci, fs.va)
+    for k in range(3):
+        assert F.solve(fs.rhs[k], precision="mixed", eps=1e-10)[1].iterations == i2[k].iterations
+
+
+@pytest.mark.parametrize("schedule", ["srpt", "all"])
+def test_min_tile_rows_changes_only_the_layout(gpu_ok, schedule):
+    """min_tile_rows: the batched server cuts each system into tiles of at
+    least that many rows.  Results are bit-identical alone and in the mix,
+    and equal the single-system solver's on a matrix given the same layout;
+    a system smaller than one tile runs as a single tile."""
+    reqs = _requests()
+    alone = []
+    for kind, obj in reqs:
+        srv = solver.Server(precision="auto", budget_bytes=2e9, min_tile_rows=1000)   # -> 1024
+        x, infos, _ = srv.wait(_submit(srv, kind, obj))
+        alone.append((x.copy(), [i.iterations for i in infos]))
+        srv.close()
+    srv = solver.Server(precision="auto", budget_bytes=2e9, min_tile_rows=1024, epoch_iters=64,
+                        schedule=schedule, epoch_ms=0.5)
+    tickets = [_submit(srv, kind, obj, arrival=0.002 * i) for i, (kind, obj) in enumerate(reqs)]
+    for t, (xa, ia) in zip(tickets, alone):
+        x, infos, _ = srv.wait(t)
+        assert all(i.status == "converged" for i in infos)
+        assert [i.iterations for i in infos] == ia and np.array_equal(x, xa)
+    srv.close()
+    for (kind, obj), (xa, ia) in zip(reqs, alone):
+        if kind == "rows":
+            M, rhs, _ = solver.assemble(obj)
+            bs, prec = [rhs[0]], "double"
+        else:
+            M, bs, prec = solver.Matrix(obj.rp, obj.ci, obj.va), list(obj.rhs), "mixed"
+        if M.tile_rows < 1024:
+            M.set_layout(0, 1024)
+        for k, b in enumerate(bs):
+            xs, inf = M.solve(b, precision=prec)
+            assert inf.iterations == ia[k] and np.array_equal(xs, xa[k])
+        M.close()
+
+
 def test_budget_admission_queues_and_rejects(gpu_ok):
     fs = [systems.fairing_system(64, 64, seed=s) for s in range(6)]
     one = solver.Server(budget_bytes=1e9)
