@@ -97,10 +97,10 @@ def parse_args():
                         "stream sit just above 1e-8 from the direct solve")
     p.add_argument("--budget-gb", type=float, default=150.0)
     p.add_argument("--plain-steps", type=int, default=2, help="steps of the serial plain-FP64 arm")
-    p.add_argument("--streams", type=int, default=16, help="concurrent chunk streams of the batched server")
-    p.add_argument("--min-tile-rows", type=int, default=1024,
+    p.add_argument("--streams", type=int, default=32, help="concurrent chunk streams of the batched server")
+    p.add_argument("--min-tile-rows", type=int, default=2048,
                    help="batched server: minimum rows per tile (fewer, fuller CTAs per system when "
-                        "16 streams share the GPU; the serial arm keeps the single-system tiling)")
+                        "many streams share the GPU; the serial arm keeps the single-system tiling)")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-spmv", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
@@ -431,12 +431,13 @@ def profile_case(which):
         return
     if which == "stream_mid":
         # mid-size requests of the serving stream through the server's
-        # stream executor (chunk kernels launched one by one): an LSCM mesh
+        # stream executor (chunk kernels launched one by one; tiles of at
+        # least 1,024 rows, as the serving bench's batched arm): an LSCM mesh
         # of 150^2 vertices (44,996 unknowns) and a fairing mesh of 300^2
         # (90,000 unknowns, 3 right-hand sides), 48 FP64 iterations each
         from graphitethree_gb300 import meshes
         os.environ["NLGB_EAGER_SOLVE"] = "1"
-        srv = solver.Server(precision="double", eps=1e-30, max_iter=48, budget_bytes=4e9)
+        srv = solver.Server(precision="double", eps=1e-30, max_iter=48, budget_bytes=4e9, min_tile_rows=1024)
         V1, F1 = meshes.height_field(150, 150, 11)
         V2, F2 = meshes.height_field(300, 300, 12)
         b2 = np.ascontiguousarray(1e-2 * V2.T)
@@ -826,8 +827,8 @@ def main():
 
     # Device work of the step: the server's executor runs every system as
     # CUDA-graph chunks of the PCG iteration kernels (k_spmv_pq + k_update_xr
-    # + k_update_p, or the mixed-precision k_mx_* kernels) on 16 concurrent
-    # streams; achieved = algorithmic bytes of all iterations run (finished
+    # + k_update_p, or the mixed-precision k_mx_* kernels) on --streams
+    # concurrent streams; achieved = algorithmic bytes of all iterations run (finished
     # requests or not) / wall time during which at least one chunk was in
     # flight.
     busy = st_last["kernel_s"]
@@ -836,8 +837,8 @@ def main():
     ach = algo / busy / 1e9 if busy > 0 else 0.0
     roofline = {"bound": "hbm",
                 "kernel": "PCG iteration kernels in CUDA-graph chunks (k_spmv_pq, k_update_xr, k_update_p; "
-                          "k_mx_spmv_pq, k_mx_update_cr, k_mx_update_p for mixed systems), 16 concurrent "
-                          "streams",
+                          "k_mx_spmv_pq, k_mx_update_cr, k_mx_update_p for mixed systems), "
+                          f"{args.streams} concurrent streams",
                 "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                 "traffic": GRAPH_DRAM_PER_ALGO_BYTE * algo / chunks,
                 "algo_bytes_per_launch": algo / chunks, "launches_per_step": chunks,

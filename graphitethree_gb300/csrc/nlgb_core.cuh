@@ -155,30 +155,70 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// Block sum of up to 4 values at once; result broadcast to all threads.
+// Block sum of up to 4 values at once, valid in thread 0 (every caller
+// uses it there).  Each value goes through the tree of warp_sum (the lane
+// butterfly, levels 16, 8, 4, 2, 1), then the eight warp totals are added in
+// order.  The first two levels of several values share one FP64 addition
+// per lane: at level 16 the lanes of one half-warp keep value a and receive
+// the partner half's a while the other half-warp does the same for value b;
+// at level 8 the quarter-warps split the pairs (a, b) and (c, d) the same
+// way.  Floating-point addition is commutative, so each value's chain of
+// additions is the butterfly's bit for bit, while GB300's narrow FP64 pipe
+// issues 5 (K <= 2) or 6 (K <= 4) warp additions instead of 5 K, and the
+// final sum of the warp totals runs in one thread instead of 256.
 template <int K>
 __device__ __forceinline__ void block_sum(double (&v)[K]) {
+  static_assert(K >= 1 && K <= 4, "block_sum: 1 to 4 values");
   __shared__ double red[K][kWarps];
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  constexpr unsigned kAll = 0xffffffffu;
+  double tot[4];
+  if constexpr (K == 1) {
+    tot[0] = warp_sum(v[0]);
+  } else {
+    const bool h16 = (l & 16) != 0;
+    // level 16, values (0, 1): lanes 0-15 carry v0, lanes 16-31 v1
+    double u = (h16 ? v[1] : v[0]) + __shfl_xor_sync(kAll, h16 ? v[0] : v[1], 16);
+    if constexpr (K == 2) {
 #pragma unroll
-  for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
+      for (int o = 8; o > 0; o >>= 1) u += __shfl_xor_sync(kAll, u, o);
+      tot[0] = u;                               // lanes 0-15
+      tot[1] = __shfl_sync(kAll, u, 16);        // lanes 16-31
+    } else {
+      // level 16, values (2, 3) (a zero stands in for a missing fourth)
+      const double v3 = K == 4 ? v[K - 1] : 0.0;
+      const double u2 = (h16 ? v3 : v[2]) + __shfl_xor_sync(kAll, h16 ? v[2] : v3, 16);
+      // level 8: quarter-warps 0 / 2 carry (v0, v1), quarter-warps 1 / 3 (v2, v3)
+      const bool h8 = (l & 8) != 0;
+      double t = (h8 ? u2 : u) + __shfl_xor_sync(kAll, h8 ? u : u2, 8);
+#pragma unroll
+      for (int o = 4; o > 0; o >>= 1) t += __shfl_xor_sync(kAll, t, o);
+      tot[0] = t;                               // lanes 0-7
+      tot[2] = __shfl_sync(kAll, t, 8);         // lanes 8-15
+      tot[1] = __shfl_sync(kAll, t, 16);        // lanes 16-23
+      tot[3] = __shfl_sync(kAll, t, 24);        // lanes 24-31
+    }
+  }
   __syncthreads();   // protect red[] from a previous use
   if (l == 0) {
 #pragma unroll
-    for (int k = 0; k < K; ++k) red[k][w] = v[k];
+    for (int k = 0; k < K; ++k) red[k][w] = tot[k];
   }
   __syncthreads();
+  if (threadIdx.x == 0) {
 #pragma unroll
-  for (int k = 0; k < K; ++k) {
-    double s = 0.0;
+    for (int k = 0; k < K; ++k) {
+      double s = 0.0;
 #pragma unroll
-    for (int i = 0; i < kWarps; ++i) s += red[k][i];
-    v[k] = s;
+      for (int i = 0; i < kWarps; ++i) s += red[k][i];
+      v[k] = s;
+    }
   }
 }
 
 // Canonical reduction of component `comp` of the tile partials (strided by
-// kParts): thread t sums tiles t, t+256, ... in order, then block_sum.
+// kParts): thread t sums tiles t, t+256, ... in order, then block_sum (the
+// result is valid in thread 0).
 template <int K>
 __device__ __forceinline__ void canon_reduce(const double* part, int n_tiles,
                                              const int (&comp)[K], double (&out)[K]) {
@@ -299,7 +339,11 @@ __device__ __forceinline__ void pair_loop(int lo, int hi, F2&& body2, F1&& body1
   if ((hi & 1) && threadIdx.x == 0) body1(hi - 1);
 }
 
-// x += a p, r -= a q; returns (r.D^-1 r, r.r).
+// x += a p, r -= a q, z = D^-1 r; returns (r.z, r.r).  z is stored over q
+// (A p is dead once r is updated, and the next SpMV rewrites q), so the p
+// update reads z instead of computing D^-1 r again: one FP64 product per
+// row fewer on GB300's narrow FP64 pipe, the same bytes (z written here,
+// r and D^-1 no longer read there) and the same bits.
 __device__ __forceinline__ void tile_update_xr(const SysView& s, int tile, double alpha,
                                                double (&out)[2]) {
   const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
@@ -307,7 +351,7 @@ __device__ __forceinline__ void tile_update_xr(const SysView& s, int tile, doubl
   double2* x2 = reinterpret_cast<double2*>(s.x);
   double2* r2 = reinterpret_cast<double2*>(s.r);
   const double2* p2 = reinterpret_cast<const double2*>(s.p);
-  const double2* q2 = reinterpret_cast<const double2*>(s.q);
+  double2* q2 = reinterpret_cast<double2*>(s.q);
   const double2* d2 = reinterpret_cast<const double2*>(s.dinv);
   pair_loop(lo, hi,
     [&](int i2) {
@@ -317,6 +361,7 @@ __device__ __forceinline__ void tile_update_xr(const SysView& s, int tile, doubl
       rv.x = fma(-alpha, qv.x, rv.x); rv.y = fma(-alpha, qv.y, rv.y);
       x2[i2] = xv; r2[i2] = rv;
       const double zx = dv.x * rv.x, zy = dv.y * rv.y;
+      q2[i2] = make_double2(zx, zy);
       rz = fma(zx, rv.x, rz); rz = fma(zy, rv.y, rz);
       rr = fma(rv.x, rv.x, rr); rr = fma(rv.y, rv.y, rr);
     },
@@ -324,29 +369,33 @@ __device__ __forceinline__ void tile_update_xr(const SysView& s, int tile, doubl
       s.x[i] = fma(alpha, __ldcg(s.p + i), __ldcg(s.x + i));
       const double ri = fma(-alpha, __ldcg(s.q + i), __ldcg(s.r + i));
       s.r[i] = ri;
-      rz = fma(s.dinv[i] * ri, ri, rz);
+      const double zi = s.dinv[i] * ri;
+      s.q[i] = zi;
+      rz = fma(zi, ri, rz);
       rr = fma(ri, ri, rr);
     });
   out[0] = rz; out[1] = rr;
   block_sum<2>(out);
 }
 
-// p = D^-1 r + beta p.
+// p = z + beta p, z = D^-1 r as tile_update_xr left it in q (every
+// executor runs this right after tile_update_xr of the same iteration, or,
+// after a true-residual check, as the pending update of the iteration that
+// stopped: q still holds that iteration's z).
 __device__ __forceinline__ void tile_update_p(const SysView& s, int tile, double beta) {
   const int lo = tile_lo(s, tile), hi = tile_hi(s, tile);
   double2* p2 = reinterpret_cast<double2*>(s.p);
-  const double2* r2 = reinterpret_cast<const double2*>(s.r);
-  const double2* d2 = reinterpret_cast<const double2*>(s.dinv);
+  const double2* z2 = reinterpret_cast<const double2*>(s.q);
   pair_loop(lo, hi,
     [&](int i2) {
-      const double2 rv = __ldcg(r2 + i2), dv = __ldg(d2 + i2);
+      const double2 zv = __ldcg(z2 + i2);
       double2 pv = __ldcg(p2 + i2);
-      pv.x = fma(beta, pv.x, dv.x * rv.x);
-      pv.y = fma(beta, pv.y, dv.y * rv.y);
+      pv.x = fma(beta, pv.x, zv.x);
+      pv.y = fma(beta, pv.y, zv.y);
       p2[i2] = pv;
     },
     [&](int i) {
-      s.p[i] = fma(beta, __ldcg(s.p + i), s.dinv[i] * __ldcg(s.r + i));
+      s.p[i] = fma(beta, __ldcg(s.p + i), __ldcg(s.q + i));
     });
 }
 
