@@ -123,10 +123,8 @@ def parse_args():
 def measure_configs(args):
     """Configs 1, 2, 3 (`--charts` charts) and 5 -- plain FP64 vs mixed,
     serial vs batched, errors against the FP64 oracles -- one JSON line
-    (device times from CUDA events)."""
-    import scipy.sparse as sp
-    import scipy.sparse.linalg as spla
-    from graphitethree_gb300 import meshes, solver, systems
+    (device times from CUDA events); --charts 0 leaves config 3 out."""
+    from graphitethree_gb300 import solver, systems
     from oracle import oracle
     out = {"workload": "configs"}
     t_start = time.perf_counter()
@@ -178,6 +176,17 @@ def measure_configs(args):
             c2[f"rhs{k}_{p}"]["error_vs_oracle_pcg_1e-14"] = errors(x, xo)
     out["config2_fairing2048"] = c2
     A.close()
+    if args.charts > 0:
+        out["config3_charts"] = measure_config3(args, progress)
+    progress("mesh builders")
+    measure_builders_krylov_config5(args, out, progress, rec, errors)
+    print(json.dumps(out))
+
+
+def measure_config3(args, progress):
+    """Config 3: `--charts` uneven LSCM charts built on the GPU, batched
+    (one persistent launch, FP64 and mixed) against one after another."""
+    from graphitethree_gb300 import meshes, solver
     progress(f"config 3: building {args.charts} charts on the GPU")
     nx, ny = meshes.chart_sizes(args.charts, seed=3, side_min=16, side_max=512)
     mats, bs, unknowns, build_s = [], [], 0, 0.0
@@ -205,10 +214,25 @@ def measure_configs(args):
     c3["serial_plain_iterations"] = serial_iters
     c3["batched_speedup_double"] = serial / c3["batched_double_s"] if c3["batched_double_s"] > 0 else None
     c3["batched_speedup_mixed"] = serial / c3["batched_mixed_s"] if c3["batched_mixed_s"] > 0 else None
+    statuses = {}
+    for i in infos:
+        statuses[i.status] = statuses.get(i.status, 0) + 1
+    c3["batched_mixed_statuses"] = statuses
+    c3["batched_mixed_not_converged"] = [
+        {"chart": c, "n": mats[c].n, "status": i.status, "iterations": i.iterations,
+         "reliable_updates": i.refinement_steps, "true_rel_residual": i.true_rel_residual}
+        for c, i in enumerate(infos) if i.status != "converged"][:16]
     for M in mats:
         M.close()
-    out["config3_charts"] = c3
-    progress("mesh builders")
+    return c3
+
+
+def measure_builders_krylov_config5(args, out, progress, rec, errors):
+    """Mesh builders, BiCGSTAB / GMRES and config 5 (stretched fairing at
+    1e-12, FP64 and mixed, against SuperLU)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    from graphitethree_gb300 import meshes, solver, systems
     V1, F1 = meshes.height_field(256, 256, seed=1)
     V2, F2 = meshes.height_field(2048, 2048, seed=2)
     solver.build_lscm(V1, F1)                       # warm-up (context, kernels)
@@ -260,7 +284,6 @@ def measure_configs(args):
     c5["plain_1e-12"]["error_vs_direct"] = errors(x5, xd)
     c5["mixed_1e-12"]["error_vs_direct"] = errors(x5m, xd)
     out["config5_stretched"] = c5
-    print(json.dumps(out))
 
 
 def run_sweep(args):

@@ -81,9 +81,10 @@ struct __align__(16) SysState {
   double rthresh2;             // FP64 / double-float: threshold^2 of the recursive residual (starts at thresh2)
   int cont_ok;                 // beta / rho of the last iteration are valid (the iteration can be continued)
   int pad_;
-  // Two-level election of the graph solver's p.q (0) and x/r (1) phase
-  // kernels: arrivals per group of tiles, groups done, and each group's
-  // warp-level sums (canonical order, see elect2 in nlgb_solver.cu).
+  // Two-level election of the x / r update (FP64, double-float) and of the
+  // mixed c / r update (index 1; index 0 is not used): arrivals per group of
+  // tiles, groups done, and each group's warp-level sums (canonical order,
+  // see elect2 in nlgb_solver.cu).
   unsigned int gcnt[2][8];
   unsigned int tcnt[2];
   unsigned int pad2_[2];

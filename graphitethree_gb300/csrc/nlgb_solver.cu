@@ -45,7 +45,8 @@ __device__ __forceinline__ bool publish_elect(const SysView& s, int tile, const 
 }
 
 // ---------------------------------------------------------------------------
-// Two-level last-CTA election with the canonical reduction.  The canonical
+// Two-level last-CTA election with the canonical reduction (the tails of
+// k_update_xr and of the mixed iteration's c / r update).  The canonical
 // order (canon_reduce) sums tile t into thread (t mod 256)'s running sum,
 // then each warp's 32 running sums by a butterfly, then the 8 warp totals in
 // order.  Here the tiles of warp g's running sums -- those with (t mod 256)
@@ -134,15 +135,37 @@ __global__ void __launch_bounds__(kCTA) k_init(SysView s) {
   }
 }
 
+// The SpMV hands p.q on without a reduction tail: k_spmv_pq stores its
+// tiles' p.q partials and ends, and every CTA of k_update_xr reduces those
+// partials itself in the canonical order and applies the scalar step
+// (alpha) to its own shared copy of the state.  The serial tail of a
+// last-CTA reduction (fence, arrival, partial loads, fence, scalar step)
+// left the SMs idle for several microseconds after the SpMV.  k_update_xr
+// keeps its tail: its r.z and r.r feed beta and the stopping test, and
+// having every CTA of k_update_p reduce them instead cost more than the tail
+// (measured on the 1.3M-unknown LSCM iteration: the SpMV 76.4 -> 69.8 us,
+// k_update_p 11.0 -> 23.1 us, with 1,134 CTAs re-reading the same partials
+// before their short tile work).  Same sums, same scalar steps: the
+// iterates are those of the other executors bit for bit.
+
+// Every thread's copy of the system state into shared memory (16-byte
+// words; the state was written by an earlier kernel).
+__device__ __forceinline__ void load_state(SysState& dst, const SysState* src) {
+  constexpr int kWords = (int)(sizeof(SysState) / 16);
+  static_assert(sizeof(SysState) % 16 == 0, "SysState is 16-byte aligned");
+  const int4* sp = reinterpret_cast<const int4*>(src);
+  int4* dp = reinterpret_cast<int4*>(&dst);
+  for (int i = threadIdx.x; i < kWords; i += blockDim.x) dp[i] = __ldcg(sp + i);
+  __syncthreads();
+}
+
 // Eight CTAs per SM (32 registers): the tile autotuner sizes one wave of
 // CTAs on that residency.
 template <int T, bool D>
 __global__ void __launch_bounds__(kCTA, 8) k_spmv_pq(SysView s) {
   if (ld_status(s.st) != ST_RUNNING) return;
-  double v[1] = {phase_spmv_pq<D, T>(s, blockIdx.x)};
-  if (threadIdx.x == 0) __stcg(s.part + (size_t)blockIdx.x * kParts + kSlotPQ, v[0]);
-  double o[1];
-  if (elect2<1>(s, blockIdx.x, 1, kSlotPQ, 0, o) && threadIdx.x == 0) scalar_after_pq(s.st, o[0]);
+  const double v = phase_spmv_pq<D, T>(s, blockIdx.x);
+  if (threadIdx.x == 0) __stcg(s.part + (size_t)blockIdx.x * kParts + kSlotPQ, v);
 }
 
 // Vector phases: each CTA handles vec_tiles_for(tile_rows) consecutive tiles
@@ -161,35 +184,35 @@ __device__ __forceinline__ void store_parts(const SysView& s, int tile, const do
   }
 }
 
-// Last-CTA election over the whole grid (partials already stored).
-__device__ __forceinline__ bool elect_last(unsigned int* counter) {
-  __shared__ int am_last;
-  if (threadIdx.x == 0) {
-    __threadfence();
-    const unsigned int prev = atomicAdd(counter, 1u);
-    am_last = (prev == gridDim.x - 1u);
-    if (am_last) *counter = 0u;
-  }
-  __syncthreads();
-  if (am_last) __threadfence();
-  return am_last != 0;
-}
-
-// Eight CTAs per SM like k_spmv_pq (at the 48 registers the compiler
-// otherwise takes, five fit, and the autotuner's one-wave grid of up to 1,216
-// CTAs ran in two waves).
+// alpha = rho / p.q from the SpMV's partials (every CTA), then x, r and
+// z = D^-1 r; the last CTA of the two-level election writes alpha back and
+// takes the step after r.z and r.r (beta, stopping test).
 template <bool D>
 __global__ void __launch_bounds__(kCTA, 8) k_update_xr(SysView s) {
-  if (ld_status(s.st) != ST_RUNNING) return;
-  const double alpha = __ldcg(&s.st->alpha);
-  for (int t = vec_t0(s), t1 = vec_t1(s); t < t1; ++t) {
-    double v[2];
-    phase_update_xr<D>(s, t, alpha, v);
-    store_parts<2>(s, t, v, kSlotXR);
+  __shared__ SysState sst;
+  load_state(sst, s.st);
+  if (sst.status != ST_RUNNING) return;
+  {
+    const int comp[1] = {kSlotPQ};
+    double o[1];
+    canon_reduce<1>(s.part, s.n_tiles, comp, o);
+    if (threadIdx.x == 0) scalar_after_pq(&sst, o[0]);
+    __syncthreads();
+  }
+  if (sst.status == ST_RUNNING) {
+    const double alpha = sst.alpha;
+    for (int t = vec_t0(s), t1 = vec_t1(s); t < t1; ++t) {
+      double v[2];
+      phase_update_xr<D>(s, t, alpha, v);
+      store_parts<2>(s, t, v, kSlotXR);
+    }
   }
   double o[2];
-  if (elect2<2>(s, vec_t0(s), vec_tiles_for(s.tile_rows), kSlotXR, 1, o) && threadIdx.x == 0)
-    scalar_after_xr(s.st, o[0], o[1]);
+  if (elect2<2>(s, vec_t0(s), vec_tiles_for(s.tile_rows), kSlotXR, 1, o) && threadIdx.x == 0) {
+    s.st->alpha = sst.alpha;
+    s.st->status = sst.status;
+    if (sst.status == ST_RUNNING) scalar_after_xr(s.st, o[0], o[1]);
+  }
 }
 
 template <bool D>
@@ -486,30 +509,44 @@ __global__ void __launch_bounds__(kCTA) k_mx_outer(SysView s) {
   }
 }
 
+// q32 = A32 p32; stores the tiles' p.q partials (alpha is taken by every CTA
+// of k_mx_update_cr, as in the FP64 iteration).
 template <int T>
 __global__ void __launch_bounds__(kCTA) k_mx_spmv_pq(SysView s) {
   if (ld_status(s.st) != ST_RUNNING || ld_mode(s.st) != 1) return;
-  double v[1] = {tile_mx_spmv_pq<T>(s, blockIdx.x)};
-  if (threadIdx.x == 0) __stcg(s.part + (size_t)blockIdx.x * kParts + kSlotPQ, v[0]);
-  double o[1];
-  if (elect2<1>(s, blockIdx.x, 1, kSlotPQ, 0, o) && threadIdx.x == 0) scalar_after_pq(s.st, o[0]);
+  const double v = tile_mx_spmv_pq<T>(s, blockIdx.x);
+  if (threadIdx.x == 0) __stcg(s.part + (size_t)blockIdx.x * kParts + kSlotPQ, v);
 }
 
-// c += a p, r -= a q; the last CTA decides whether a reliable update is due
-// and sets the condition of the IF node that runs it (use_handle == 0: eager
+// alpha from the SpMV's partials (every CTA), then c += a p, r -= a q; the
+// last CTA writes alpha back, decides whether a reliable update is due and
+// sets the condition of the IF node that runs it (use_handle == 0: eager
 // mode, the update kernels are launched anyway and check the mode).
 __global__ void __launch_bounds__(kCTA) k_mx_update_cr(SysView s, cudaGraphConditionalHandle h_upd,
                                                        int use_handle) {
-  if (ld_status(s.st) != ST_RUNNING || ld_mode(s.st) != 1) return;
-  const double alpha = __ldcg(&s.st->alpha);
-  for (int t = vec_t0(s), t1 = vec_t1(s); t < t1; ++t) {
-    double v[2];
-    tile_mx_update_cr(s, t, alpha, v);
-    store_parts<2>(s, t, v, kSlotXR);
+  __shared__ SysState sst;
+  load_state(sst, s.st);
+  if (sst.status != ST_RUNNING || sst.mode != 1) return;
+  {
+    const int comp[1] = {kSlotPQ};
+    double o[1];
+    canon_reduce<1>(s.part, s.n_tiles, comp, o);
+    if (threadIdx.x == 0) scalar_after_pq(&sst, o[0]);
+    __syncthreads();
+  }
+  if (sst.status == ST_RUNNING) {
+    const double alpha = sst.alpha;
+    for (int t = vec_t0(s), t1 = vec_t1(s); t < t1; ++t) {
+      double v[2];
+      tile_mx_update_cr(s, t, alpha, v);
+      store_parts<2>(s, t, v, kSlotXR);
+    }
   }
   double o[2];
   if (elect2<2>(s, vec_t0(s), vec_tiles_for(s.tile_rows), kSlotXR, 1, o) && threadIdx.x == 0) {
-    scalar_after_mx_cr(s.st, o[0], o[1]);
+    s.st->alpha = sst.alpha;
+    s.st->status = sst.status;
+    if (sst.status == ST_RUNNING) scalar_after_mx_cr(s.st, o[0], o[1]);
     const bool upd = s.st->status == ST_RUNNING && s.st->mode == 0;
     if (use_handle) cudaGraphSetConditional(h_upd, upd ? 1u : 0u);
   }
