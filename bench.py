@@ -69,12 +69,14 @@ os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 import numpy as np  # noqa: E402
 
 METRIC = "solves/s & p99 latency at rel-residual 1e-10: batched mixed vs plain FP64 GPU"
-# DRAM bytes (read + write) per algorithmic byte of the PCG iteration
-# kernels, from one ncu capture on the 1.3M-unknown LSCM system (808^2
-# grid): its SpMV read 252.9 MB for 245.2 MB algorithmic; the serving
-# workload is too large to capture whole, and its traffic grows in
+# DRAM bytes (read + write) per algorithmic byte of one PCG iteration (the
+# three phase kernels), from one ncu capture on the 1.3M-unknown LSCM system
+# (808^2 grid): 252.6 + 52.6 + 20.9 MB of DRAM traffic for 360.1 MB
+# algorithmic (0.906; vectors written by one phase are partly read back
+# from L2 by the next).  The 4.2M-unknown fairing system measured 0.953.
+# The serving workload is too large to capture whole; its traffic grows in
 # proportion to the iterations run.
-GRAPH_DRAM_PER_ALGO_BYTE = 1.03
+GRAPH_DRAM_PER_ALGO_BYTE = 0.906
 HBM_FALLBACK_GBS = 6800.0
 
 
@@ -866,9 +868,10 @@ def main():
                 "traffic": GRAPH_DRAM_PER_ALGO_BYTE * algo / chunks,
                 "algo_bytes_per_launch": algo / chunks, "launches_per_step": chunks,
                 "busy_s_per_step": busy, "peak_source": peak_src,
-                "traffic_note": "dram read+write per chunk: 1.03 DRAM byte per algorithmic byte, from the ncu "
-                                "capture of k_spmv_pq on the 1.3M-unknown LSCM system (the vector kernels "
-                                "stream exactly their bytes), times this workload's algorithmic bytes per chunk",
+                "traffic_note": "dram read+write per chunk: 0.906 DRAM byte per algorithmic byte of a PCG "
+                                "iteration (k_spmv_pq + k_update_xr + k_update_p), from one ncu capture on "
+                                "the 1.3M-unknown LSCM system, times this workload's algorithmic bytes per "
+                                "chunk",
                 "fp64_note": "the FP64 phases are co-limited by GB300's FP64 pipe, not only by HBM"}
 
     infos = [i for infs in last["infos"].values() for i in infs]
