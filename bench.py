@@ -109,7 +109,7 @@ def parse_args():
     p.add_argument("--no-parity", action="store_true")
     p.add_argument("--parity-max-unknowns", type=int, default=300_000,
                    help="largest completed request checked against the direct oracle")
-    p.add_argument("--profile-case", choices=["spmv", "batch", "batch_small", "batch_lscm", "stream_mid",
+    p.add_argument("--profile-case", choices=["spmv", "batch", "batch_small", "batch_lscm", "stream_mid", "mid_systems",
                                               "plain", "mixed", "plain_lscm", "mixed_lscm", "df_lscm",
                                               "kernels"], default=None,
                    help="run one small case for an ncu capture and exit")
@@ -471,6 +471,27 @@ def profile_case(which):
         i1, i2 = srv.wait(t1)[1], srv.wait(t2)[1]
         srv.close()
         print(json.dumps({"case": which, "iterations": [i.iterations for i in i1 + i2]}))
+        return
+    if which == "mid_systems":
+        # the mid-size requests of the serving stream as the batched server
+        # runs them (tiles of at least 2,048 rows, AUTO precision: FP64 for
+        # LSCM, mixed for fairing), through the single-system solver with
+        # its kernels launched one by one: an LSCM mesh of 150^2 vertices
+        # (44,996 unknowns) and a fairing mesh of 300^2 (90,000 unknowns),
+        # 48 iterations each
+        from graphitethree_gb300 import meshes
+        os.environ["NLGB_EAGER_SOLVE"] = "1"
+        V1, F1 = meshes.height_field(150, 150, 11)
+        V2, F2 = meshes.height_field(300, 300, 12)
+        M1, rhs1, _ = solver.build_lscm(V1, F1)
+        M2, _ = solver.build_fairing(V2, F2, 1e-2)
+        its = []
+        for M, b, prec in ((M1, rhs1, "double"), (M2, np.ascontiguousarray(1e-2 * V2[:, 0]), "mixed")):
+            if M.tile_rows < 2048:
+                M.set_layout(0, 2048)
+            its.append(M.solve(b, max_iter=48, eps=1e-30, precision=prec)[1].iterations)
+            M.close()
+        print(json.dumps({"case": which, "iterations": its}))
         return
     if which == "batch_small":
         # one small LSCM system (4,604 unknowns, 35 tiles) in the persistent
