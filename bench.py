@@ -103,6 +103,9 @@ def parse_args():
     p.add_argument("--min-tile-rows", type=int, default=2048,
                    help="batched server: minimum rows per tile (fewer, fuller CTAs per system when "
                         "many streams share the GPU; the serial arm keeps the single-system tiling)")
+    p.add_argument("--cta-budget", type=int, default=-1,
+                   help="batched server: CTA budget of the chunks in flight (-1: one resident wave of "
+                        "the phase kernels, SMs x 8; 0: no limit)")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-spmv", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
@@ -313,7 +316,8 @@ def run_sweep(args):
         for arm, mode, prec in (("batched_auto", "batched", "auto"), ("serial_fp64", "serial", "double")):
             srv = solver.Server(budget_bytes=args.budget_gb * 1e9, precision=prec, mode=mode, eps=args.eps,
                                 streams=args.streams, eps_least_squares=args.eps_lsq,
-                                min_tile_rows=args.min_tile_rows if mode == "batched" else 0)
+                                min_tile_rows=args.min_tile_rows if mode == "batched" else 0,
+                                chunk_cta_budget=args.cta_budget if mode == "batched" else 0)
             srv.reset_clock()
             T0 = 0.5
             tickets = [None] * len(reqs)
@@ -613,7 +617,8 @@ def run_stream(stream, args, mode: str, precision: str, keep_x: bool = False):
     from graphitethree_gb300 import solver
     srv = solver.Server(budget_bytes=args.budget_gb * 1e9, precision=precision, mode=mode, eps=args.eps,
                         streams=args.streams, eps_least_squares=args.eps_lsq,
-                        min_tile_rows=args.min_tile_rows if mode == "batched" else 0)
+                        min_tile_rows=args.min_tile_rows if mode == "batched" else 0,
+                        chunk_cta_budget=args.cta_budget if mode == "batched" else 0)
     srv.reset_clock()
     T0 = args.lead
     tickets = [srv.submit_mesh(r.kind, r.V, r.F, b=r.b, lam=r.lam, arrival=T0 + r.arrival) for r in stream]
@@ -774,7 +779,7 @@ def config(args, stream):
             "precision": "auto: mixed FP32/FP64 (with FP64 fallback) for the square fairing "
                         "systems, FP64 for the least-squares LSCM normal equations",
             "schedule": "shortest estimated remaining work first, epochs time-boxed to 10 ms",
-            "min_tile_rows": args.min_tile_rows,
+            "min_tile_rows": args.min_tile_rows, "chunk_cta_budget": args.cta_budget,
             "l2": "inputs larger than L2 for the large requests; every step re-uploads, rebuilds and "
                   "re-solves every request (no cached data)"}
 

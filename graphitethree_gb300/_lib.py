@@ -65,7 +65,7 @@ class NlgbServerConfig(C.Structure):
                 ("eps", C.c_double), ("max_iter", C.c_longlong), ("inner_eps", C.c_double),
                 ("epoch_iters", C.c_longlong), ("max_systems", C.c_int), ("schedule", C.c_int),
                 ("epoch_ms", C.c_double), ("streams", C.c_int), ("eps_least_squares", C.c_double),
-                ("min_tile_rows", C.c_int)]
+                ("min_tile_rows", C.c_int), ("chunk_cta_budget", C.c_int)]
 
 
 class NlgbServerStats(C.Structure):

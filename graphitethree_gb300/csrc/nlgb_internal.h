@@ -74,6 +74,8 @@ long long device_bytes(const DeviceCRS& A);
 // Autotuner: threads per row and tile rows from the nnz-per-row histogram.
 struct TuneChoice { int tpr; int tile_rows; };
 TuneChoice autotune(int n, long long nnz, int max_row, const int* hist33);
+// 256-thread phase CTAs resident on the current device at once (SMs x 8).
+long long phase_resident_slots();
 cudaError_t row_histogram(const DeviceCRS& A, int* hist33_host, int* max_row, cudaStream_t s);
 
 // SpMV y = A x with the autotuned layout (device pointers).

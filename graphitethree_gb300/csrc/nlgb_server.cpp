@@ -970,8 +970,16 @@ void worker_streams(nlgb_server_s* S) {
     int k = -1;
     long long iter_before = 0;
     double t_free = -1.0;       // server clock when the lane's last chunk was seen done (tracing)
+    long long ctas = 0;         // CTAs per phase kernel of the running system
   };
   std::vector<Lane> lanes((size_t)ns);
+  // CTA budget of the chunks in flight (config.chunk_cta_budget; 0: none)
+  const long long cta_cap = S->cfg.chunk_cta_budget < 0 ? phase_resident_slots()
+                                                        : (long long)S->cfg.chunk_cta_budget;
+  long long running_ctas = 0;
+  auto ctas_of = [](const Req* r) {
+    return ((long long)r->A.n + r->A.tile_rows - 1) / std::max(1, r->A.tile_rows);
+  };
   int least = 0, greatest = 0;
   cudaDeviceGetStreamPriorityRange(&least, &greatest);
   cudaStream_t su = nullptr;   // aborts and failures: result downloads and releases
@@ -1059,6 +1067,8 @@ void worker_streams(nlgb_server_s* S) {
     l.r = nullptr;
     l.k = -1;
     l.m = nullptr;
+    running_ctas -= l.ctas;
+    l.ctas = 0;
     busy_change(-1);
   };
   // requests whose systems are all done go to the completion threads
@@ -1137,6 +1147,9 @@ void worker_streams(nlgb_server_s* S) {
       for (Req* r : S->active)
         for (int k = 0; k < r->n_rhs; ++k) {
           if (r->sys_done[k] || r->running[k]) continue;
+          // within the CTA budget (a system that does not fit waits; the
+          // least-work one that fits runs meanwhile)
+          if (cta_cap > 0 && running_ctas > 0 && running_ctas + ctas_of(r) > cta_cap) continue;
           const double key = r->est_left[k] < 0.0 ? -1.0 : r->est_left[k] * r->iter_cost;
           if (!best || key < bkey || (key == bkey && r->id < best->id)) { best = r; bk = k; bkey = key; }
         }
@@ -1159,6 +1172,8 @@ void worker_streams(nlgb_server_s* S) {
       l.iter_before = best->sys_iter[bk];
       l.seq0 = mirror_seq(m);
       best->running[bk] = 1;
+      l.ctas = ctas_of(best);
+      running_ctas += l.ctas;
       // the budget is read by the chunk's first kernel
       __atomic_store_n(&m->budget, iters, __ATOMIC_RELEASE);
       const double tr = S->now();
@@ -1323,6 +1338,7 @@ void nlgb_server_default_config(nlgb_server_config* c) {
   c->streams = 16;
   c->eps_least_squares = 0.0;
   c->min_tile_rows = 0;
+  c->chunk_cta_budget = 0;
 }
 
 nlgb_server nlgb_server_create(const nlgb_server_config* cfg) {

@@ -672,6 +672,7 @@ static long long resident_slots() {
   }
   return 8LL * sms;
 }
+long long phase_resident_slots() { return resident_slots(); }
 
 // CTAs of the single-kernel iteration k_iter<T> resident at once (0 if the
 // occupancy cannot be queried).

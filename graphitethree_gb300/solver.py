@@ -199,7 +199,7 @@ class Server:
                  eps: float = 1e-10, epoch_iters: int = 256, inner_eps: float = 0.1,
                  max_systems: int = 8192, max_iter: int = -1, schedule: str = "srpt",
                  epoch_ms: float = 10.0, streams: int = 16, eps_least_squares: float = 0.0,
-                 min_tile_rows: int = 0):
+                 min_tile_rows: int = 0, chunk_cta_budget: int = 0):
         L = _lib.load()
         cfg = _lib.NlgbServerConfig()
         L.nlgb_server_default_config(ctypes.byref(cfg))
@@ -216,6 +216,7 @@ class Server:
         cfg.streams = streams
         cfg.eps_least_squares = eps_least_squares
         cfg.min_tile_rows = min_tile_rows
+        cfg.chunk_cta_budget = chunk_cta_budget
         h = L.nlgb_server_create(ctypes.byref(cfg))
         if not h:
             raise SolverError(f"nlgb_server_create failed: {_lib.last_error()}")

@@ -232,6 +232,19 @@ typedef struct {
                                     and in any mix; against nlgb_solve they
                                     are bit-identical when the matrix has the
                                     same layout (nlgb_matrix_set_layout).   */
+    int       chunk_cta_budget;  /* batched SRPT server: a chunk starts only
+                                    while the phase-kernel CTAs of the chunks
+                                    in flight, its own included, stay within
+                                    this many (the first chunk always starts).
+                                    0 (default): no limit; < 0: one resident
+                                    wave of the phase kernels (SMs x 8).  With
+                                    one wave, large systems no longer share
+                                    the GPU many ways and finish sooner: on the
+                                    serving stream 20 % more requests
+                                    completed over 60 s and 6 % more in the
+                                    4-s window (32 streams, tiles of at least
+                                    2,048 rows).  Scheduling only: results do
+                                    not change.                              */
 } nlgb_server_config;
 
 typedef struct {

@@ -103,7 +103,8 @@ def test_least_squares_tolerance_applies_to_lscm_only(gpu_ok, mode):
 @pytest.mark.parametrize("schedule", ["srpt", "all"])
 def test_min_tile_rows_changes_only_the_layout(gpu_ok, schedule):
     """min_tile_rows: the batched server cuts each system into tiles of at
-    least that many rows.  Results are bit-identical alone and in the mix,
+    least that many rows; chunk_cta_budget holds back chunks that would not
+    fit the budget.  Results are bit-identical alone and in the mix,
     and equal the single-system solver's on a matrix given the same layout;
     a system smaller than one tile runs as a single tile."""
     reqs = _requests()
@@ -113,8 +114,9 @@ def test_min_tile_rows_changes_only_the_layout(gpu_ok, schedule):
         x, infos, _ = srv.wait(_submit(srv, kind, obj))
         alone.append((x.copy(), [i.iterations for i in infos]))
         srv.close()
+    # a CTA budget of 8 lets only a few of these 1-10-tile systems run at once
     srv = solver.Server(precision="auto", budget_bytes=2e9, min_tile_rows=1024, epoch_iters=64,
-                        schedule=schedule, epoch_ms=0.5)
+                        schedule=schedule, epoch_ms=0.5, chunk_cta_budget=8)
     tickets = [_submit(srv, kind, obj, arrival=0.002 * i) for i, (kind, obj) in enumerate(reqs)]
     for t, (xa, ia) in zip(tickets, alone):
         x, infos, _ = srv.wait(t)
