@@ -93,10 +93,11 @@ def parse_args():
     p.add_argument("--lead", type=float, default=1.5,
                    help="submission lead time before the window opens (s; not timed)")
     p.add_argument("--eps", type=float, default=1e-10)
-    p.add_argument("--eps-lsq", type=float, default=3e-11,
+    p.add_argument("--eps-lsq", type=float, default=1e-11,
                    help="relative residual of the least-squares (LSCM) requests, every arm: the "
-                        "normal equations square kappa, and at 1e-10 a few LSCM solutions of the "
-                        "stream sit just above 1e-8 from the direct solve")
+                        "normal equations square kappa; at 1e-10 (and at 3e-11 for the larger "
+                        "ones) a few LSCM solutions of the stream sit just above 1e-8 from the "
+                        "direct solve")
     p.add_argument("--budget-gb", type=float, default=150.0)
     p.add_argument("--plain-steps", type=int, default=2, help="steps of the serial plain-FP64 arm")
     p.add_argument("--streams", type=int, default=32, help="concurrent chunk streams of the batched server")
