@@ -15,7 +15,8 @@
 // all calls share the one array and each call overwrites it, so calls that
 // overlap on the GPU (several host threads, or several streams) race -- the
 // caller must serialise them.  The first call on a device looks up the
-// array's device address (cudaGetSymbolAddress) with that device current.
+// array's device address (cudaGetSymbolAddress) with that device current;
+// that first call belongs before any stream capture.
 #include "../../include/nl.h"
 #include "../../include/nl_gb300.h"
 #include "nlgb_core.cuh"

@@ -147,8 +147,10 @@ int nlgb_batch_solve(int n_sys, const nlgb_matrix* A, const double* const* b, do
  * one static device array of the library (8.1 MiB per GPU, kept until the
  * process exits), so n is limited to 262144 rows (larger n: NLGB_E_INVALID).
  * The first call on a device looks up the array's address with that device
- * current.  Every call reuses the same array: calls that overlap on the GPU
- * race and must be serialised by the caller.  stream: a cudaStream_t (NULL:
+ * current (cudaGetSymbolAddress); make that first call before any stream
+ * capture begins.  Every call reuses the same array and clears what must
+ * start at zero: calls that overlap on the GPU race and must be serialised
+ * by the caller.  stream: a cudaStream_t (NULL:
  * the default stream); the call returns when the solve is finished
  * (res->seconds: host time of the call).  n == 0 returns at once
  * (converged). */
